@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark of the plain single-solve RK4 step: 3D Taylor-Green vortex,
+compressible Euler, gamma 1.4, periodic [0, 2 pi)^3 Fourier grid 256^3,
+float32 state, 2/3 dealiasing, RK4 with fixed dt = 1e-3.
+
+One "step" is one full RK4 step (four right-hand-side evaluations, the
+end-of-step filter) of the whole grid; the metric is cell-updates/s (grid
+nodes advanced by one RK4 step per second).  Inputs (the state and the pass
+intermediates, ~2.7 GB) are far larger than the 129 MB L2, so no flush is
+needed between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank advances its own replica (a single solve
+does not shard); the value is the total cell-updates of all ranks over the
+slowest rank's time.  ``--impl reference`` times the CPU restatement of the
+reference algorithm (float64 NumPy/SciPy FFT, all host cores) on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "cell-updates/s vs plain; ensemble solves/s, p50/p99 latency at rel-L2 err≤1e-5"
+UNIT = "cell-updates/s"
+DT = 1e-3
+PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_config(n: int, world: int) -> dict:
+    return {
+        "workload": f"3D Taylor-Green vortex, compressible Euler, {n}^3 periodic Fourier, RK4 dt={DT}",
+        "grid": [n, n, n],
+        "state_dtype": "float32",
+        "dealias": "2/3",
+        "filter": "off (mask-only end-of-step filter applied every step)",
+        "cells_per_step": n ** 3,
+        "l2_policy": "inputs larger than L2 (state + pass intermediates ~2.7 GB >> 129 MB)",
+        "parallelism": f"replicas x{world}" if world > 1 else "single solve",
+    }
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_from_profiles(kind: str):
+    """DRAM bytes per launch of a pass kind, from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "tgv256_passes.md")
+    try:
+        for line in open(path):
+            if line.startswith(f"traffic_bytes_per_launch[{kind}]"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_step_rate(n: int, max_steps: int, budget_s: float):
+    """Time the float64 CPU restatement of the reference step at n^3."""
+    from oracle import spectral as O
+    from phrike_gb300 import problems
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("PHRIKE_ORACLE_WORKERS", str(cores))
+    s = O.EulerSolver(O.FourierBox((n, n, n), (2 * np.pi,) * 3, dealias=True), cfl=0.25)
+    U = problems.taylor_green_3d(n)
+    done, t_total = 0, 0.0
+    while done < max_steps:
+        t0 = time.perf_counter()
+        U = s.step(U, DT)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total >= budget_s:
+            break
+    return n ** 3 * done / t_total, done, t_total, cores
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    n = args.n
+    # bounded sample: at most 1 warm-up and 3 timed full RK4 steps at n^3
+    from oracle import spectral as O  # noqa: F401  (checker import only)
+    if args.warmup > 0:
+        cpu_oracle_step_rate(n, 1, 0.0)
+    rate, done, t_total, cores = cpu_oracle_step_rate(n, max(1, min(args.steps, 3)), 120.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+        "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * t_total / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic Taylor-Green initial condition)",
+        "config": workload_config(n, 1),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{done} full RK4 step(s) at {n}^3 (float64 NumPy/SciPy FFT restatement "
+                                   f"of the reference, scipy.fft workers={cores})"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank: int, world: int):
+    import torch
+    import torch.distributed as dist
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.engine import Plan
+
+    _build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    n = args.n
+    cells = n ** 3
+    plan = Plan((n, n, n), (2 * np.pi,) * 3, device=device)
+    U0h = torch.from_numpy(problems.taylor_green_3d(n).astype(np.float32))
+    U = U0h.to(device)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # warm-up
+    plan.run_(U, args.warmup, DT)
+    torch.cuda.synchronize()
+
+    # timed region: K steps, device-resident state
+    sampler = ClockSampler(local)
+    plan.profile(True)
+    plan.collect_profile()
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    stream = torch.cuda.current_stream(device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.run_(U, args.steps, DT)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    prof = plan.collect_profile()
+    plan.profile(False)
+    finite = bool(torch.isfinite(U).all().item())
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = cells * args.steps * world / (ms_max * 1e-3)
+
+    # end-to-end through the public API with host buffers: per step, H2D of
+    # the state from pinned memory, one RK4 step, D2H of the new state.
+    e2e_steps = max(1, min(args.steps, 10))
+    hin = U0h.pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    Ud = torch.empty_like(U)
+    for _ in range(2):  # warm-up of the copy path
+        Ud.copy_(hin, non_blocking=True)
+        plan.step_(Ud, DT)
+        hout.copy_(Ud, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Ud.copy_(hin, non_blocking=True)
+        plan.step_(Ud, DT)
+        hout.copy_(Ud, non_blocking=True)
+        torch.cuda.current_stream(device).synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = cells * e2e_steps * world / float(te.item())
+    state_bytes = U.numel() * 4
+
+    if rank != 0:
+        return
+    # roofline of the dominant pass kernel (largest share of device time)
+    peak, peak_kind = hbm_peak()
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    per_launch_ms = d["ms"] / d["launches"]
+    per_launch_bytes = d["bytes"] / d["launches"]
+    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+    total_ms = sum(v["ms"] for v in prof.values())
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+        "traffic": traffic_from_profiles(dom), "algorithmic_bytes_per_launch": per_launch_bytes,
+        "launch_ms": per_launch_ms,
+        "kernels": {k: {"launches": v["launches"], "share": v["ms"] / total_ms,
+                        "achieved_GBps": v["bytes"] / (v["ms"] * 1e-3) / 1e9}
+                    for k, v in prof.items()},
+        "step_GBps": sum(v["bytes"] for v in prof.values()) / (ms * 1e-3) / 1e9,
+    }
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        rate, done, t_total, cores = cpu_oracle_step_rate(n, 1, 0.0)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{done} full RK4 step at {n}^3, {t_total:.1f} s (float64 NumPy/SciPy FFT "
+                         f"restatement of the reference, scipy.fft workers={cores})"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (analytic Taylor-Green initial condition)",
+        "config": workload_config(n, world),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes, "steps": e2e_steps,
+                "path": "phrike_gb300.engine.Plan.step_ -> ps_step_rk4 (C ABI) with pinned host state"},
+        "gpu_launches": sum(v["launches"] for v in prof.values()),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "state_finite": finite,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend=backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gb300(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

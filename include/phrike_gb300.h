@@ -1,0 +1,139 @@
+/*
+ * phrike_gb300 — C ABI of the GB300 pseudo-spectral Euler step engine.
+ *
+ * Every entry point takes plain pointers (device pointers for field data),
+ * sizes and a CUDA stream handle passed as void* (a cudaStream_t; NULL is the
+ * legacy default stream), and returns an int status (PS_OK = 0).  On failure
+ * ps_last_error() returns a thread-local message.  Field arrays are float32,
+ * component-first and C-contiguous: (ncomp, [Nz,] [Ny,] Nx), x fastest — the
+ * layout of the reference's state arrays (phrike/grid.py:779-780, 1361).
+ *
+ * Each declaration names the reference interface it replaces (paths inside
+ * the reference project, file:line).  A Python binding over ctypes lives in
+ * phrike_gb300/_lib.py.
+ */
+#ifndef PHRIKE_GB300_H
+#define PHRIKE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PS_OK 0
+#define PS_ERR_INVALID 1     /* bad argument, null pointer, inconsistent descriptor */
+#define PS_ERR_UNSUPPORTED 2 /* grid size / basis / equation set not supported     */
+#define PS_ERR_CUDA 3        /* CUDA runtime error                                  */
+#define PS_ERR_OOM 4         /* device allocation failed                            */
+
+/* basis per axis */
+#define PS_BASIS_FOURIER 0
+#define PS_BASIS_LEGENDRE 1
+
+/* equation sets */
+#define PS_EQ_EULER 0
+
+typedef struct ps_plan_s* ps_plan;
+
+/*
+ * One solve: grid, basis, equations and step options.
+ * Mirrors the constructor arguments of Grid1D/2D/3D (grid.py:170-181,
+ * 782-797, 1364-1376), EulerEquations1D/2D/3D(gamma) (equations.py:217,
+ * 322, 551) and SpectralSolver1D/2D/3D (solver.py:156, 565, 1262).
+ */
+typedef struct {
+  int ndim;              /* 1, 2 or 3                                         */
+  int n[3];              /* points along x, y, z (unused axes: 1)             */
+  double length[3];      /* Lx, Ly, Lz                                        */
+  int basis[3];          /* PS_BASIS_*                                        */
+  int equations;         /* PS_EQ_*                                           */
+  double gamma;          /* adiabatic index                                   */
+  int dealias;           /* 2/3-rule mask (grid.py:47-54)                     */
+  int filter_enabled;    /* exponential filter (grid.py:57-63)                */
+  int filter_p;          /* filter order p                                    */
+  double filter_alpha;   /* filter strength alpha                             */
+  int filter_interval;   /* cadence of the end-of-step filter (1D/2D)         */
+  double gravity[3];     /* constant gravity (solver.py:82-91); 0 = off       */
+  double cfl;            /* CFL number for ps_compute_dt                      */
+} ps_plan_desc;
+
+/* Fill a descriptor with the reference defaults for `ndim` (dealias on,
+ * filter off with p=8, alpha=36, interval 1, gamma 1.4, cfl 0.4/0.3/0.25). */
+int ps_plan_desc_init(ps_plan_desc* desc, int ndim);
+
+/* Device scratch a plan allocates at creation (bytes), for HBM admission. */
+int ps_plan_scratch_bytes(const ps_plan_desc* desc, size_t* bytes);
+
+/* Build spectral tables and allocate scratch on the current device.
+ * Replaces Grid*.__post_init__ + _setup_fourier_backend (grid.py:183-383,
+ * 806-992, 1378-1495) and solver construction (solver.py:156-232). */
+int ps_plan_create(const ps_plan_desc* desc, ps_plan* out);
+int ps_plan_destroy(ps_plan plan);
+
+/* rhs = -(sum_a d/dx_a F_a(U)) for U (ncomp fields).  Replaces
+ * _compute_rhs / _compute_rhs_2d / _compute_rhs_3d (solver.py:62-93,
+ * 428-466, 1177-1208). */
+int ps_rhs(ps_plan plan, const float* U, float* rhs, void* stream);
+
+/* One fixed-dt RK4 step in place, including the positivity clamp (1D/2D)
+ * and the end-of-step filter with the reference cadence.  Replaces
+ * SpectralSolver*.step / _fixed_step (solver.py:242-269, 623-648,
+ * 1313-1337).  If d_dt is non-NULL the step size is read from device memory
+ * (one double) and `dt` is ignored, so the call can be captured in a graph. */
+int ps_step_rk4(ps_plan plan, float* U, double dt, const double* d_dt, void* stream);
+
+/* nsteps fixed-dt RK4 steps in place (same semantics as nsteps calls of
+ * ps_step_rk4; consecutive steps share fused filter passes). */
+int ps_run_steps(ps_plan plan, float* U, int nsteps, double dt, const double* d_dt, void* stream);
+
+/* out = dx1/dy1/dz1(f) for nfields fields (axis 0 = x).  Replaces
+ * Grid1D.dx1 (grid.py:512-522), Grid2D.dx1/dy1 (grid.py:1226-1252),
+ * Grid3D.dx1/dy1/dz1 (grid.py:1705-1721). */
+int ps_derivative(ps_plan plan, int axis, const float* f, float* out, int nfields, void* stream);
+
+/* out = apply_spectral_filter(f) for nfields fields (may alias).  Replaces
+ * Grid*.apply_spectral_filter (grid.py:524-538, 1254-1287, 1723-1726). */
+int ps_filter(ps_plan plan, const float* f, float* out, int nfields, void* stream);
+
+/* *d_out (device float) = max wave speed of U with the reference's
+ * per-dimension rule.  Replaces Euler*.max_wave_speed (equations.py:297-301,
+ * 365-370, 609-620).  The result stays on the device. */
+int ps_max_wave_speed(ps_plan plan, const float* U, float* d_out, void* stream);
+
+/* d_out (device doubles, ncomp values: mass, momenta..., energy) = plain
+ * sums of the conserved quantities, accumulated in float64.  Replaces the
+ * solvers' record() (solver.py:372-377, 741-767, 1439-1468). */
+int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);
+
+/* Launch profiling: when enabled, every pass launch is bracketed by CUDA
+ * events on its stream and tagged with its kind and the algorithmic bytes it
+ * moves.  ps_profile_collect waits for the recorded events, fills per-kind
+ * launch counts, elapsed milliseconds and bytes (arrays of nkinds entries,
+ * indexed by PS_KIND_*) and clears the log.  No reference counterpart: the
+ * reference has no built-in tracing (its timings are ad-hoc perf_counter
+ * calls, benchmark_tracers.py:64-75). */
+#define PS_KIND_X 0      /* x pass: flux + D_x / P_x               */
+#define PS_KIND_Y 1      /* 3D y pass                              */
+#define PS_KIND_LAST 2   /* last pass: rhs + RK4 stage (+ filter)  */
+#define PS_KIND_OP 3     /* one-axis operator / filter pass        */
+#define PS_KIND_STEP1D 4 /* 1D whole-step kernel                   */
+#define PS_NKINDS 5
+int ps_profile_enable(ps_plan plan, int enable);
+int ps_profile_collect(ps_plan plan, int nkinds, int* launches, double* ms, double* bytes);
+
+/* Number of state components (ndim + 2 for Euler). */
+int ps_plan_ncomp(ps_plan plan);
+
+/* Thread-local message of the last failed call ("" if none). */
+const char* ps_last_error(void);
+
+/* Library version string. */
+const char* ps_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHRIKE_GB300_H */

@@ -1,0 +1,93 @@
+"""ctypes binding of the C ABI in include/phrike_gb300.h.
+
+Field data crosses the boundary as raw device pointers (``tensor.data_ptr()``)
+and the stream as ``torch.cuda.current_stream().cuda_stream``.  A non-zero
+status becomes a RuntimeError carrying ``ps_last_error()``.  There is no
+fallback: if the library is missing, loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libphrike_gb300.so")
+
+PS_OK = 0
+PS_BASIS_FOURIER = 0
+PS_BASIS_LEGENDRE = 1
+PS_EQ_EULER = 0
+KIND_NAMES = ["x_pass", "y_pass", "last_pass", "op_pass", "step1d"]
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int),
+        ("n", C.c_int * 3),
+        ("length", C.c_double * 3),
+        ("basis", C.c_int * 3),
+        ("equations", C.c_int),
+        ("gamma", C.c_double),
+        ("dealias", C.c_int),
+        ("filter_enabled", C.c_int),
+        ("filter_p", C.c_int),
+        ("filter_alpha", C.c_double),
+        ("filter_interval", C.c_int),
+        ("gravity", C.c_double * 3),
+        ("cfl", C.c_double),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point
+_SIGNATURES = [
+    ("ps_plan_desc_init", C.c_int, [C.POINTER(PlanDesc), C.c_int]),
+    ("ps_plan_scratch_bytes", C.c_int, [C.POINTER(PlanDesc), C.POINTER(C.c_size_t)]),
+    ("ps_plan_create", C.c_int, [C.POINTER(PlanDesc), C.POINTER(C.c_void_p)]),
+    ("ps_plan_destroy", C.c_int, [C.c_void_p]),
+    ("ps_rhs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_step_rk4", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    ("ps_run_steps", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
+    ("ps_derivative", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("ps_filter", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("ps_max_wave_speed", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_conserved", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_plan_ncomp", C.c_int, [C.c_void_p]),
+    ("ps_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]),
+    ("ps_last_error", C.c_char_p, []),
+    ("ps_version", C.c_char_p, []),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def exported_names():
+    return [n for n, _, _ in _SIGNATURES]
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load the shared library (build it first with phrike_gb300._build.build())."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{path} not found: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        lib = C.CDLL(path)
+        for name, res, args in _SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(rc: int) -> None:
+    if rc != PS_OK:
+        msg = load().ps_last_error().decode(errors="replace")
+        raise RuntimeError(f"phrike_gb300 error {rc}: {msg}")

@@ -1,0 +1,161 @@
+// 1D Fourier Euler: whole RK4 steps in one launch, one CTA per solve.
+//
+// Follows SpectralSolver1D._fixed_step / _rk4_step / _compute_rhs
+// (phrike/solver.py:62-132, 259-269):
+//   k_i = -D_x F(U_i)               (flux equations.py:67-86, D = i k m s)
+//   U_{i+1} = clamp(U + c_i dt k_i) (clamp solver.py:32-59, floors 1e-10/1e-12)
+//   U_new = clamp(U + dt/6 (k1 + 2 k2 + 2 k3 + k4)), then the filter P_x is
+//   applied inside the step and once more by the cadence counter.
+// The three state tiles (U^n, stage input, accumulator) stay in shared
+// memory for all nsteps, so a launch touches HBM only to load and store U.
+#pragma once
+#include "pass_common.cuh"
+
+namespace ps {
+
+struct Step1DArgs {
+  float* U;           // [nsolve][3][N]
+  long solve_stride;  // elements between solves
+  AxisOps ax;
+  int nsteps;
+  const double* dt_dev;  // if non-null, dt = *dt_dev (one value for all solves)
+  double dt;
+  float gamma;
+  float rho_min, p_min;
+  int filter_interval;
+  int step_counter0;     // cadence counter value before the first step
+  float gx;              // gravity along x (0 when disabled)
+};
+
+template <int N>
+struct Step1DSmem {
+  AxisSmem<N> ax;
+  float2 buf[Pencil<N, 1, false>::BUF];
+  float un[3 * N];
+  float us[3 * N];
+  float acc[3 * N];
+};
+
+template <int N>
+__global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  using PF = Pencil<N, 1, false>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  auto& S = *reinterpret_cast<Step1DSmem<N>*>(smem_raw);
+  const int t = threadIdx.x;
+  PF pf{0, t, S.buf, S.ax.twf, S.ax.twi};
+  load_axis<N>(S.ax, a.ax);
+  float* U = a.U + (long)blockIdx.x * a.solve_stride;
+  // private slots: (c*B + n2)*A + t  <-> position t + A*n2
+  auto sl = [&](int c, int n2) { return (c * B + n2) * A + t; };
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      const float v = U[c * N + t + A * n2];
+      S.un[sl(c, n2)] = v;
+      S.us[sl(c, n2)] = v;
+    }
+  __syncthreads();
+  const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
+  const float g1 = a.gamma - 1.0f;
+
+  auto filter_pair = [&](float2 (&w)[B]) {
+    pf.fwd(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const float s = S.ax.P[pf.kidx(r)];
+      w[r].x *= s;
+      w[r].y *= s;
+    }
+    pf.inv(w);
+  };
+
+#pragma unroll 1
+  for (int step = 0; step < a.nsteps; ++step) {
+#pragma unroll 1
+    for (int stage = 0; stage < 4; ++stage) {
+      const RKCoef rc = rk4_coef(stage, dt);
+      float2 w01[B], w2[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const float rho = S.us[sl(0, n2)], m = S.us[sl(1, n2)], E = S.us[sl(2, n2)];
+        const float u = m / rho;
+        const float p = g1 * (E - 0.5f * rho * u * u);
+        const float mom = rho * u;
+        w01[n2] = make_float2(mom, mom * u + p);
+        w2[n2] = make_float2((E + p) * u, 0.0f);
+      }
+      // k = -i d FFT(F): multiply by -i d
+      pf.fwd(w01);
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float dd = S.ax.d[pf.kidx(r)];
+        w01[r] = make_float2(w01[r].y * dd, -w01[r].x * dd);
+      }
+      pf.inv(w01);
+      pf.fwd(w2);
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float dd = S.ax.d[pf.kidx(r)];
+        w2[r] = make_float2(w2[r].y * dd, -w2[r].x * dd);
+      }
+      pf.inv(w2);
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        float k[3] = {w01[n2].x, w01[n2].y, w2[n2].x};
+        if (a.gx != 0.0f) {  // gravity source (solver.py:82-91)
+          const float rho = S.us[sl(0, n2)];
+          const float u = S.us[sl(1, n2)] / rho;
+          k[1] += rho * a.gx;
+          k[2] += rho * a.gx * u;
+        }
+        float u3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int s = sl(c, n2);
+          if (stage == 3) {
+            u3[c] = fmaf(rc.wacc, k[c], S.acc[s]);
+          } else {
+            const float un = S.un[s];
+            const float ac = (stage == 0) ? un : S.acc[s];
+            S.acc[s] = fmaf(rc.wacc, k[c], ac);
+            u3[c] = fmaf(rc.wnext, k[c], un);
+          }
+        }
+        clamp_state<1>(u3, a.gamma, a.rho_min, a.p_min);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S.us[sl(c, n2)] = u3[c];
+      }
+    }
+    // end of step: filter inside the RK step, then again by cadence
+    const bool second = ((a.step_counter0 + step) % a.filter_interval) == 0;
+    float2 w01[B], w2[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      w01[n2] = make_float2(S.us[sl(0, n2)], S.us[sl(1, n2)]);
+      w2[n2] = make_float2(S.us[sl(2, n2)], 0.0f);
+    }
+    filter_pair(w01);
+    filter_pair(w2);
+    if (second) {
+      filter_pair(w01);
+      filter_pair(w2);
+    }
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      const float v[3] = {w01[n2].x, w01[n2].y, w2[n2].x};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        S.un[sl(c, n2)] = v[c];
+        S.us[sl(c, n2)] = v[c];
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) U[c * N + t + A * n2] = S.un[sl(c, n2)];
+}
+
+}  // namespace ps

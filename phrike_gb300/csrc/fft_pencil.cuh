@@ -1,0 +1,242 @@
+// Register-resident pencil FFTs for the pseudo-spectral pass kernels.
+//
+// A pencil of N = A*B complex points is owned by A threads.  The forward
+// transform is a two-step (four-step without the explicit transpose pass)
+// decomposition:
+//   input layout    : thread t holds x[t + A*n2],         n2 = 0..B-1
+//   step 1          : B-point DFT in registers, twiddle W_N^{t*k2}
+//   exchange        : one shared-memory transpose
+//   step 2          : B/A A-point DFTs per thread
+//   spectral layout : register j*A+k1 of thread t holds X[(t + A*j) + B*k1]
+// The inverse runs the same steps backwards and returns to the input layout,
+// so a forward/multiply/inverse round trip never reorders data in memory.
+//
+// All in-register DFTs are radix-2 decimation-in-frequency with compile-time
+// twiddles; the constants are produced at compile time by a Taylor series
+// after octant reduction (see ct_cos2pi / ct_sin2pi).
+#pragma once
+#include <cuda_runtime.h>
+#include <type_traits>
+#include <utility>
+
+namespace ps {
+
+// ---------------------------------------------------------------- constexpr trig
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+constexpr double taylor_sin(double x) {
+  double term = x, sum = x;
+  for (int n = 1; n < 16; ++n) {
+    term *= -x * x / double((2 * n) * (2 * n + 1));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double taylor_cos(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int n = 1; n < 16; ++n) {
+    term *= -x * x / double((2 * n - 1) * (2 * n));
+    sum += term;
+  }
+  return sum;
+}
+// cos/sin of 2*pi*num/den, reduced to [0, pi/4] by octant with exact integer
+// arithmetic on the residual.
+constexpr void cs2pi(long num, long den, double& c, double& s) {
+  long r = ((num % den) + den) % den;
+  long q = (8 * r) / den;                                     // octant 0..7
+  double phi = kPi * double(8 * r - q * den) / double(4 * den);        // [0, pi/4)
+  double psi = kPi * double((q + 1) * den - 8 * r) / double(4 * den);  // pi/4 - phi
+  double Cp = taylor_cos(phi), Sp = taylor_sin(phi);
+  double Cq = taylor_cos(psi), Sq = taylor_sin(psi);
+  switch (q) {
+    case 0: c = Cp; s = Sp; break;
+    case 1: c = Sq; s = Cq; break;
+    case 2: c = -Sp; s = Cp; break;
+    case 3: c = -Cq; s = Sq; break;
+    case 4: c = -Cp; s = -Sp; break;
+    case 5: c = -Sq; s = -Cq; break;
+    case 6: c = Sp; s = -Cp; break;
+    default: c = Cq; s = -Sq; break;
+  }
+}
+constexpr double ct_cos2pi(long num, long den) { double c = 0, s = 0; cs2pi(num, den, c, s); return c; }
+constexpr double ct_sin2pi(long num, long den) { double c = 0, s = 0; cs2pi(num, den, c, s); return s; }
+
+// ---------------------------------------------------------------- static_for
+template <int I, int E, typename F>
+__device__ __forceinline__ void sfor(F&& f) {
+  if constexpr (I < E) {
+    f(std::integral_constant<int, I>{});
+    sfor<I + 1, E>(f);
+  }
+}
+
+constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+constexpr int bitrev(int i, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
+  return r;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+
+// d * exp(-+ 2 pi i J / M)   (forward sign -, inverse sign +)
+template <int M, int J, bool INV>
+__device__ __forceinline__ float2 twmul(float2 d) {
+  if constexpr (J == 0) {
+    return d;
+  } else if constexpr (4 * J == M) {
+    return INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+  } else if constexpr (8 * J == M) {
+    constexpr float r = 0.70710678118654752440f;
+    return INV ? make_float2((d.x - d.y) * r, (d.y + d.x) * r)
+               : make_float2((d.x + d.y) * r, (d.y - d.x) * r);
+  } else if constexpr (8 * J == 3 * M) {
+    constexpr float r = 0.70710678118654752440f;
+    return INV ? make_float2((-d.x - d.y) * r, (d.x - d.y) * r)
+               : make_float2((d.y - d.x) * r, (-d.y - d.x) * r);
+  } else {
+    constexpr float c = (float)ct_cos2pi(J, M);
+    constexpr float s = (float)ct_sin2pi(J, M);
+    return INV ? make_float2(fmaf(d.x, c, -d.y * s), fmaf(d.y, c, d.x * s))
+               : make_float2(fmaf(d.x, c, d.y * s), fmaf(d.y, c, -d.x * s));
+  }
+}
+
+// In-register DFT of L points starting at v[OFF]; natural order in and out.
+template <int L, bool INV, int OFF = 0, int CAP>
+__device__ __forceinline__ void dft(float2 (&v)[CAP]) {
+  if constexpr (L > 1) {
+    constexpr int LOG = ilog2(L);
+    sfor<0, LOG>([&](auto sc) {
+      constexpr int span = L >> (decltype(sc)::value + 1);
+      sfor<0, L / (2 * span)>([&](auto gc) {
+        constexpr int start = OFF + decltype(gc)::value * 2 * span;
+        sfor<0, span>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          float2 a = v[start + j];
+          float2 b = v[start + j + span];
+          v[start + j] = cadd(a, b);
+          v[start + j + span] = twmul<2 * span, j, INV>(csub(a, b));
+        });
+      });
+    });
+    float2 tmp[L];
+    sfor<0, L>([&](auto ic) { tmp[decltype(ic)::value] = v[OFF + bitrev(decltype(ic)::value, LOG)]; });
+    sfor<0, L>([&](auto ic) { v[OFF + decltype(ic)::value] = tmp[decltype(ic)::value]; });
+  }
+}
+
+// ---------------------------------------------------------------- pencil shapes
+template <int N> struct Shape;
+template <> struct Shape<16> { static constexpr int A = 4, B = 4; };
+template <> struct Shape<32> { static constexpr int A = 4, B = 8; };
+template <> struct Shape<64> { static constexpr int A = 8, B = 8; };
+template <> struct Shape<128> { static constexpr int A = 8, B = 16; };
+template <> struct Shape<256> { static constexpr int A = 16, B = 16; };
+template <> struct Shape<512> { static constexpr int A = 16, B = 32; };
+template <> struct Shape<1024> { static constexpr int A = 32, B = 32; };
+
+// Exchange-buffer layout for T pencils.  Element (q, s) of pencil p, with
+// q in [0,B) and s in [0,A).  In the contiguous-lane layout (the A threads of
+// a pencil are adjacent lanes) each pencil owns a padded block; in the strided
+// layout (lanes run over pencils) pencils are interleaved innermost.  Both are
+// bank-conflict free for the access patterns below.
+template <int N, int T, bool STRIDED>
+struct Pencil {
+  static constexpr int A = Shape<N>::A;
+  static constexpr int B = Shape<N>::B;
+  static constexpr int J = B / A;
+  static_assert(B % A == 0, "pencil shape needs B multiple of A");
+  static constexpr int PAD = STRIDED ? 0 : 1;
+  static constexpr int BUF = T * B * (A + PAD);  // float2 elements
+
+  int p;   // pencil within the tile
+  int t;   // thread within the pencil
+  float2* buf;
+  const float2* twf;  // [B][A]: W_N^{n1 k2}
+  const float2* twi;  // [A][B]: W_N^{-n1 k2}
+
+  __device__ __forceinline__ int xi(int q, int s) const {
+    if constexpr (STRIDED) return (q * A + s) * T + p;
+    else return p * (B * (A + PAD)) + q * (A + PAD) + s;
+  }
+  // spectral index of register r = j*A + k1
+  __device__ __forceinline__ int kidx(int r) const { return t + A * (r / A) + B * (r % A); }
+
+  __device__ __forceinline__ void fwd(float2 (&v)[B]) const {
+    dft<B, false>(v);
+    sfor<1, B>([&](auto kc) {
+      constexpr int k2 = decltype(kc)::value;
+      v[k2] = cmul(v[k2], twf[k2 * A + t]);
+    });
+    __syncthreads();
+    sfor<0, B>([&](auto kc) {
+      constexpr int k2 = decltype(kc)::value;
+      buf[xi(k2, t)] = v[k2];
+    });
+    __syncthreads();
+    sfor<0, J>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      sfor<0, A>([&](auto nc) {
+        constexpr int n1 = decltype(nc)::value;
+        v[j * A + n1] = buf[xi(t + A * j, n1)];
+      });
+      dft<A, false, j * A>(v);
+    });
+  }
+
+  __device__ __forceinline__ void inv(float2 (&v)[B]) const {
+    sfor<0, J>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      dft<A, true, j * A>(v);
+      sfor<1, A>([&](auto nc) {
+        constexpr int n1 = decltype(nc)::value;
+        v[j * A + n1] = cmul(v[j * A + n1], twi[n1 * B + t + A * j]);
+      });
+    });
+    __syncthreads();
+    sfor<0, J>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      sfor<0, A>([&](auto nc) {
+        constexpr int n1 = decltype(nc)::value;
+        buf[xi(t + A * j, n1)] = v[j * A + n1];
+      });
+    });
+    __syncthreads();
+    sfor<0, B>([&](auto kc) {
+      constexpr int k2 = decltype(kc)::value;
+      v[k2] = buf[xi(k2, t)];
+    });
+    dft<B, true>(v);
+  }
+
+  // vn[r] = X[-k(r) mod N] for a pencil in spectral layout.
+  __device__ __forceinline__ void negk(const float2 (&v)[B], float2 (&vn)[B]) const {
+    __syncthreads();
+    sfor<0, B>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      buf[xi(t + A * (r / A), r % A)] = v[r];
+    });
+    __syncthreads();
+    sfor<0, B>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      constexpr int k1 = r % A;
+      const int k2 = t + A * (r / A);
+      const int q = (k2 == 0) ? 0 : (B - k2);
+      const int s = (k2 == 0) ? ((A - k1) % A) : (A - 1 - k1);
+      vn[r] = buf[xi(q, s)];
+    });
+  }
+};
+
+}  // namespace ps

@@ -1,0 +1,6 @@
+// Pass-kernel instantiations for pencils of 1024 points.
+#include "launch.cuh"
+
+namespace ps {
+PS_DEFINE_LAUNCHERS(1024)
+}  // namespace ps

@@ -1,0 +1,6 @@
+// Pass-kernel instantiations for pencils of 16 points.
+#include "launch.cuh"
+
+namespace ps {
+PS_DEFINE_LAUNCHERS(16)
+}  // namespace ps

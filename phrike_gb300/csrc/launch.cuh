@@ -1,0 +1,112 @@
+// Host-side launchers of the pass kernels, one explicit instantiation set per
+// pencil length (kern_n*.cu), dispatched at run time by ps::dispatch_n.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "euler1d.cuh"
+#include "euler_passes.cuh"
+
+namespace ps {
+
+template <int N> cudaError_t launch_xfirst(int nd, const XFirstArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_ymid3(const YMidArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_last(int nd, const LastArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
+
+inline bool supported_n(int n) {
+  return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
+}
+
+// Calls f(std::integral_constant<int, N>) for the supported pencil length n.
+template <typename F>
+cudaError_t dispatch_n(int n, F&& f) {
+  switch (n) {
+    case 16: return f(std::integral_constant<int, 16>{});
+    case 32: return f(std::integral_constant<int, 32>{});
+    case 64: return f(std::integral_constant<int, 64>{});
+    case 128: return f(std::integral_constant<int, 128>{});
+    case 256: return f(std::integral_constant<int, 256>{});
+    case 512: return f(std::integral_constant<int, 512>{});
+    case 1024: return f(std::integral_constant<int, 1024>{});
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename K>
+inline cudaError_t set_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+#define PS_DEFINE_LAUNCHERS(NN)                                                                       \
+  template <>                                                                                         \
+  cudaError_t launch_xfirst<NN>(int nd, const XFirstArgs& a, cudaStream_t s) {                        \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const dim3 grid((a.rows + T - 1) / T);                                                            \
+    const dim3 block(Shape<NN>::A * T);                                                               \
+    cudaError_t e;                                                                                    \
+    if (nd == 3) {                                                                                    \
+      const size_t sm = sizeof(XFirstSmem<NN, T, 3>);                                                 \
+      if ((e = set_smem(k_xfirst<NN, T, 3>, sm)) != cudaSuccess) return e;                            \
+      k_xfirst<NN, T, 3><<<grid, block, sm, s>>>(a);                                                  \
+    } else {                                                                                          \
+      const size_t sm = sizeof(XFirstSmem<NN, T, 2>);                                                 \
+      if ((e = set_smem(k_xfirst<NN, T, 2>, sm)) != cudaSuccess) return e;                            \
+      k_xfirst<NN, T, 2><<<grid, block, sm, s>>>(a);                                                  \
+    }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_ymid3<NN>(const YMidArgs& a, cudaStream_t s) {                                   \
+    constexpr int T = Tile<NN>::TS;                                                                   \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const size_t sm = sizeof(StridedSmem<NN, T>);                                                     \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_ymid3<NN, T>, sm)) != cudaSuccess) return e;                                  \
+    k_ymid3<NN, T><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                             \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_last<NN>(int nd, const LastArgs& a, cudaStream_t s) {                            \
+    constexpr int T = Tile<NN>::TS;                                                                   \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const size_t sm = sizeof(StridedSmem<NN, T>);                                                     \
+    cudaError_t e;                                                                                    \
+    if (nd == 3) {                                                                                    \
+      if ((e = set_smem(k_last<NN, T, 3, false>, sm)) != cudaSuccess) return e;                       \
+      k_last<NN, T, 3, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                  \
+    } else {                                                                                          \
+      if ((e = set_smem(k_last<NN, T, 2, true>, sm)) != cudaSuccess) return e;                        \
+      k_last<NN, T, 2, true><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                   \
+    }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_op<NN>(bool strided, const OpArgs& a, cudaStream_t s) {                          \
+    cudaError_t e;                                                                                    \
+    if (strided) {                                                                                    \
+      constexpr int T = Tile<NN>::TS;                                                                 \
+      const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                            \
+      const size_t sm = sizeof(StridedSmem<NN, T, true>);                                             \
+      if ((e = set_smem(k_op<NN, T, true>, sm)) != cudaSuccess) return e;                             \
+      k_op<NN, T, true><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                        \
+    } else {                                                                                          \
+      constexpr int T = Tile<NN>::TC;                                                                 \
+      const dim3 grid((a.rows + T - 1) / T);                                                          \
+      const size_t sm = sizeof(StridedSmem<NN, T, false>);                                            \
+      if ((e = set_smem(k_op<NN, T, false>, sm)) != cudaSuccess) return e;                            \
+      k_op<NN, T, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                       \
+    }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_step1d<NN>(const Step1DArgs& a, int nsolve, cudaStream_t s) {                    \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
+    k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
+    return cudaGetLastError();                                                                        \
+  }
+
+}  // namespace ps

@@ -1,0 +1,111 @@
+// Shared pieces of the pencil pass kernels: per-axis spectral tables staged in
+// shared memory, tile shapes and small helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_pencil.cuh"
+
+namespace ps {
+
+// Per-axis device tables (built on the host in float64, stored as float).
+//   P[k]  = mask(k) * sigma(k) / N                 projection / filter symbol
+//   d[k]  = kphys(k) * mask(k) * sigma(k) / N      derivative symbol is i*d[k];
+//           d = 0 at the Nyquist index (the reference keeps only the real part
+//           of a full complex inverse transform, which drops that term)
+//   twf   = W_N^{n1*k2}  laid out [k2][n1]   (forward twiddles)
+//   twi   = W_N^{-n1*k2} laid out [n1][k2]   (inverse twiddles)
+struct AxisOps {
+  const float* P;
+  const float* d;
+  const float2* twf;
+  const float2* twi;
+};
+
+// Shared-memory copy of one axis' tables.
+template <int N>
+struct AxisSmem {
+  float P[N];
+  float d[N];
+  float2 twf[N];
+  float2 twi[N];
+};
+
+template <int N>
+__device__ __forceinline__ void load_axis(AxisSmem<N>& s, const AxisOps& ax) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    s.P[i] = ax.P[i];
+    s.d[i] = ax.d[i];
+    s.twf[i] = ax.twf[i];
+    s.twi[i] = ax.twi[i];
+  }
+}
+
+// Pencils per CTA: contiguous passes (pencils along x) and strided passes
+// (pencils along y or z, tiles of adjacent x columns).
+template <int N> struct Tile;
+template <> struct Tile<16> { static constexpr int TC = 32, TS = 16; };
+template <> struct Tile<32> { static constexpr int TC = 32, TS = 16; };
+template <> struct Tile<64> { static constexpr int TC = 16, TS = 16; };
+template <> struct Tile<128> { static constexpr int TC = 16, TS = 16; };
+template <> struct Tile<256> { static constexpr int TC = 8, TS = 16; };
+template <> struct Tile<512> { static constexpr int TC = 4, TS = 16; };
+template <> struct Tile<1024> { static constexpr int TC = 2, TS = 8; };
+
+// Non-negative float max via integer compare (valid for x >= 0).
+__device__ __forceinline__ void atomic_max_nonneg(float* addr, float x) {
+  atomicMax(reinterpret_cast<int*>(addr), __float_as_int(x));
+}
+
+__device__ __forceinline__ float block_max(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (l < nw) ? red[l] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;  // valid in thread 0
+}
+
+// RK4 stage bookkeeping (classical RK4, low-storage accumulator form):
+//   stage 0: acc  = U + dt/6 k;  next = U + dt/2 k
+//   stage 1: acc += dt/3 k;      next = U + dt/2 k
+//   stage 2: acc += dt/3 k;      next = U + dt k
+//   stage 3: new  = acc + dt/6 k
+struct RKCoef {
+  float wacc;   // weight of k in the accumulator
+  float wnext;  // weight of k in the next stage input
+};
+__device__ __forceinline__ RKCoef rk4_coef(int stage, float dt) {
+  RKCoef c;
+  c.wacc = (stage == 0 || stage == 3) ? dt * (1.0f / 6.0f) : dt * (1.0f / 3.0f);
+  c.wnext = (stage == 2) ? dt : 0.5f * dt;
+  return c;
+}
+
+// Conservative -> primitive -> floors -> conservative (the positivity clamp of
+// the 1D/2D solvers).  comps: NC = ND + 2, velocity components ND.
+template <int ND>
+__device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, float rho_min, float p_min) {
+  const float rho = u[0];
+  float vel[ND];
+  float kin = 0.0f;
+#pragma unroll
+  for (int a = 0; a < ND; ++a) {
+    vel[a] = u[1 + a] / rho;
+    kin = fmaf(vel[a], vel[a], kin);
+  }
+  const float p = (gamma - 1.0f) * (u[ND + 1] - 0.5f * rho * kin);
+  const float rc = fmaxf(rho, rho_min);
+  const float pc = fmaxf(p, p_min);
+  u[0] = rc;
+#pragma unroll
+  for (int a = 0; a < ND; ++a) u[1 + a] = rc * vel[a];
+  u[ND + 1] = pc / (gamma - 1.0f) + 0.5f * rc * kin;
+}
+
+}  // namespace ps

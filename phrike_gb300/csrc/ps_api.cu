@@ -1,0 +1,524 @@
+// C ABI of the step engine: plan construction (spectral tables, scratch) and
+// the step / rhs / operator / reduction entry points declared in
+// include/phrike_gb300.h.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/phrike_gb300.h"
+#include "launch.cuh"
+#include "reduce.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char msg[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(PS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define PS_CU(expr, what)                      \
+  do {                                         \
+    cudaError_t _e = (expr);                   \
+    if (_e != cudaSuccess) return cuda_fail(_e, what); \
+  } while (0)
+
+}  // namespace
+
+struct ps_plan_s {
+  ps_plan_desc desc;
+  int nd = 0;
+  int n[3] = {1, 1, 1};
+  long cells = 0;
+  int nc = 0;
+  // per-axis spectral tables (device): P, d, twf, twi
+  float* P[3] = {nullptr, nullptr, nullptr};
+  float* d[3] = {nullptr, nullptr, nullptr};
+  float2* twf[3] = {nullptr, nullptr, nullptr};
+  float2* twi[3] = {nullptr, nullptr, nullptr};
+  // scratch
+  float* G = nullptr;    // X-pass outputs (2D: 8 fields, 3D: 15)
+  float* AB = nullptr;   // 3D Y-pass outputs (10 fields)
+  float* acc = nullptr;  // RK accumulator (nc fields)
+  float* Us = nullptr;   // stage input (nc fields)
+  float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
+  float* speed = nullptr;
+  long step_counter = 0;
+  std::vector<void*> allocations;
+  // launch profiling: CUDA events around every pass launch
+  struct LaunchRec {
+    int kind;
+    double bytes;
+    cudaEvent_t start, stop;
+  };
+  bool profiling = false;
+  std::vector<LaunchRec> launches;
+  std::vector<cudaEvent_t> event_pool;
+
+  ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
+  float* field(float* base, int i) const { return base + (long)i * cells; }
+};
+
+namespace {
+
+// Launch profiling.  begin() records a start event before a pass launch;
+// end() records the stop event and the algorithmic bytes the pass moves.
+cudaEvent_t take_event(ps_plan p) {
+  if (!p->event_pool.empty()) {
+    cudaEvent_t e = p->event_pool.back();
+    p->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct ProfScope {
+  ps_plan p;
+  cudaStream_t s;
+  int kind;
+  double bytes;
+  cudaEvent_t start = nullptr;
+  ProfScope(ps_plan p_, cudaStream_t s_, int kind_, double bytes_) : p(p_), s(s_), kind(kind_), bytes(bytes_) {
+    if (p->profiling) {
+      start = take_event(p);
+      cudaEventRecord(start, s);
+    }
+  }
+  ~ProfScope() {
+    if (p->profiling && start) {
+      cudaEvent_t stop = take_event(p);
+      cudaEventRecord(stop, s);
+      p->launches.push_back({kind, bytes, start, stop});
+    }
+  }
+};
+
+int validate(const ps_plan_desc* d) {
+  if (!d) return fail(PS_ERR_INVALID, "null descriptor");
+  if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
+  if (d->equations != PS_EQ_EULER) return fail(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
+  for (int a = 0; a < d->ndim; ++a) {
+    if (d->basis[a] != PS_BASIS_FOURIER)
+      return fail(PS_ERR_UNSUPPORTED, "axis %d: only the Fourier basis is supported by this plan type", a);
+    if (!ps::supported_n(d->n[a]))
+      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 16..1024)", a, d->n[a]);
+    if (!(d->length[a] > 0.0)) return fail(PS_ERR_INVALID, "axis %d: length must be positive", a);
+  }
+  if (!(d->gamma > 1.0)) return fail(PS_ERR_INVALID, "gamma must exceed 1");
+  if (d->filter_interval < 1) return fail(PS_ERR_INVALID, "filter_interval must be >= 1");
+  return PS_OK;
+}
+
+size_t scratch_fields(int nd) {
+  // G + AB + acc + Us (+ 1D flux)
+  if (nd == 1) return 3;
+  if (nd == 2) return 8 + 4 + 4;
+  return 15 + 10 + 5 + 5;
+}
+
+// Spectral tables of one axis in float64, stored as float (grid.py:47-63 for
+// the mask and filter; wavenumbers 2 pi fftfreq(N, L/N), grid.py:255-257).
+void build_axis(int N, double L, int dealias, int fon, int fp, double falpha, std::vector<float>& P,
+                std::vector<float>& d, std::vector<float2>& twf, std::vector<float2>& twi) {
+  P.resize(N);
+  d.resize(N);
+  twf.resize(N);
+  twi.resize(N);
+  const double kmax = N / 2;  // max |fftfreq(N) * N| for even N
+  for (int k = 0; k < N; ++k) {
+    const int kk = (k < N / 2) ? k : k - N;  // fftfreq ordering, index N/2 -> -N/2
+    const double ak = fabs((double)kk);
+    double m = (!dealias || ak <= (double)(N / 3)) ? 1.0 : 0.0;
+    if (fon) m *= exp(-falpha * pow(ak / (kmax > 1.0 ? kmax : 1.0), fp));
+    P[k] = (float)(m / N);
+    const double kphys = 2.0 * M_PI * kk / L;
+    d[k] = (k == N / 2) ? 0.0f : (float)(kphys * m / N);
+  }
+  const int A = (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
+  const int B = N / A;
+  for (int k2 = 0; k2 < B; ++k2)
+    for (int n1 = 0; n1 < A; ++n1) {
+      const double ang = -2.0 * M_PI * (double)((long)n1 * k2 % N) / N;
+      twf[k2 * A + n1] = make_float2((float)cos(ang), (float)sin(ang));
+      twi[n1 * B + k2] = make_float2((float)cos(ang), (float)-sin(ang));
+    }
+}
+
+template <typename Tp>
+int dalloc(ps_plan p, Tp** ptr, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(Tp));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(Tp), cudaGetErrorString(e));
+  }
+  p->allocations.push_back(q);
+  *ptr = static_cast<Tp*>(q);
+  return PS_OK;
+}
+
+ps::StridedGeom geom_y(const ps_plan_s* p) {
+  // pencils along y: axis stride Nx, outer slabs z (stride Nx*Ny)
+  return ps::StridedGeom{p->n[0], (long)p->n[0], (long)p->n[0] * p->n[1], p->n[2]};
+}
+ps::StridedGeom geom_z(const ps_plan_s* p) {
+  // pencils along z: axis stride Nx*Ny, outer rows y (stride Nx)
+  return ps::StridedGeom{p->n[0], (long)p->n[0] * p->n[1], (long)p->n[0], p->n[1]};
+}
+
+// One-axis operator on nf fields (P or D), axis 0 = x.
+int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s) {
+  ps::OpArgs a{};
+  a.in = in;
+  a.out = out;
+  a.nf = nf;
+  a.fs = p->cells;
+  a.rows = (int)(p->cells / p->n[0]);
+  a.g = (axis == 1) ? geom_y(p) : geom_z(p);
+  a.ax = p->ax(axis);
+  a.deriv = deriv;
+  a.scale = scale;
+  ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells);
+  cudaError_t e = ps::dispatch_n(p->n[axis], [&](auto nc) {
+    return ps::launch_op<decltype(nc)::value>(axis != 0, a, s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "operator pass");
+  return PS_OK;
+}
+
+int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s) {
+  ps::XFirstArgs a{};
+  a.U = U;
+  a.Uw = Uw;
+  a.out = p->G;
+  a.fs = p->cells;
+  a.rows = (int)(p->cells / p->n[0]);
+  a.ax = p->ax(0);
+  a.gamma = (float)p->desc.gamma;
+  a.speed = speed;
+  ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * (p->nc * (Uw ? 2 : 1) + p->nd * p->nc));
+  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
+    return ps::launch_xfirst<decltype(nc)::value>(p->nd, a, s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "x pass");
+  return PS_OK;
+}
+
+int ymid(ps_plan p, cudaStream_t s) {
+  ps::YMidArgs a{};
+  a.in = p->G;
+  a.out = p->AB;
+  a.fs = p->cells;
+  a.g = geom_y(p);
+  a.ax = p->ax(1);
+  ProfScope prof(p, s, PS_KIND_Y, 4.0 * p->cells * 25);
+  cudaError_t e = ps::dispatch_n(p->n[1], [&](auto nc) { return ps::launch_ymid3<decltype(nc)::value>(a, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "y pass");
+  return PS_OK;
+}
+
+int last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
+         cudaStream_t s) {
+  ps::LastArgs a{};
+  const int nc = p->nc;
+  if (p->nd == 3) {
+    a.a = p->AB;
+    a.b = p->AB + (long)5 * p->cells;
+    a.g = geom_z(p);
+    a.ax = p->ax(2);
+  } else {
+    a.a = p->G;
+    a.b = p->G + (long)nc * p->cells;
+    a.g = geom_y(p);
+    a.ax = p->ax(1);
+  }
+  a.fs = p->cells;
+  a.stage = stage;
+  a.Un = Un;
+  a.acc = p->acc;
+  a.out = out;
+  a.dt_dev = d_dt;
+  a.dt = dt;
+  a.gamma = (float)p->desc.gamma;
+  // the 2D kernel clamps (solver.py:467-513); the 3D solver has none (1220-1230)
+  a.rho_min = 1e-8f;               // _positivity_clamp_2d floors (solver.py:467)
+  a.p_min = 1e-10f;
+  a.filter_last = filter_last ? 1 : 0;
+  const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
+  // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
+  const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
+  ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * nc * (2 + st_words));
+  cudaError_t e = ps::dispatch_n(naxis, [&](auto nc2) {
+    return ps::launch_last<decltype(nc2)::value>(p->nd, a, s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "last pass");
+  return PS_OK;
+}
+
+bool filter_due(ps_plan p, long counter) {
+  if (p->nd == 3) return true;  // every step (solver.py:1336)
+  return (counter % p->desc.filter_interval) == 0;
+}
+
+int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cudaStream_t s) {
+  ps::Step1DArgs a{};
+  a.U = U;
+  a.solve_stride = 0;
+  a.ax = p->ax(0);
+  a.nsteps = nsteps;
+  a.dt_dev = d_dt;
+  a.dt = dt;
+  a.gamma = (float)p->desc.gamma;
+  a.rho_min = 1e-10f;  // _positivity_clamp floors (solver.py:32)
+  a.p_min = 1e-12f;
+  a.filter_interval = p->desc.filter_interval;
+  a.step_counter0 = (int)(p->step_counter % p->desc.filter_interval);
+  a.gx = (float)p->desc.gravity[0];
+  ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3);
+  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_step1d<decltype(nc)::value>(a, 1, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "1D step");
+  p->step_counter += nsteps;
+  return PS_OK;
+}
+
+// nsteps RK4 steps for 2D/3D; the x axis of the end-of-step filter of step i
+// is fused into the first x pass of step i+1.
+int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cudaStream_t s) {
+  int rc;
+  bool pending_px = false;
+  for (int it = 0; it < nsteps; ++it) {
+    const bool filt = filter_due(p, p->step_counter);
+    for (int stage = 0; stage < 4; ++stage) {
+      const float* src = (stage == 0) ? U : p->Us;
+      float* Uw = (stage == 0 && pending_px) ? U : nullptr;
+      if ((rc = xfirst(p, src, Uw, nullptr, s)) != PS_OK) return rc;
+      if (p->nd == 3 && (rc = ymid(p, s)) != PS_OK) return rc;
+      float* out = (stage < 3) ? p->Us : U;
+      if ((rc = last(p, stage, U, out, dt, d_dt, filt && stage == 3, s)) != PS_OK) return rc;
+    }
+    pending_px = false;
+    if (filt) {
+      if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s)) != PS_OK) return rc;
+      pending_px = true;
+    }
+    p->step_counter += 1;
+  }
+  if (pending_px && (rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s)) != PS_OK) return rc;
+  return PS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ps_last_error(void) { return g_err.c_str(); }
+
+const char* ps_version(void) { return "phrike_gb300 0.1.0 (sm_103a)"; }
+
+int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
+  if (!d) return fail(PS_ERR_INVALID, "null descriptor");
+  memset(d, 0, sizeof(*d));
+  d->ndim = ndim;
+  for (int a = 0; a < 3; ++a) {
+    d->n[a] = 1;
+    d->length[a] = 1.0;
+    d->basis[a] = PS_BASIS_FOURIER;
+  }
+  d->equations = PS_EQ_EULER;
+  d->gamma = 1.4;
+  d->dealias = 1;
+  d->filter_enabled = 0;
+  d->filter_p = 8;
+  d->filter_alpha = 36.0;
+  d->filter_interval = 1;
+  d->cfl = (ndim == 1) ? 0.4 : (ndim == 2) ? 0.3 : 0.25;
+  return PS_OK;
+}
+
+int ps_plan_scratch_bytes(const ps_plan_desc* d, size_t* bytes) {
+  int rc = validate(d);
+  if (rc != PS_OK) return rc;
+  if (!bytes) return fail(PS_ERR_INVALID, "null output");
+  long cells = 1;
+  for (int a = 0; a < d->ndim; ++a) cells *= d->n[a];
+  size_t tables = 0;
+  for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
+  *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) + tables + 64;
+  return PS_OK;
+}
+
+int ps_plan_create(const ps_plan_desc* d, ps_plan* out) {
+  int rc = validate(d);
+  if (rc != PS_OK) return rc;
+  if (!out) return fail(PS_ERR_INVALID, "null output handle");
+  ps_plan p = new ps_plan_s();
+  p->desc = *d;
+  p->nd = d->ndim;
+  p->nc = d->ndim + 2;
+  p->cells = 1;
+  for (int a = 0; a < p->nd; ++a) {
+    p->n[a] = d->n[a];
+    p->cells *= d->n[a];
+  }
+  auto cleanup = [&](int code) {
+    ps_plan_destroy(p);
+    return code;
+  };
+  for (int a = 0; a < p->nd; ++a) {
+    std::vector<float> P, dd;
+    std::vector<float2> twf, twi;
+    build_axis(p->n[a], d->length[a], d->dealias, d->filter_enabled, d->filter_p, d->filter_alpha, P, dd, twf, twi);
+    const int N = p->n[a];
+    if ((rc = dalloc(p, &p->P[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->d[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->twf[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->twi[a], N)) != PS_OK) return cleanup(rc);
+    cudaError_t e;
+    if ((e = cudaMemcpy(p->P[a], P.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->d[a], dd.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->twf[a], twf.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->twi[a], twi.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cleanup(cuda_fail(e, "table upload"));
+  }
+  const long c = p->cells;
+  if (p->nd == 1) {
+    if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
+  } else {
+    const int ng = (p->nd == 3) ? 15 : 8;
+    if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
+    if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
+  }
+  if ((rc = dalloc(p, &p->speed, 1)) != PS_OK) return cleanup(rc);
+  *out = p;
+  return PS_OK;
+}
+
+int ps_plan_destroy(ps_plan p) {
+  if (!p) return PS_OK;
+  for (void* q : p->allocations) cudaFree(q);
+  for (auto& r : p->launches) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  for (cudaEvent_t e : p->event_pool) cudaEventDestroy(e);
+  delete p;
+  return PS_OK;
+}
+
+int ps_plan_ncomp(ps_plan p) { return p ? p->nc : -1; }
+
+int ps_profile_enable(ps_plan p, int enable) {
+  if (!p) return fail(PS_ERR_INVALID, "null plan");
+  p->profiling = enable != 0;
+  return PS_OK;
+}
+
+int ps_profile_collect(ps_plan p, int nkinds, int* launches, double* ms, double* bytes) {
+  if (!p || nkinds < 1 || !launches || !ms || !bytes) return fail(PS_ERR_INVALID, "null argument");
+  for (int k = 0; k < nkinds; ++k) {
+    launches[k] = 0;
+    ms[k] = 0.0;
+    bytes[k] = 0.0;
+  }
+  for (auto& r : p->launches) {
+    float t = 0.0f;
+    cudaError_t e = cudaEventSynchronize(r.stop);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.start, r.stop);
+    if (e != cudaSuccess) return cuda_fail(e, "profile events");
+    if (r.kind < nkinds) {
+      launches[r.kind] += 1;
+      ms[r.kind] += t;
+      bytes[r.kind] += r.bytes;
+    }
+    p->event_pool.push_back(r.start);
+    p->event_pool.push_back(r.stop);
+  }
+  p->launches.clear();
+  return PS_OK;
+}
+
+int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
+  if (!p || !U || !rhs) return fail(PS_ERR_INVALID, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  if (p->nd == 1) {
+    PS_CU(ps::launch_flux1d(U, p->cells, (float)p->desc.gamma, p->F1, s), "1D flux");
+    return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
+  }
+  if ((rc = xfirst(p, U, nullptr, nullptr, s)) != PS_OK) return rc;
+  if (p->nd == 3 && (rc = ymid(p, s)) != PS_OK) return rc;
+  return last(p, -1, U, rhs, 0.0, nullptr, false, s);
+}
+
+int ps_step_rk4(ps_plan p, float* U, double dt, const double* d_dt, void* stream) {
+  return ps_run_steps(p, U, 1, dt, d_dt, stream);
+}
+
+int ps_run_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, void* stream) {
+  if (!p || !U) return fail(PS_ERR_INVALID, "null argument");
+  if (nsteps < 0) return fail(PS_ERR_INVALID, "nsteps must be >= 0");
+  if (nsteps == 0) return PS_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->nd == 1) return step_1d(p, U, nsteps, dt, d_dt, s);
+  return steps_nd(p, U, nsteps, dt, d_dt, s);
+}
+
+int ps_derivative(ps_plan p, int axis, const float* f, float* out, int nf, void* stream) {
+  if (!p || !f || !out) return fail(PS_ERR_INVALID, "null argument");
+  if (axis < 0 || axis >= p->nd) return fail(PS_ERR_INVALID, "axis %d out of range", axis);
+  if (nf < 1) return fail(PS_ERR_INVALID, "nfields must be >= 1");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float* src = f;
+  int rc;
+  for (int a = 0; a < p->nd; ++a) {
+    if ((rc = apply_op(p, a, src, out, nf, a == axis ? 1 : 0, 1.0f, s)) != PS_OK) return rc;
+    src = out;
+  }
+  return PS_OK;
+}
+
+int ps_filter(ps_plan p, const float* f, float* out, int nf, void* stream) {
+  if (!p || !f || !out) return fail(PS_ERR_INVALID, "null argument");
+  if (nf < 1) return fail(PS_ERR_INVALID, "nfields must be >= 1");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float* src = f;
+  int rc;
+  for (int a = 0; a < p->nd; ++a) {
+    if ((rc = apply_op(p, a, src, out, nf, 0, 1.0f, s)) != PS_OK) return rc;
+    src = out;
+  }
+  return PS_OK;
+}
+
+int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
+  if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
+  PS_CU(ps::launch_speed(p->nd, U, p->cells, (float)p->desc.gamma, d_out, (cudaStream_t)stream), "max wave speed");
+  return PS_OK;
+}
+
+int ps_conserved(ps_plan p, const float* U, double* d_out, void* stream) {
+  if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
+  PS_CU(ps::launch_conserved(p->nd, U, p->cells, p->desc.gamma, d_out, (cudaStream_t)stream), "conserved sums");
+  return PS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+"""Thin torch-facing wrapper of one C-ABI plan (one solve on one GPU).
+
+Tensors are handed over by device pointer on the caller's current CUDA
+stream; the library never sees torch types.  State tensors are float32,
+component-first, C-contiguous, shape (ncomp, [Nz,] [Ny,] Nx).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional, Sequence
+
+import torch
+
+from . import _lib
+
+
+def _stream(device: torch.device) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _ptr(t: torch.Tensor) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+class Plan:
+    """One Fourier pseudo-spectral Euler solve (1-3 dimensions).
+
+    ``shape`` is the spatial shape in array order ((N,), (Ny, Nx) or
+    (Nz, Ny, Nx)); ``lengths`` follows the same order.
+    """
+
+    def __init__(self, shape: Sequence[int], lengths: Sequence[float], gamma: float = 1.4,
+                 dealias: bool = True, filter_params: Optional[Dict] = None,
+                 cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
+                 device: Optional[torch.device] = None):
+        lib = _lib.load()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if self.device.type != "cuda":
+            raise RuntimeError("phrike_gb300 plans run on a CUDA device only")
+        self.shape = tuple(int(n) for n in shape)
+        self.ndim = len(self.shape)
+        self.ncomp = self.ndim + 2
+        desc = _lib.PlanDesc()
+        _lib.check(lib.ps_plan_desc_init(C.byref(desc), self.ndim))
+        xyz = list(reversed(self.shape))
+        lxyz = list(reversed([float(L) for L in lengths]))
+        for a in range(self.ndim):
+            desc.n[a] = xyz[a]
+            desc.length[a] = lxyz[a]
+        desc.gamma = float(gamma)
+        desc.dealias = 1 if dealias else 0
+        fp = filter_params or {}
+        desc.filter_enabled = 1 if bool(fp.get("enabled", False)) else 0
+        desc.filter_p = int(fp.get("p", 8))
+        desc.filter_alpha = float(fp.get("alpha", 36.0))
+        desc.filter_interval = max(1, int(fp.get("interval", 1) or 1))
+        if cfl is not None:
+            desc.cfl = float(cfl)
+        if gravity is not None:
+            for a, g in enumerate(gravity):
+                desc.gravity[a] = float(g)
+        self.desc = desc
+        self._handle = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(lib.ps_plan_create(C.byref(desc), C.byref(self._handle)))
+        self._lib = lib
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_handle", None) and self._handle.value:
+            with torch.cuda.device(self.device):
+                self._lib.ps_plan_destroy(self._handle)
+            self._handle = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- helpers ----------------------------------------------------------
+    def _check_state(self, U: torch.Tensor, nf: Optional[int] = None) -> None:
+        nf = self.ncomp if nf is None else nf
+        if not isinstance(U, torch.Tensor) or U.device != self.device:
+            raise RuntimeError(f"expected a tensor on {self.device}")
+        if U.dtype != torch.float32:
+            raise RuntimeError(f"expected float32 fields, got {U.dtype}")
+        if not U.is_contiguous():
+            raise RuntimeError("fields must be C-contiguous")
+        if tuple(U.shape[-self.ndim:]) != self.shape or U.numel() != nf * self.cells:
+            raise RuntimeError(f"expected shape ({nf}, {self.shape}), got {tuple(U.shape)}")
+
+    @property
+    def cells(self) -> int:
+        c = 1
+        for n in self.shape:
+            c *= n
+        return c
+
+    def scratch_bytes(self) -> int:
+        b = C.c_size_t()
+        _lib.check(self._lib.ps_plan_scratch_bytes(C.byref(self.desc), C.byref(b)))
+        return int(b.value)
+
+    # -- operations -------------------------------------------------------
+    def rhs(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        self._check_state(U)
+        out = torch.empty_like(U) if out is None else out
+        _lib.check(self._lib.ps_rhs(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
+        return out
+
+    def step_(self, U: torch.Tensor, dt: float = 0.0, dt_dev: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """One RK4 step in place (dt from ``dt_dev`` if given: a float64 device scalar)."""
+        self._check_state(U)
+        dptr = _ptr(dt_dev) if dt_dev is not None else None
+        _lib.check(self._lib.ps_step_rk4(self._handle, _ptr(U), float(dt), dptr, _stream(self.device)))
+        return U
+
+    def run_(self, U: torch.Tensor, nsteps: int, dt: float = 0.0,
+             dt_dev: Optional[torch.Tensor] = None) -> torch.Tensor:
+        self._check_state(U)
+        dptr = _ptr(dt_dev) if dt_dev is not None else None
+        _lib.check(self._lib.ps_run_steps(self._handle, _ptr(U), int(nsteps), float(dt), dptr,
+                                          _stream(self.device)))
+        return U
+
+    def derivative(self, f: torch.Tensor, axis: int, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """axis 0 = x (last array axis)."""
+        nf = f.numel() // self.cells
+        self._check_state(f, nf)
+        out = torch.empty_like(f) if out is None else out
+        _lib.check(self._lib.ps_derivative(self._handle, int(axis), _ptr(f), _ptr(out), nf,
+                                           _stream(self.device)))
+        return out
+
+    def filter(self, f: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        nf = f.numel() // self.cells
+        self._check_state(f, nf)
+        out = torch.empty_like(f) if out is None else out
+        _lib.check(self._lib.ps_filter(self._handle, _ptr(f), _ptr(out), nf, _stream(self.device)))
+        return out
+
+    def max_wave_speed(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        self._check_state(U)
+        out = torch.empty(1, dtype=torch.float32, device=self.device) if out is None else out
+        _lib.check(self._lib.ps_max_wave_speed(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
+        return out
+
+    def conserved(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        self._check_state(U)
+        out = torch.empty(self.ncomp, dtype=torch.float64, device=self.device) if out is None else out
+        _lib.check(self._lib.ps_conserved(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
+        return out
+
+    # -- launch profiling -------------------------------------------------
+    def profile(self, enable: bool = True) -> None:
+        """Bracket every pass launch with CUDA events (kind, algorithmic bytes)."""
+        _lib.check(self._lib.ps_profile_enable(self._handle, 1 if enable else 0))
+
+    def collect_profile(self) -> Dict[str, Dict[str, float]]:
+        """Per-kind {launches, ms, bytes} of the launches since the last collect."""
+        n = len(_lib.KIND_NAMES)
+        la = (C.c_int * n)()
+        ms = (C.c_double * n)()
+        by = (C.c_double * n)()
+        _lib.check(self._lib.ps_profile_collect(self._handle, n, la, ms, by))
+        return {name: {"launches": int(la[i]), "ms": float(ms[i]), "bytes": float(by[i])}
+                for i, name in enumerate(_lib.KIND_NAMES) if la[i] > 0}

@@ -1,0 +1,105 @@
+"""Initial conditions of the benchmark workloads (host-side NumPy, float64).
+
+The formulas are the analytic set-ups used for the single-solve, batched and
+served workloads:
+
+* smoothed Sod-type step, 1D periodic [0, L)            (``sod_smoothed``)
+* Taylor-Green vortex, 3D periodic [0, 2 pi)^3           (``taylor_green_3d``)
+* Kelvin-Helmholtz shear layer, 2D periodic [0, 1)^2     (``kelvin_helmholtz_2d``)
+* Orszag-Tang vortex (ideal MHD), 2D periodic [0, 2 pi)^2 (``orszag_tang_2d``)
+* Gaussian acoustic pulse on Legendre-Gauss-Lobatto nodes (``acoustic_pulse_lgl_2d``)
+
+All return conservative states with component-first layout and spatial axes
+(..., Ny, Nx) / (Nz, Ny, Nx), x last, which is the layout of the reference
+(phrike/grid.py:779-780, 1361).
+"""
+from __future__ import annotations
+
+from typing import Tuple
+
+import numpy as np
+
+
+def _euler_conservative(rho, vel, p, gamma):
+    E = p / (gamma - 1.0) + 0.5 * rho * sum(v * v for v in vel)
+    return np.stack([rho] + [rho * v for v in vel] + [E])
+
+
+def sod_smoothed(N: int, L: float = 1.0, gamma: float = 1.4, width: float = 0.005) -> np.ndarray:
+    """rho=1, p=1 on [0.25, 0.75) else rho=0.125, p=0.1, u=0; tanh edges."""
+    x = np.linspace(0.0, L, N, endpoint=False)
+    s = 0.5 * (np.tanh((x - 0.25 * L) / width) - np.tanh((x - 0.75 * L) / width))
+    rho = 0.125 + (1.0 - 0.125) * s
+    p = 0.1 + (1.0 - 0.1) * s
+    u = np.zeros_like(x)
+    return _euler_conservative(rho, [u], p, gamma)
+
+
+def taylor_green_3d(Nx: int, Ny: int = None, Nz: int = None, gamma: float = 1.4,
+                    L: float = 2.0 * np.pi) -> np.ndarray:
+    """rho=1, u=sin x cos y cos z, v=-cos x sin y cos z, w=0,
+    p = 100/gamma + (cos 2x + cos 2y)(cos 2z + 2)/16 on [0, L)^3."""
+    Ny = Nx if Ny is None else Ny
+    Nz = Nx if Nz is None else Nz
+    x = np.linspace(0.0, L, Nx, endpoint=False)
+    y = np.linspace(0.0, L, Ny, endpoint=False)
+    z = np.linspace(0.0, L, Nz, endpoint=False)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    rho = np.ones_like(X)
+    u = np.sin(X) * np.cos(Y) * np.cos(Z)
+    v = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    w = np.zeros_like(X)
+    p = 100.0 / gamma + (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
+    return _euler_conservative(rho, [u, v, w], p, gamma)
+
+
+def kelvin_helmholtz_2d(Nx: int, Ny: int = None, U0: float = 1.0, A: float = 0.01,
+                        gamma: float = 1.4) -> np.ndarray:
+    """Double shear layer on [0,1)^2: profile s(y) = tanh((y-.25)/.05) - tanh((y-.75)/.05) - 1,
+    u = U0 s, rho = 1.5 + 0.5 s, p = 2.5,
+    v = A sin(4 pi x)(exp(-(y-.25)^2/.0025) + exp(-(y-.75)^2/.0025))."""
+    Ny = Nx if Ny is None else Ny
+    x = np.linspace(0.0, 1.0, Nx, endpoint=False)
+    y = np.linspace(0.0, 1.0, Ny, endpoint=False)
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    s = np.tanh((Y - 0.25) / 0.05) - np.tanh((Y - 0.75) / 0.05) - 1.0
+    u = U0 * s
+    rho = 1.5 + 0.5 * s
+    p = 2.5 * np.ones_like(X)
+    v = A * np.sin(4.0 * np.pi * X) * (np.exp(-(Y - 0.25) ** 2 / 0.0025)
+                                        + np.exp(-(Y - 0.75) ** 2 / 0.0025))
+    return _euler_conservative(rho, [u, v], p, gamma)
+
+
+def orszag_tang_2d(Nx: int, Ny: int = None, gamma: float = 5.0 / 3.0) -> np.ndarray:
+    """rho = gamma^2, p = gamma, u = -sin y, v = sin x, Bx = -sin y, By = sin 2x
+    on [0, 2 pi)^2.  8 components [rho, mx, my, mz, Bx, By, Bz, E] with
+    E = p/(gamma-1) + rho|u|^2/2 + |B|^2/2."""
+    Ny = Nx if Ny is None else Ny
+    L = 2.0 * np.pi
+    x = np.linspace(0.0, L, Nx, endpoint=False)
+    y = np.linspace(0.0, L, Ny, endpoint=False)
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    rho = gamma ** 2 * np.ones_like(X)
+    p = gamma * np.ones_like(X)
+    u = -np.sin(Y)
+    v = np.sin(X)
+    w = np.zeros_like(X)
+    Bx = -np.sin(Y)
+    By = np.sin(2.0 * X)
+    Bz = np.zeros_like(X)
+    E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    return np.stack([rho, rho * u, rho * v, rho * w, Bx, By, Bz, E])
+
+
+def acoustic_pulse_lgl_2d(x: np.ndarray, y: np.ndarray, gamma: float = 1.4,
+                          amp: float = 0.01, width2: float = 0.01,
+                          center: Tuple[float, float] = (0.0, 0.0)) -> np.ndarray:
+    """rho = 1 + amp exp(-r^2/width2), p = rho^gamma/gamma, u = v = 0 on
+    the given node coordinates (1-D arrays for x and y, domain [-1, 1]^2)."""
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    r2 = (X - center[0]) ** 2 + (Y - center[1]) ** 2
+    rho = 1.0 + amp * np.exp(-r2 / width2)
+    p = rho ** gamma / gamma
+    z = np.zeros_like(X)
+    return _euler_conservative(rho, [z, z], p, gamma)

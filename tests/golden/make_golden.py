@@ -1,0 +1,128 @@
+"""Generate golden vectors by running the reference package (phrike) itself.
+
+Run once where the reference source tree is available:
+
+    python tests/golden/make_golden.py /path/to/phrike-checkout
+
+The reference imports ``yaml`` and ``matplotlib`` only for config loading and
+plotting; both are replaced by empty placeholder modules here.  numba is not
+installed, so the reference runs its plain-NumPy fallbacks (float64).
+
+Each fixture stores the inputs (or the recipe to rebuild them) and the
+reference outputs after a few fixed-dt steps, so the oracle and the CUDA path
+can be compared against the reference without the reference present.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+
+def import_reference(path: str):
+    for name in ("yaml", "matplotlib", "matplotlib.pyplot", "matplotlib.animation",
+                 "matplotlib.colors", "matplotlib.cm"):
+        if name not in sys.modules:
+            mod = types.ModuleType(name)
+            mod.use = lambda *a, **k: None
+            sys.modules[name] = mod
+    sys.path.insert(0, path)
+    import phrike  # noqa: F401
+    from phrike import grid, equations, solver
+    return grid, equations, solver
+
+
+def main(ref_path: str) -> None:
+    grid, equations, solver = import_reference(ref_path)
+    from phrike_gb300 import problems
+
+    out = {}
+
+    # --- operator fixtures: random fields through dx1/dy1/dz1/filter -------
+    rng = np.random.default_rng(20261203)
+    filt = {"enabled": True, "p": 8, "alpha": 36.0}
+    ops = {}
+    for dealias in (True, False):
+        for fon in (False, True):
+            tag = f"d{int(dealias)}f{int(fon)}"
+            fp = filt if fon else None
+            g1 = grid.Grid1D(N=64, Lx=1.0, dealias=dealias, filter_params=fp)
+            f1 = rng.standard_normal((3, 64))
+            ops[f"g1_{tag}_in"] = f1
+            ops[f"g1_{tag}_dx"] = g1.dx1(f1.copy())
+            ops[f"g1_{tag}_filt"] = g1.apply_spectral_filter(f1.copy())
+            g2 = grid.Grid2D(Nx=32, Ny=16, Lx=1.0, Ly=0.5, dealias=dealias, filter_params=fp)
+            f2 = rng.standard_normal((2, 16, 32))
+            ops[f"g2_{tag}_in"] = f2
+            ops[f"g2_{tag}_dx"] = g2.dx1(f2.copy())
+            ops[f"g2_{tag}_dy"] = g2.dy1(f2.copy())
+            ops[f"g2_{tag}_filt"] = g2.apply_spectral_filter(f2.copy())
+            g3 = grid.Grid3D(Nx=16, Ny=8, Nz=16, Lx=2 * np.pi, Ly=np.pi, Lz=4 * np.pi,
+                             dealias=dealias, filter_params=fp)
+            f3 = rng.standard_normal((1, 16, 8, 16))
+            ops[f"g3_{tag}_in"] = f3
+            ops[f"g3_{tag}_dx"] = g3.dx1(f3.copy())
+            ops[f"g3_{tag}_dy"] = g3.dy1(f3.copy())
+            ops[f"g3_{tag}_dz"] = g3.dz1(f3.copy())
+            ops[f"g3_{tag}_filt"] = g3.apply_spectral_filter(f3.copy())
+    np.savez_compressed(os.path.join(HERE, "fourier_ops.npz"), **ops)
+
+    # --- 1D Sod, filter p=8 alpha=36, dealias, dt=2e-5 ------------------
+    for N, nsteps in ((128, 5), (1024, 3)):
+        g = grid.Grid1D(N=N, Lx=1.0, dealias=True, filter_params=dict(filt))
+        eq = equations.EulerEquations1D(gamma=1.4)
+        s = solver.SpectralSolver1D(g, eq, scheme="rk4", cfl=0.4)
+        U0 = problems.sod_smoothed(N)
+        rhs0 = solver._compute_rhs(g, eq, U0.copy())
+        U = U0.copy()
+        for _ in range(nsteps):
+            U = s.step(U, 2e-5)
+        np.savez_compressed(os.path.join(HERE, f"sod1d_n{N}.npz"), U0=U0, rhs0=rhs0, U=U,
+                            dt=2e-5, nsteps=nsteps, dt_cfl0=s.compute_dt(U0),
+                            cons=np.array([eq.conserved_quantities(U)[k]
+                                           for k in ("mass", "momentum", "energy")]))
+
+    # --- 3D TGV, dealias, filter off, dt=1e-3 --------------------------
+    for (Nx, Ny, Nz), nsteps in (((16, 16, 16), 3), ((16, 8, 32), 2)):
+        g = grid.Grid3D(Nx=Nx, Ny=Ny, Nz=Nz, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, dealias=True)
+        eq = equations.EulerEquations3D(gamma=1.4)
+        s = solver.SpectralSolver3D(g, eq, scheme="rk4", cfl=0.25)
+        U0 = problems.taylor_green_3d(Nx, Ny, Nz)
+        rhs0 = solver._compute_rhs_3d(g, eq, U0.copy())
+        U = U0.copy()
+        for _ in range(nsteps):
+            U = s.step(U, 1e-3)
+        np.savez_compressed(os.path.join(HERE, f"tgv3d_{Nx}x{Ny}x{Nz}.npz"), U0=U0, rhs0=rhs0,
+                            U=U, dt=1e-3, nsteps=nsteps, dt_cfl0=s.compute_dt(U0),
+                            speed0=eq.max_wave_speed(U0))
+
+    # --- 2D KHI, CFL 0.4 run loop --------------------------------------
+    for (Nx, Ny), nsteps in (((32, 32), 4), ((64, 16), 3)):
+        g = grid.Grid2D(Nx=Nx, Ny=Ny, Lx=1.0, Ly=1.0, dealias=True)
+        eq = equations.EulerEquations2D(gamma=1.4)
+        s = solver.SpectralSolver2D(g, eq, scheme="rk4", cfl=0.4)
+        U0 = problems.kelvin_helmholtz_2d(Nx, Ny, U0=1.2, A=0.015)
+        rhs0 = solver._compute_rhs_2d(g, eq, U0.copy())
+        U = U0.copy()
+        t = 0.0
+        dts = []
+        dt = s.compute_dt(U)
+        for _ in range(nsteps):
+            U = s.step(U, dt)
+            t += dt
+            dts.append(dt)
+            dt = s.compute_dt(U)
+        np.savez_compressed(os.path.join(HERE, f"khi2d_{Nx}x{Ny}.npz"), U0=U0, rhs0=rhs0, U=U,
+                            dts=np.array(dts), t=t, U0_param=1.2, A=0.015)
+
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

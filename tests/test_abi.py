@@ -1,0 +1,45 @@
+"""The C-ABI library builds, loads and exports every symbol the header
+declares (no compute calls: these run without a GPU)."""
+import os
+import re
+
+from conftest import REPO
+
+
+def _declared():
+    names = []
+    for fn in os.listdir(os.path.join(REPO, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(REPO, "include", fn)).read()
+            names += re.findall(r"^\s*(?:int|const char\*)\s+(ps_\w+)\s*\(", src, re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "ps_step_rk4" in names and "ps_plan_create" in names and len(names) >= 12
+
+
+def test_library_exports_declared_symbols(built_lib):
+    from phrike_gb300 import _lib
+    for name in _declared():
+        assert hasattr(built_lib, name), name
+    assert set(_declared()) <= set(_lib.exported_names())
+
+
+def test_error_paths_without_device(built_lib):
+    import ctypes as C
+    from phrike_gb300 import _lib
+    desc = _lib.PlanDesc()
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 3) == 0
+    desc.n[0] = desc.n[1] = desc.n[2] = 48  # not a supported pencil length
+    h = C.c_void_p()
+    rc = built_lib.ps_plan_create(C.byref(desc), C.byref(h))
+    assert rc == 2 and b"N=48" in built_lib.ps_last_error()
+    desc.ndim = 4
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 1
+    size = C.c_size_t()
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 3) == 0
+    desc.n[0] = desc.n[1] = desc.n[2] = 256
+    assert built_lib.ps_plan_scratch_bytes(C.byref(desc), C.byref(size)) == 0
+    assert size.value >= 35 * 256 ** 3 * 4
