@@ -8,6 +8,9 @@
 //   applied inside the step and once more by the cadence counter.
 // The three state tiles (U^n, stage input, accumulator) stay in shared
 // memory for all nsteps, so a launch touches HBM only to load and store U.
+// Energy is held in perturbation form E' = E - E_ref (E_ref = energy of the
+// first cell at launch) and filters use the complementary form; both are
+// exact rewrites that cut float32 rounding noise (see pass_common.cuh).
 #pragma once
 #include "pass_common.cuh"
 
@@ -48,27 +51,36 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
   float* U = a.U + (long)blockIdx.x * a.solve_stride;
   // private slots: (c*B + n2)*A + t  <-> position t + A*n2
   auto sl = [&](int c, int n2) { return (c * B + n2) * A + t; };
+  const float er = U[2 * N];  // E_ref; U is written only after the last step
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) {
-      const float v = U[c * N + t + A * n2];
+      float v = U[c * N + t + A * n2];
+      if (c == 2) v -= er;
       S.un[sl(c, n2)] = v;
       S.us[sl(c, n2)] = v;
     }
   __syncthreads();
   const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
   const float g1 = a.gamma - 1.0f;
+  const float href = a.gamma * er;
+  const float pmin_shift = a.p_min - g1 * er;
 
-  auto filter_pair = [&](float2 (&w)[B]) {
+  auto filter_pair = [&](float2 (&w)[B]) {  // complementary form
+    float2 w0[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) w0[r] = w[r];
     pf.fwd(w);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
-      const float s = S.ax.P[pf.kidx(r)];
-      w[r].x *= s;
-      w[r].y *= s;
+      const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];
+      w[r].x *= q;
+      w[r].y *= q;
     }
     pf.inv(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
   };
 
 #pragma unroll 1
@@ -81,10 +93,10 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
       for (int n2 = 0; n2 < B; ++n2) {
         const float rho = S.us[sl(0, n2)], m = S.us[sl(1, n2)], E = S.us[sl(2, n2)];
         const float u = m / rho;
-        const float p = g1 * (E - 0.5f * rho * u * u);
+        const float p = g1 * (E - 0.5f * rho * u * u);  // p' (E holds E')
         const float mom = rho * u;
         w01[n2] = make_float2(mom, mom * u + p);
-        w2[n2] = make_float2((E + p) * u, 0.0f);
+        w2[n2] = make_float2(((E + p) + href) * u, 0.0f);
       }
       // k = -i d FFT(F): multiply by -i d
       pf.fwd(w01);
@@ -123,7 +135,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
             u3[c] = fmaf(rc.wnext, k[c], un);
           }
         }
-        clamp_state<1>(u3, a.gamma, a.rho_min, a.p_min);
+        clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
         for (int c = 0; c < 3; ++c) S.us[sl(c, n2)] = u3[c];
       }
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int n2 = 0; n2 < B; ++n2) U[c * N + t + A * n2] = S.un[sl(c, n2)];
+    for (int n2 = 0; n2 < B; ++n2) U[c * N + t + A * n2] = S.un[sl(c, n2)] + (c == 2 ? er : 0.0f);
 }
 
 }  // namespace ps

@@ -39,6 +39,8 @@ struct XFirstArgs {
   AxisOps ax;
   float gamma;
   float* speed;      // if non-null: atomic max of the CFL wave speed
+  const float* eref; // device scalar E_ref of the energy-perturbation form
+  int shift_in;      // 1: U holds E (subtract E_ref on load); 0: U holds E'
 };
 
 template <int N, int T, int ND>
@@ -67,12 +69,17 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   // per-thread private slots of the tile: ((c*B + n2)*T + p)*A + t
   auto slot = [&](int c, int n2) -> float& { return S.tile[((c * B + n2) * T + p) * A + t]; };
   const long rbase = (long)row * N + t;
+  const float er = *a.eref;
+  const float eshift = a.shift_in ? er : 0.0f;
+  const float pref = (a.gamma - 1.0f) * er;
+  const float href = a.gamma * er;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) {
-      float v = (c == 0 || c == NC - 1) ? 1.0f : 0.0f;
+      float v = (c == 0) ? 1.0f : 0.0f;
       if (valid) v = a.U[c * a.fs + rbase + A * n2];  // may alias a.Uw: plain load
+      if (c == NC - 1 && valid) v -= eshift;
       slot(c, n2) = v;
     }
   }
@@ -87,18 +94,20 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
       pf.fwd(v);
 #pragma unroll
       for (int r = 0; r < B; ++r) {
-        const float s = S.ax.P[pf.kidx(r)];
-        v[r].x *= s;
-        v[r].y *= s;
+        const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];  // complementary symbol
+        v[r].x *= q;
+        v[r].y *= q;
       }
       pf.inv(v);
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        slot(c, n2) = v[n2].x;
-        if (valid) a.Uw[c * a.fs + rbase + A * n2] = v[n2].x;
+        const float f0 = slot(c, n2) - v[n2].x;
+        slot(c, n2) = f0;
+        if (valid) a.Uw[c * a.fs + rbase + A * n2] = f0;
         if (c + 1 < NC) {
-          slot(c + 1, n2) = v[n2].y;
-          if (valid) a.Uw[(c + 1) * a.fs + rbase + A * n2] = v[n2].y;
+          const float f1 = slot(c + 1, n2) - v[n2].y;
+          slot(c + 1, n2) = f1;
+          if (valid) a.Uw[(c + 1) * a.fs + rbase + A * n2] = f1;
         }
       }
     }
@@ -121,7 +130,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
     const float pr = (a.gamma - 1.0f) * (slot(NC - 1, n2) - 0.5f * rho * kin);
     slot(NC - 1, n2) = pr;
     if (a.speed != nullptr && valid) {
-      const float cs = sqrtf(a.gamma * pr / rho);
+      const float cs = sqrtf(a.gamma * (pr + pref) / rho);
       float um = fabsf(vel[0]);
       if (ND == 3) um = fmaxf(um, fmaxf(fabsf(vel[1]), fabsf(vel[ND - 1])));
       // 2D keeps |u_x| + a only (equations.py:137-147)
@@ -143,8 +152,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
       float kin = 0.0f;
 #pragma unroll
       for (int d = 0; d < ND; ++d) kin = fmaf(slot(1 + d, n2), slot(1 + d, n2), kin);
-      const float E = pr / (a.gamma - 1.0f) + 0.5f * rho * kin;
-      return (E + pr) * ua;
+      const float Ep = pr / (a.gamma - 1.0f) + 0.5f * rho * kin;  // E' = E - E_ref
+      return ((Ep + pr) + href) * ua;                               // (E + p) u_a
     }
     const float ub = slot(c, n2);  // c in 1..ND -> velocity component c-1
     return rho * ua * ub + ((c - 1 == dir) ? pr : 0.0f);
@@ -336,6 +345,7 @@ struct LastArgs {
   double dt;
   float gamma;
   float rho_min, p_min;
+  const float* eref;   // E_ref of the energy-perturbation form (clamp floor shift)
   int filter_last;     // stage 3: apply P along this axis to the new state
 };
 
@@ -374,17 +384,23 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_last(LastArgs a) {
     }
     pf.inv(w);
   };
-  auto filter_pair = [&](float2 (&w)[B]) {
+  auto filter_pair = [&](float2 (&w)[B]) {  // complementary form, see AxisOps
+    float2 w0[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) w0[r] = w[r];
     pf.fwd(w);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
-      const float s = S.ax.P[pf.kidx(r)];
-      w[r].x *= s;
-      w[r].y *= s;
+      const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];
+      w[r].x *= q;
+      w[r].y *= q;
     }
     pf.inv(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
   };
   auto addr = [&](int c, int n2) { return c * a.fs + base + n2 * step; };
+  const float pmin_shift = a.p_min - (a.gamma - 1.0f) * (*a.eref);
 
   if (!CLAMP || a.stage < 0) {
     // components are independent: process pair by pair
@@ -458,11 +474,11 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_last(LastArgs a) {
           res = fmaf(rc.wnext, k, un);
         }
       } else {
-        res = (c == 0 || c == NC - 1) ? 1.0f : 0.0f;
+        res = (c == 0) ? 1.0f : 0.0f;
       }
       u[c] = res;
     }
-    clamp_state<ND>(u, a.gamma, a.rho_min, a.p_min);
+    clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (c & 1) kk[c / 2][n2].y = u[c];
@@ -497,6 +513,7 @@ struct OpArgs {
   AxisOps ax;
   int deriv;         // 0: P, 1: D
   float scale;       // multiplies the symbol (e.g. -1 for a right-hand side)
+  int complement;    // P only: out = in - IFFT((1/N - P) FFT in)  (exact, see AxisOps)
 };
 
 template <int N, int T, bool STRIDED>
@@ -529,8 +546,11 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
 #pragma unroll 1
   for (int c = 0; c < a.nf; c += 2) {
     const bool two = c + 1 < a.nf;
-    float2 w[B];
+    float2 w[B], w0[B];
     load_pair<N>(w, a.in + c * a.fs, two ? a.in + (c + 1) * a.fs : nullptr, base, step, valid);
+    const bool comp = a.complement && !a.deriv;
+#pragma unroll
+    for (int r = 0; r < B; ++r) w0[r] = w[r];
     pf.fwd(w);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
@@ -539,12 +559,16 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
         const float dd = a.scale * S.ax.d[k];
         w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
       } else {
-        const float s = a.scale * S.ax.P[k];
+        const float s = comp ? (1.0f / N) - S.ax.P[k] : a.scale * S.ax.P[k];
         w[r].x *= s;
         w[r].y *= s;
       }
     }
     pf.inv(w);
+    if (comp) {
+#pragma unroll
+      for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
+    }
     if (valid) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {

@@ -138,6 +138,7 @@ __device__ __forceinline__ void dft(float2 (&v)[CAP]) {
 
 // ---------------------------------------------------------------- pencil shapes
 template <int N> struct Shape;
+template <> struct Shape<8> { static constexpr int A = 2, B = 4; };
 template <> struct Shape<16> { static constexpr int A = 4, B = 4; };
 template <> struct Shape<32> { static constexpr int A = 4, B = 8; };
 template <> struct Shape<64> { static constexpr int A = 8, B = 8; };

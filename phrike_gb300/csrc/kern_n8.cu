@@ -1,0 +1,6 @@
+// Pass-kernel instantiations for pencils of 8 points.
+#include "launch.cuh"
+
+namespace ps {
+PS_DEFINE_LAUNCHERS(8)
+}  // namespace ps

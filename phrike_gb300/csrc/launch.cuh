@@ -15,13 +15,14 @@ template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream
 template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
 
 inline bool supported_n(int n) {
-  return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
+  return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
 }
 
 // Calls f(std::integral_constant<int, N>) for the supported pencil length n.
 template <typename F>
 cudaError_t dispatch_n(int n, F&& f) {
   switch (n) {
+    case 8: return f(std::integral_constant<int, 8>{});
     case 16: return f(std::integral_constant<int, 16>{});
     case 32: return f(std::integral_constant<int, 32>{});
     case 64: return f(std::integral_constant<int, 64>{});

@@ -15,6 +15,11 @@ namespace ps {
 //           of a full complex inverse transform, which drops that term)
 //   twf   = W_N^{n1*k2}  laid out [k2][n1]   (forward twiddles)
 //   twi   = W_N^{-n1*k2} laid out [n1][k2]   (inverse twiddles)
+// Filters of the state are applied in complementary form,
+//   P f = f - IFFT((1/N - P[k]) FFT f),
+// which is exact and leaves the retained band untouched when m*s = 1 there
+// (1/N - P[k] is then exactly 0), so a filter round trip adds no float32
+// rounding noise to the modes it keeps.
 struct AxisOps {
   const float* P;
   const float* d;
@@ -44,6 +49,7 @@ __device__ __forceinline__ void load_axis(AxisSmem<N>& s, const AxisOps& ax) {
 // Pencils per CTA: contiguous passes (pencils along x) and strided passes
 // (pencils along y or z, tiles of adjacent x columns).
 template <int N> struct Tile;
+template <> struct Tile<8> { static constexpr int TC = 64, TS = 16; };
 template <> struct Tile<16> { static constexpr int TC = 32, TS = 16; };
 template <> struct Tile<32> { static constexpr int TC = 32, TS = 16; };
 template <> struct Tile<64> { static constexpr int TC = 16, TS = 16; };
@@ -87,10 +93,22 @@ __device__ __forceinline__ RKCoef rk4_coef(int stage, float dt) {
   return c;
 }
 
+// Energy-perturbation form.  Inside the engine the energy slot of a state holds
+// E' = E - E_ref for a per-run constant E_ref (the energy of the first cell
+// when the run starts).  With p_ref = (gamma-1) E_ref the primitive pressure
+// becomes p' = p - p_ref = (gamma-1)(E' - rho|u|^2/2), computed from small
+// numbers, and every flux keeps its exact value:
+//   momentum:  rho u_a u_b + delta_ab p'      (constant offset; each flux is
+//              differentiated along its own axis, which annihilates constants)
+//   energy:    (E' + p' + gamma E_ref) u_a  == (E + p) u_a
+// In float32 this removes the rounding noise of |E| >> |p - <p>| at low Mach
+// number from the pressure gradient.
+
 // Conservative -> primitive -> floors -> conservative (the positivity clamp of
-// the 1D/2D solvers).  comps: NC = ND + 2, velocity components ND.
+// the 1D/2D solvers) in energy-perturbation form: pmin_shift = p_min - p_ref.
+// comps: NC = ND + 2, velocity components ND.
 template <int ND>
-__device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, float rho_min, float p_min) {
+__device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, float rho_min, float pmin_shift) {
   const float rho = u[0];
   float vel[ND];
   float kin = 0.0f;
@@ -101,7 +119,7 @@ __device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, flo
   }
   const float p = (gamma - 1.0f) * (u[ND + 1] - 0.5f * rho * kin);
   const float rc = fmaxf(rho, rho_min);
-  const float pc = fmaxf(p, p_min);
+  const float pc = fmaxf(p, pmin_shift);
   u[0] = rc;
 #pragma unroll
   for (int a = 0; a < ND; ++a) u[1 + a] = rc * vel[a];

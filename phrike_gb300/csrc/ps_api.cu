@@ -58,6 +58,7 @@ struct ps_plan_s {
   float* Us = nullptr;   // stage input (nc fields)
   float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
   float* speed = nullptr;
+  float* eref = nullptr;  // E_ref of the energy-perturbation form (device scalar)
   long step_counter = 0;
   std::vector<void*> allocations;
   // launch profiling: CUDA events around every pass launch
@@ -118,7 +119,7 @@ int validate(const ps_plan_desc* d) {
     if (d->basis[a] != PS_BASIS_FOURIER)
       return fail(PS_ERR_UNSUPPORTED, "axis %d: only the Fourier basis is supported by this plan type", a);
     if (!ps::supported_n(d->n[a]))
-      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 16..1024)", a, d->n[a]);
+      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 8..1024)", a, d->n[a]);
     if (!(d->length[a] > 0.0)) return fail(PS_ERR_INVALID, "axis %d: length must be positive", a);
   }
   if (!(d->gamma > 1.0)) return fail(PS_ERR_INVALID, "gamma must exceed 1");
@@ -151,7 +152,8 @@ void build_axis(int N, double L, int dealias, int fon, int fp, double falpha, st
     const double kphys = 2.0 * M_PI * kk / L;
     d[k] = (k == N / 2) ? 0.0f : (float)(kphys * m / N);
   }
-  const int A = (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
+  // threads per pencil, as ps::Shape<N>::A in fft_pencil.cuh
+  const int A = (N == 8) ? 2 : (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
   const int B = N / A;
   for (int k2 = 0; k2 < B; ++k2)
     for (int n1 = 0; n1 < A; ++n1) {
@@ -184,7 +186,8 @@ ps::StridedGeom geom_z(const ps_plan_s* p) {
 }
 
 // One-axis operator on nf fields (P or D), axis 0 = x.
-int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s) {
+int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s,
+             bool complement = false) {
   ps::OpArgs a{};
   a.in = in;
   a.out = out;
@@ -195,6 +198,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
   a.ax = p->ax(axis);
   a.deriv = deriv;
   a.scale = scale;
+  a.complement = complement ? 1 : 0;
   ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells);
   cudaError_t e = ps::dispatch_n(p->n[axis], [&](auto nc) {
     return ps::launch_op<decltype(nc)::value>(axis != 0, a, s);
@@ -203,7 +207,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
   return PS_OK;
 }
 
-int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s) {
+int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, bool shift_in = false) {
   ps::XFirstArgs a{};
   a.U = U;
   a.Uw = Uw;
@@ -213,6 +217,8 @@ int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s) {
   a.ax = p->ax(0);
   a.gamma = (float)p->desc.gamma;
   a.speed = speed;
+  a.eref = p->eref;
+  a.shift_in = shift_in ? 1 : 0;
   ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * (p->nc * (Uw ? 2 : 1) + p->nd * p->nc));
   cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
     return ps::launch_xfirst<decltype(nc)::value>(p->nd, a, s);
@@ -260,6 +266,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   // the 2D kernel clamps (solver.py:467-513); the 3D solver has none (1220-1230)
   a.rho_min = 1e-8f;               // _positivity_clamp_2d floors (solver.py:467)
   a.p_min = 1e-10f;
+  a.eref = p->eref;
   a.filter_last = filter_last ? 1 : 0;
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
@@ -303,6 +310,9 @@ int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cuda
 int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cudaStream_t s) {
   int rc;
   bool pending_px = false;
+  float* UE = U + (long)(p->nc - 1) * p->cells;
+  PS_CU(ps::launch_eref_set(UE, p->eref, s), "energy reference");
+  PS_CU(ps::launch_energy_shift(UE, p->cells, p->eref, -1.0f, s), "energy shift");
   for (int it = 0; it < nsteps; ++it) {
     const bool filt = filter_due(p, p->step_counter);
     for (int stage = 0; stage < 4; ++stage) {
@@ -315,12 +325,13 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cud
     }
     pending_px = false;
     if (filt) {
-      if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s)) != PS_OK) return rc;
+      if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s, true)) != PS_OK) return rc;
       pending_px = true;
     }
     p->step_counter += 1;
   }
-  if (pending_px && (rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s)) != PS_OK) return rc;
+  if (pending_px && (rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s, true)) != PS_OK) return rc;
+  PS_CU(ps::launch_energy_shift(UE, p->cells, p->eref, 1.0f, s), "energy shift");
   return PS_OK;
 }
 
@@ -408,6 +419,8 @@ int ps_plan_create(const ps_plan_desc* d, ps_plan* out) {
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
   }
   if ((rc = dalloc(p, &p->speed, 1)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->eref, 1)) != PS_OK) return cleanup(rc);
+  PS_CU(cudaMemset(p->eref, 0, sizeof(float)), "eref init");
   *out = p;
   return PS_OK;
 }
@@ -464,7 +477,8 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
     PS_CU(ps::launch_flux1d(U, p->cells, (float)p->desc.gamma, p->F1, s), "1D flux");
     return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
   }
-  if ((rc = xfirst(p, U, nullptr, nullptr, s)) != PS_OK) return rc;
+  PS_CU(ps::launch_eref_set(U + (long)(p->nc - 1) * p->cells, p->eref, s), "energy reference");
+  if ((rc = xfirst(p, U, nullptr, nullptr, s, true)) != PS_OK) return rc;
   if (p->nd == 3 && (rc = ymid(p, s)) != PS_OK) return rc;
   return last(p, -1, U, rhs, 0.0, nullptr, false, s);
 }
@@ -503,7 +517,7 @@ int ps_filter(ps_plan p, const float* f, float* out, int nf, void* stream) {
   const float* src = f;
   int rc;
   for (int a = 0; a < p->nd; ++a) {
-    if ((rc = apply_op(p, a, src, out, nf, 0, 1.0f, s)) != PS_OK) return rc;
+    if ((rc = apply_op(p, a, src, out, nf, 0, 1.0f, s, true)) != PS_OK) return rc;
     src = out;
   }
   return PS_OK;

@@ -96,6 +96,27 @@ __global__ void k_cfl_dt(const float* speed, double cfl, double hmin, const doub
   *dt = d;
 }
 
+// E_ref of the energy-perturbation form: the energy of the first cell.
+__global__ void k_eref_set(const float* E, float* eref) { *eref = E[0]; }
+
+// E <- E + sign * E_ref (sign -1: to perturbation form, +1: back)
+__global__ void k_energy_shift(float* E, long n, const float* eref, float sign) {
+  const float s = sign * (*eref);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) E[i] += s;
+}
+
+cudaError_t launch_eref_set(const float* E, float* eref, cudaStream_t s) {
+  k_eref_set<<<1, 1, 0, s>>>(E, eref);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy_shift(float* E, long n, const float* eref, float sign, cudaStream_t s) {
+  const long want = (n + 255) / 256;
+  const int blocks = (int)(want < 4096 ? want : 4096);
+  k_energy_shift<<<blocks, 256, 0, s>>>(E, n, eref, sign);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_speed(int nd, const float* U, long cells, float gamma, float* out, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float), s);
   if (e != cudaSuccess) return e;

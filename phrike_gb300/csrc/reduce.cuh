@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 namespace ps {
+cudaError_t launch_eref_set(const float* E, float* eref, cudaStream_t s);
+cudaError_t launch_energy_shift(float* E, long n, const float* eref, float sign, cudaStream_t s);
 cudaError_t launch_speed(int nd, const float* U, long cells, float gamma, float* out, cudaStream_t s);
 cudaError_t launch_conserved(int nd, const float* U, long cells, double gamma, double* out, cudaStream_t s);
 cudaError_t launch_flux1d(const float* U, long n, float gamma, float* F, cudaStream_t s);
