@@ -263,7 +263,7 @@ struct YMidArgs {
 };
 
 template <int N, int T>
-__global__ void __launch_bounds__(Shape<N>::A * T) k_ymid3(YMidArgs a) {
+__global__ void __launch_bounds__(Shape<N>::A * T, (Shape<N>::A * T <= 256) ? 2 : 1) k_ymid3(YMidArgs a) {
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -350,7 +350,7 @@ struct LastArgs {
 };
 
 template <int N, int T, int ND, bool CLAMP>
-__global__ void __launch_bounds__(Shape<N>::A * T) k_last(LastArgs a) {
+__global__ void __launch_bounds__(Shape<N>::A * T, (Shape<N>::A * T <= 256) ? 2 : 1) k_last(LastArgs a) {
   constexpr int NC = ND + 2;
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
@@ -419,25 +419,41 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_last(LastArgs a) {
         }
         continue;
       }
+      // batch the epilogue loads (U^n, accumulator) before any store so the
+      // DRAM latencies overlap instead of serialising behind the acc writes
+      float un[2][B], ac[2][B];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          const bool live = valid && (q == 0 || two);
+          un[q][n2] = (live && a.stage != 3) ? __ldg(a.Un + addr(c + q, n2)) : 0.0f;
+          ac[q][n2] = (live && a.stage != 0) ? a.acc[addr(c + q, n2)] : 0.0f;
+        }
+      }
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        float k[2] = {w[n2].x, w[n2].y};
-        float res[2] = {0.0f, 0.0f};
+        const float k[2] = {w[n2].x, w[n2].y};
+        float res[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-          if (q == 1 && !two) break;
-          const long ad = addr(c + q, n2);
-          if (!valid) continue;
           if (a.stage == 3) {
-            res[q] = fmaf(rc.wacc, k[q], a.acc[ad]);
+            res[q] = fmaf(rc.wacc, k[q], ac[q][n2]);
           } else {
-            const float un = __ldg(a.Un + ad);
-            const float ac = (a.stage == 0) ? un : a.acc[ad];
-            a.acc[ad] = fmaf(rc.wacc, k[q], ac);
-            res[q] = fmaf(rc.wnext, k[q], un);
+            const float base_acc = (a.stage == 0) ? un[q][n2] : ac[q][n2];
+            ac[q][n2] = fmaf(rc.wacc, k[q], base_acc);
+            res[q] = fmaf(rc.wnext, k[q], un[q][n2]);
           }
         }
         w[n2] = make_float2(res[0], res[1]);
+      }
+      if (valid && a.stage != 3) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          if (q == 1 && !two) break;
+#pragma unroll
+          for (int n2 = 0; n2 < B; ++n2) a.acc[addr(c + q, n2)] = ac[q][n2];
+        }
       }
       if (a.stage == 3 && a.filter_last) filter_pair(w);
       if (valid) {
@@ -456,33 +472,46 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_last(LastArgs a) {
   float2 kk[(NC + 1) / 2][B];
 #pragma unroll
   for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
+  constexpr int CH = 4;  // positions per batch of epilogue loads
 #pragma unroll
-  for (int n2 = 0; n2 < B; ++n2) {
-    float u[NC];
+  for (int n0 = 0; n0 < B; n0 += CH) {
+    float un[CH][NC], ac[CH][NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const float k = (c & 1) ? kk[c / 2][n2].y : kk[c / 2][n2].x;
-      const long ad = addr(c, n2);
-      float res = 0.0f;
-      if (valid) {
-        if (a.stage == 3) {
-          res = fmaf(rc.wacc, k, a.acc[ad]);
-        } else {
-          const float un = __ldg(a.Un + ad);
-          const float ac = (a.stage == 0) ? un : a.acc[ad];
-          a.acc[ad] = fmaf(rc.wacc, k, ac);
-          res = fmaf(rc.wnext, k, un);
-        }
-      } else {
-        res = (c == 0) ? 1.0f : 0.0f;
+    for (int j = 0; j < CH; ++j)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        un[j][c] = (valid && a.stage != 3) ? __ldg(a.Un + addr(c, n0 + j)) : 0.0f;
+        ac[j][c] = (valid && a.stage != 0) ? a.acc[addr(c, n0 + j)] : 0.0f;
       }
-      u[c] = res;
-    }
-    clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      if (c & 1) kk[c / 2][n2].y = u[c];
-      else kk[c / 2][n2].x = u[c];
+    for (int j = 0; j < CH; ++j) {
+      const int n2 = n0 + j;
+      float u[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float k = (c & 1) ? kk[c / 2][n2].y : kk[c / 2][n2].x;
+        float res;
+        if (a.stage == 3) {
+          res = fmaf(rc.wacc, k, ac[j][c]);
+        } else {
+          const float base_acc = (a.stage == 0) ? un[j][c] : ac[j][c];
+          ac[j][c] = fmaf(rc.wacc, k, base_acc);
+          res = fmaf(rc.wnext, k, un[j][c]);
+        }
+        u[c] = valid ? res : ((c == 0) ? 1.0f : 0.0f);
+      }
+      clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c & 1) kk[c / 2][n2].y = u[c];
+        else kk[c / 2][n2].x = u[c];
+      }
+    }
+    if (valid && a.stage != 3) {
+#pragma unroll
+      for (int j = 0; j < CH; ++j)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) a.acc[addr(c, n0 + j)] = ac[j][c];
     }
   }
 #pragma unroll

@@ -34,9 +34,13 @@ cudaError_t dispatch_n(int n, F&& f) {
   }
 }
 
+// Dynamic shared memory above 48 KB needs an opt-in; every pass kernel also
+// asks for the largest shared-memory carveout so that several CTAs fit per SM.
 template <typename K>
 inline cudaError_t set_smem(K kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess || bytes <= 48 * 1024) return e;
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
