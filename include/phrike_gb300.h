@@ -123,6 +123,22 @@ int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);
 int ps_profile_enable(ps_plan plan, int enable);
 int ps_profile_collect(ps_plan plan, int nkinds, int* launches, double* ms, double* bytes);
 
+/* Allocation-free right-hand side (no counterpart in the reference).
+ * Same result as ps_rhs for a 2D or 3D Fourier Euler grid, but it takes the
+ * descriptor by value instead of a plan and allocates no device memory: the
+ * spectral tables and pass intermediates live in one static device array of
+ * PS_RHS_STATIC_MAX_CELLS cells' worth of scratch (about 6.6 MB, held by every
+ * GPU that loads the library until the process exits).  For callers that
+ * cannot call cudaMalloc where they evaluate a right-hand side: code inside a
+ * stream capture, frameworks that own all device memory through their own
+ * pool, allocation-free real-time loops.  Grids of more cells return
+ * PS_ERR_UNSUPPORTED.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race, so keep them on one
+ * stream. */
+#define PS_RHS_STATIC_MAX_CELLS 65536
+int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rhs, void* stream);
+
 /* Number of state components (ndim + 2 for Euler). */
 int ps_plan_ncomp(ps_plan plan);
 

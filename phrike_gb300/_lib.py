@@ -56,6 +56,7 @@ _SIGNATURES = [
     ("ps_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
+    ("ps_rhs_static", C.c_int, [C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_last_error", C.c_char_p, []),
     ("ps_version", C.c_char_p, []),
 ]

@@ -40,6 +40,15 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 }  // namespace
 
+namespace ps {
+// Records `msg` as the thread's last error (read by ps_last_error) and
+// returns `code`; for entry points implemented in other translation units.
+int record_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace ps
+
 struct ps_plan_s {
   ps_plan_desc desc;
   int nd = 0;

@@ -1,0 +1,206 @@
+// ps_rhs_static: the right-hand side of ps_rhs for small 2D/3D Fourier
+// grids, computed without allocating any device memory.
+//
+// Who needs it: callers that cannot call cudaMalloc at the point where they
+// evaluate a right-hand side -- code running inside a CUDA stream capture
+// (allocation is not a capturable operation), solvers embedded in a host
+// framework that owns every device allocation through its own pool, and
+// real-time loops that forbid allocator calls after start-up.  ps_rhs needs a
+// plan, and ps_plan_create allocates the spectral tables and the pass
+// intermediates; this entry point takes the grid description by value and
+// keeps everything it needs in one fixed-size array in device global memory.
+//
+// Scratch: g_rhs_static_scratch below (file-scope __device__ array, 256-byte
+// aligned).  Every GPU that loads the library holds it until the process
+// exits.  It is sized for grids of at most PS_RHS_STATIC_MAX_CELLS cells and
+// pencils of at most 1024 points; larger grids are rejected.  All calls share
+// the one array and it keeps the last call's contents: a call rebuilds the
+// spectral tables and E_ref and overwrites every intermediate before reading
+// it, so nothing has to start at zero.  Two calls whose kernels overlap on the
+// GPU (different streams, or different host threads on one device) race on
+// the array; order them on one stream.
+//
+// Device address: host code cannot pass g_rhs_static_scratch to a kernel
+// directly (in host code the name is a host-side shadow, not a device
+// address).  The first call on each device, with that device current, calls
+// cudaGetSymbolAddress once and caches the result; that first call should
+// therefore come before any stream capture.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+
+#include <mutex>
+
+#include "../../include/phrike_gb300.h"
+#include "launch.cuh"
+#include "reduce.cuh"
+
+namespace ps {
+int record_error(int code, const char* msg);
+}
+
+namespace {
+
+constexpr long kMaxCells = PS_RHS_STATIC_MAX_CELLS;
+constexpr int kMaxN = 1024;
+constexpr long kAxisFloats = 6L * kMaxN;       // P, d (N floats each), twf, twi (N float2 each)
+constexpr long kTableFloats = 3 * kAxisFloats;  // three axes
+constexpr long kErefOffset = kTableFloats;      // one float, padded to 256 bytes
+constexpr long kGOffset = kErefOffset + 64;
+constexpr long kABOffset = kGOffset + 15 * kMaxCells;
+constexpr long kTotalFloats = kABOffset + 10 * kMaxCells;
+
+__device__ __align__(256) float g_rhs_static_scratch[kTotalFloats];
+
+std::mutex g_addr_mutex;
+float* g_addr[64] = {nullptr};
+
+int fail(int code, const char* msg) { return ps::record_error(code, msg); }
+
+int fail_cuda(cudaError_t e, const char* what) {
+  char msg[256];
+  snprintf(msg, sizeof(msg), "ps_rhs_static: %s: %s", what, cudaGetErrorString(e));
+  return ps::record_error(PS_ERR_CUDA, msg);
+}
+
+// Spectral tables of one axis, built on the device in float64 (same
+// definitions as the plan's host-built tables: 2/3 mask, exponential filter,
+// 1/N folded in, Nyquist derivative term zeroed, twiddles of the pencil FFT).
+__global__ void k_static_axis(int N, int A, double L, int dealias, int fon, int fp, double falpha, float* P,
+                              float* d, float2* twf, float2* twi) {
+  const int B = N / A;
+  const double kmax = N / 2;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    const int kk = (k < N / 2) ? k : k - N;
+    const double ak = fabs((double)kk);
+    double m = (!dealias || ak <= (double)(N / 3)) ? 1.0 : 0.0;
+    if (fon) m *= exp(-falpha * pow(ak / (kmax > 1.0 ? kmax : 1.0), (double)fp));
+    P[k] = (float)(m / N);
+    d[k] = (k == N / 2) ? 0.0f : (float)((2.0 * kk / L) * 3.14159265358979323846 * m / N);
+    // twiddle entry k = k2*A + n1 of the forward table, n1*B + k2 of the inverse
+    const int k2 = k / A, n1 = k % A;
+    double sn, cs;
+    sincospi(-2.0 * (double)((long)n1 * k2 % N) / N, &sn, &cs);
+    twf[k2 * A + n1] = make_float2((float)cs, (float)sn);
+    twi[n1 * B + k2] = make_float2((float)cs, (float)-sn);
+  }
+}
+
+int threads_per_pencil(int N) {
+  return (N == 8) ? 2 : (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
+}
+
+}  // namespace
+
+extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rhs, void* stream) {
+  if (!desc || !U || !rhs) return fail(PS_ERR_INVALID, "ps_rhs_static: null argument");
+  if (desc->ndim != 2 && desc->ndim != 3)
+    return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: only 2D and 3D grids are supported");
+  if (desc->equations != PS_EQ_EULER) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: Euler equations only");
+  long cells = 1;
+  for (int a = 0; a < desc->ndim; ++a) {
+    if (desc->basis[a] != PS_BASIS_FOURIER) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: Fourier basis only");
+    if (!ps::supported_n(desc->n[a]))
+      return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: axis length must be a power of two in 8..1024");
+    if (!(desc->length[a] > 0.0)) return fail(PS_ERR_INVALID, "ps_rhs_static: lengths must be positive");
+    cells *= desc->n[a];
+  }
+  if (!(desc->gamma > 1.0)) return fail(PS_ERR_INVALID, "ps_rhs_static: gamma must exceed 1");
+  if (cells > kMaxCells) {
+    char msg[200];
+    snprintf(msg, sizeof(msg), "ps_rhs_static: grid of %ld cells exceeds the static scratch limit of %ld cells",
+             cells, kMaxCells);
+    return fail(PS_ERR_UNSUPPORTED, msg);
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: device ordinal out of range");
+  float* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_addr_mutex);
+    if (g_addr[dev] == nullptr) {
+      void* ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_rhs_static_scratch);
+      if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress");
+      g_addr[dev] = static_cast<float*>(ptr);
+    }
+    base = g_addr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nd = desc->ndim, nc = nd + 2;
+  ps::AxisOps ax[3];
+  for (int a = 0; a < nd; ++a) {
+    const int N = desc->n[a];
+    float* tab = base + a * kAxisFloats;
+    float* P = tab;
+    float* d = tab + kMaxN;
+    float2* twf = reinterpret_cast<float2*>(tab + 2 * kMaxN);
+    float2* twi = reinterpret_cast<float2*>(tab + 4 * kMaxN);
+    k_static_axis<<<(N + 127) / 128, 128, 0, s>>>(N, threads_per_pencil(N), desc->length[a], desc->dealias,
+                                                  desc->filter_enabled, desc->filter_p, desc->filter_alpha, P, d,
+                                                  twf, twi);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "table kernel");
+    ax[a] = ps::AxisOps{P, d, twf, twi};
+  }
+  float* eref = base + kErefOffset;
+  float* G = base + kGOffset;
+  float* AB = base + kABOffset;
+  const int nx = desc->n[0], ny = desc->n[1], nz = (nd == 3) ? desc->n[2] : 1;
+  if ((e = ps::launch_eref_set(U + (long)(nc - 1) * cells, eref, s)) != cudaSuccess)
+    return fail_cuda(e, "energy reference");
+
+  ps::XFirstArgs xa{};
+  xa.U = U;
+  xa.Uw = nullptr;
+  xa.out = G;
+  xa.fs = cells;
+  xa.rows = (int)(cells / nx);
+  xa.ax = ax[0];
+  xa.gamma = (float)desc->gamma;
+  xa.speed = nullptr;
+  xa.eref = eref;
+  xa.shift_in = 1;
+  e = ps::dispatch_n(nx, [&](auto n) { return ps::launch_xfirst<decltype(n)::value>(nd, xa, s); });
+  if (e != cudaSuccess) return fail_cuda(e, "x pass");
+
+  const ps::StridedGeom gy{nx, (long)nx, (long)nx * ny, nz};
+  if (nd == 3) {
+    ps::YMidArgs ya{};
+    ya.in = G;
+    ya.out = AB;
+    ya.fs = cells;
+    ya.g = gy;
+    ya.ax = ax[1];
+    e = ps::dispatch_n(ny, [&](auto n) { return ps::launch_ymid3<decltype(n)::value>(ya, s); });
+    if (e != cudaSuccess) return fail_cuda(e, "y pass");
+  }
+  ps::LastArgs la{};
+  if (nd == 3) {
+    la.a = AB;
+    la.b = AB + 5 * cells;
+    la.g = ps::StridedGeom{nx, (long)nx * ny, (long)nx, ny};
+    la.ax = ax[2];
+  } else {
+    la.a = G;
+    la.b = G + (long)nc * cells;
+    la.g = gy;
+    la.ax = ax[1];
+  }
+  la.fs = cells;
+  la.stage = -1;
+  la.Un = U;
+  la.acc = nullptr;
+  la.out = rhs;
+  la.dt_dev = nullptr;
+  la.dt = 0.0;
+  la.gamma = (float)desc->gamma;
+  la.rho_min = 1e-8f;
+  la.p_min = 1e-10f;
+  la.eref = eref;
+  la.filter_last = 0;
+  const int nlast = (nd == 3) ? nz : ny;
+  e = ps::dispatch_n(nlast, [&](auto n) { return ps::launch_last<decltype(n)::value>(nd, la, s); });
+  if (e != cudaSuccess) return fail_cuda(e, "last pass");
+  return PS_OK;
+}
