@@ -1,0 +1,211 @@
+"""Fourier grids with the reference's constructor signatures and operators,
+backed by the CUDA engine (backend "gb300").
+
+Mirrors phrike/grid.py: Grid1D (lines 144-735), Grid2D (775-1354) and
+Grid3D (1357-1744).  Arrays are float32 torch tensors on the grid's CUDA
+device, component-first with spatial axes (..., [Nz,] [Ny,] Nx).  NumPy
+inputs are moved to the device on entry.  Attributes keep the reference's
+names and values (x, y, z, dx, dy, dz, k*, dealias_mask, filter_sigma).
+"""
+from __future__ import annotations
+
+from typing import Any, Dict, Optional, Tuple
+
+import numpy as np
+import torch
+
+from .engine import Plan
+
+
+def _fftfreq_k(n: int, length: float) -> np.ndarray:
+    return 2.0 * np.pi * np.fft.fftfreq(n, d=length / n)
+
+
+def _mask_1d(n: int, dealias: bool) -> np.ndarray:
+    if not dealias:
+        return np.ones(n)
+    k = np.fft.fftfreq(n) * n
+    return (np.abs(k) <= n // 3).astype(float)
+
+
+def _sigma_1d(n: int, fp: Optional[Dict]) -> np.ndarray:
+    if not (fp and bool(fp.get("enabled", False))):
+        return np.ones(n)
+    p = int(fp.get("p", 8))
+    alpha = float(fp.get("alpha", 36.0))
+    k = np.fft.fftfreq(n) * n
+    kmax = np.max(np.abs(k)) if n > 0 else 1.0
+    return np.exp(-alpha * (np.abs(k) / max(kmax, 1.0)) ** p)
+
+
+def _check_backend(backend: str, basis: str = "fourier") -> None:
+    if str(backend).lower() != "gb300":
+        raise ValueError(f"phrike_gb300 grids implement backend 'gb300' only (got {backend!r})")
+    if str(basis).lower() != "fourier":
+        raise ValueError(f"Unknown or unsupported basis for the gb300 Fourier grids: {basis!r}")
+
+
+class _FourierGridBase:
+    """Shared device plumbing: the plan, tensor conversion, operators."""
+
+    _shape: Tuple[int, ...]
+    _lengths: Tuple[float, ...]
+
+    def _init_plan(self, dealias: bool, filter_params: Optional[Dict], torch_device: Optional[str],
+                   precision: str, gamma: float = 1.4) -> None:
+        if precision not in ("single", "double"):
+            raise ValueError(f"precision must be 'single' or 'double' (got {precision!r})")
+        # the engine computes in float32 whatever the requested precision
+        self.precision = precision
+        dev = torch.device(torch_device if torch_device else "cuda")
+        if dev.type != "cuda":
+            raise RuntimeError("backend 'gb300' runs on a CUDA device only")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.torch_device = str(dev)
+        self.device = dev
+        self.filter_params = filter_params
+        self.dealias = dealias
+        self._gamma = gamma
+        self._plans: Dict[float, Plan] = {}
+        self.plan = self._plan_for(gamma)
+
+    def _plan_for(self, gamma: float) -> Plan:
+        g = float(gamma)
+        if g not in self._plans:
+            self._plans[g] = Plan(self._shape, self._lengths, gamma=g, dealias=self.dealias,
+                                  filter_params=self.filter_params, device=self.device)
+        return self._plans[g]
+
+    def to_device(self, f: Any) -> torch.Tensor:
+        if isinstance(f, torch.Tensor):
+            t = f
+            if t.device != self.device or t.dtype != torch.float32:
+                t = t.to(device=self.device, dtype=torch.float32)
+        else:
+            t = torch.as_tensor(np.asarray(f), dtype=torch.float32, device=self.device)
+        return t.contiguous()
+
+    def _op(self, f: Any, axis: int) -> torch.Tensor:
+        t = self.to_device(f)
+        shape = t.shape
+        return self.plan.derivative(t.reshape((-1,) + self._shape), axis).reshape(shape)
+
+    def apply_spectral_filter(self, f: Any) -> torch.Tensor:
+        t = self.to_device(f)
+        shape = t.shape
+        return self.plan.filter(t.reshape((-1,) + self._shape)).reshape(shape)
+
+    def apply_boundary_conditions(self, U: Any, equations: Any = None) -> Any:
+        """Periodic Fourier grids have no boundary conditions (grid.py:631-632, 1087-1089)."""
+        return U
+
+
+class Grid1D(_FourierGridBase):
+    """1D periodic Fourier grid (reference: phrike/grid.py:144-735)."""
+
+    def __init__(self, N: int, Lx: float, basis: str = "fourier", bc: Optional[str] = None,
+                 dealias: bool = True, filter_params: Optional[Dict[str, float]] = None, fft_workers: int = 1,
+                 backend: str = "gb300", torch_device: Optional[str] = None, precision: str = "single",
+                 debug: bool = False, problem_config: Optional[Dict[str, Any]] = None):
+        _check_backend(backend, basis)
+        self.N, self.Lx, self.basis, self.bc = int(N), float(Lx), basis, bc
+        self.fft_workers, self.backend, self.debug, self.problem_config = fft_workers, backend, debug, problem_config
+        self._shape = (self.N,)
+        self._lengths = (self.Lx,)
+        self.dx = self.Lx / self.N
+        self._init_plan(dealias, filter_params, torch_device, precision)
+        self.x = torch.linspace(0.0, self.Lx, self.N + 1, dtype=torch.float64)[:-1].to(self.device)
+        self.k = torch.as_tensor(_fftfreq_k(self.N, self.Lx), device=self.device)
+        self.ik = 1j * self.k
+        self.dealias_mask = torch.as_tensor(_mask_1d(self.N, dealias), device=self.device)
+        self.filter_sigma = torch.as_tensor(_sigma_1d(self.N, filter_params), device=self.device)
+
+    def dx1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 0)
+
+
+class Grid2D(_FourierGridBase):
+    """2D periodic Fourier grid, spatial axes (Ny, Nx) (reference: phrike/grid.py:775-1354)."""
+
+    def __init__(self, Nx: int, Ny: int, Lx: float, Ly: float, dealias: bool = True,
+                 filter_params: Optional[Dict[str, float]] = None, fft_workers: int = 1,
+                 backend: str = "gb300", torch_device: Optional[str] = None, precision: str = "single",
+                 debug: bool = False, basis_x: str = "fourier", basis_y: str = "fourier",
+                 bc: str = "dirichlet", bc_config: Optional[Dict[str, Any]] = None):
+        _check_backend(backend, basis_x)
+        _check_backend(backend, basis_y)
+        self.Nx, self.Ny, self.Lx, self.Ly = int(Nx), int(Ny), float(Lx), float(Ly)
+        self.basis_x, self.basis_y, self.bc, self.bc_config = basis_x, basis_y, bc, bc_config
+        self.fft_workers, self.backend, self.debug = fft_workers, backend, debug
+        self._shape = (self.Ny, self.Nx)
+        self._lengths = (self.Ly, self.Lx)
+        self.dx, self.dy = self.Lx / self.Nx, self.Ly / self.Ny
+        self.dx_min = None
+        self.dy_min = None
+        self._init_plan(dealias, filter_params, torch_device, precision)
+        self.x = torch.as_tensor(np.linspace(0.0, self.Lx, self.Nx, endpoint=False), device=self.device)
+        self.y = torch.as_tensor(np.linspace(0.0, self.Ly, self.Ny, endpoint=False), device=self.device)
+        self.kx = torch.as_tensor(_fftfreq_k(self.Nx, self.Lx), device=self.device)
+        self.ky = torch.as_tensor(_fftfreq_k(self.Ny, self.Ly), device=self.device)
+        self.ikx = (1j * self.kx)[None, :]
+        self.iky = (1j * self.ky)[:, None]
+        mx, my = _mask_1d(self.Nx, dealias), _mask_1d(self.Ny, dealias)
+        sx, sy = _sigma_1d(self.Nx, filter_params), _sigma_1d(self.Ny, filter_params)
+        self.dealias_mask = torch.as_tensor(my[:, None] * mx[None, :], device=self.device)
+        self.filter_sigma = torch.as_tensor(sy[:, None] * sx[None, :], device=self.device)
+
+    def dx1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 0)
+
+    def dy1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 1)
+
+    def xy_mesh(self) -> Tuple[torch.Tensor, torch.Tensor]:
+        Y, X = torch.meshgrid(self.y, self.x, indexing="ij")
+        return X, Y
+
+
+class Grid3D(_FourierGridBase):
+    """3D periodic Fourier grid, spatial axes (Nz, Ny, Nx) (reference: phrike/grid.py:1357-1744)."""
+
+    def __init__(self, Nx: int, Ny: int, Nz: int, Lx: float, Ly: float, Lz: float, dealias: bool = True,
+                 filter_params: Optional[Dict[str, float]] = None, fft_workers: int = 1,
+                 backend: str = "gb300", torch_device: Optional[str] = None, precision: str = "single",
+                 debug: bool = False):
+        _check_backend(backend)
+        self.Nx, self.Ny, self.Nz = int(Nx), int(Ny), int(Nz)
+        self.Lx, self.Ly, self.Lz = float(Lx), float(Ly), float(Lz)
+        self.fft_workers, self.backend, self.debug = fft_workers, backend, debug
+        self._shape = (self.Nz, self.Ny, self.Nx)
+        self._lengths = (self.Lz, self.Ly, self.Lx)
+        self.dx, self.dy, self.dz = self.Lx / self.Nx, self.Ly / self.Ny, self.Lz / self.Nz
+        self._init_plan(dealias, filter_params, torch_device, precision)
+        self.x = torch.as_tensor(np.linspace(0.0, self.Lx, self.Nx, endpoint=False), device=self.device)
+        self.y = torch.as_tensor(np.linspace(0.0, self.Ly, self.Ny, endpoint=False), device=self.device)
+        self.z = torch.as_tensor(np.linspace(0.0, self.Lz, self.Nz, endpoint=False), device=self.device)
+        self.kx = torch.as_tensor(_fftfreq_k(self.Nx, self.Lx), device=self.device)
+        self.ky = torch.as_tensor(_fftfreq_k(self.Ny, self.Ly), device=self.device)
+        self.kz = torch.as_tensor(_fftfreq_k(self.Nz, self.Lz), device=self.device)
+        self.ikx = (1j * self.kx)[None, None, :]
+        self.iky = (1j * self.ky)[None, :, None]
+        self.ikz = (1j * self.kz)[:, None, None]
+        m = [_mask_1d(n, dealias) for n in (self.Nz, self.Ny, self.Nx)]
+        s = [_sigma_1d(n, filter_params) for n in (self.Nz, self.Ny, self.Nx)]
+        self.dealias_mask = torch.as_tensor(m[0][:, None, None] * m[1][None, :, None] * m[2][None, None, :],
+                                            device=self.device)
+        self.filter_sigma = torch.as_tensor(s[0][:, None, None] * s[1][None, :, None] * s[2][None, None, :],
+                                            device=self.device)
+
+    def dx1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 0)
+
+    def dy1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 1)
+
+    def dz1(self, f: Any) -> torch.Tensor:
+        return self._op(f, 2)
+
+    def xyz_mesh(self) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        Z, Y, X = torch.meshgrid(self.z, self.y, self.x, indexing="ij")
+        return X, Y, Z

@@ -1,0 +1,156 @@
+"""Fixed-step RK4 solvers with the reference's interface (backend "gb300").
+
+Mirrors SpectralSolver1D/2D/3D of phrike/solver.py (lines 135-422, 527-812,
+1237-1513): same constructor arguments, compute_dt / step / run methods, the
+same history keys and the same CFL run loop.  A step is one call into the C
+ABI (ps_step_rk4), which runs the fused pass kernels including the clamp and
+the filter cadence; the plan's step counter plays the role of the
+reference's _step_counter.  step() is functional like the reference: it
+returns a new tensor and leaves its argument untouched.
+"""
+from __future__ import annotations
+
+from typing import Any, Callable, Dict, List, Optional
+
+import torch
+
+from .engine import Plan
+
+
+class _SpectralSolverBase:
+    _ndim = 1
+    _history_keys: List[str] = []
+
+    def __init__(self, grid, equations, U0: Optional[Any] = None, scheme: str = "rk4", cfl: float = 0.4,
+                 adaptive_config: Optional[Dict] = None, artificial_viscosity_config: Optional[Dict] = None,
+                 gravity_config: Optional[Dict] = None):
+        if str(scheme).lower() != "rk4":
+            raise NotImplementedError(f"backend 'gb300' implements the fixed-step rk4 scheme (got {scheme!r})")
+        if adaptive_config and adaptive_config.get("enabled", False):
+            raise NotImplementedError("backend 'gb300': adaptive embedded RK is not implemented")
+        if artificial_viscosity_config and artificial_viscosity_config.get("enabled", False):
+            raise NotImplementedError("backend 'gb300': artificial viscosity is not implemented")
+        gravity = None
+        if gravity_config and gravity_config.get("enabled", False):
+            if self._ndim != 1:
+                raise NotImplementedError("backend 'gb300': gravity is implemented for 1D only")
+            gravity = [float(gravity_config.get("gx", 0.0))]
+        self.grid = grid
+        self.equations = equations
+        self.scheme = "rk4"
+        self.cfl = float(cfl)
+        self.t = 0.0
+        self.U = U0
+        self.adaptive_enabled = False
+        self.artificial_viscosity = None
+        self.gravity_config = gravity_config
+        fp = dict(getattr(grid, "filter_params", None) or {})
+        interval = fp.get("interval", None)
+        self.filter_interval = max(1, int(interval)) if interval is not None else 1
+        fp["interval"] = self.filter_interval
+        self.plan = Plan(grid._shape, grid._lengths, gamma=float(equations.gamma), dealias=grid.dealias,
+                         filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device)
+
+    # -- reference interface -----------------------------------------------
+    def _spacing(self) -> float:
+        raise NotImplementedError
+
+    def compute_dt(self, U: Any) -> float:
+        s = float(self.plan.max_wave_speed(self.grid.to_device(U)).item())
+        if s <= 0.0:
+            return 1e-6
+        return self.cfl * self._spacing() / s
+
+    def step(self, U: Any, dt: float) -> torch.Tensor:
+        V = self.grid.to_device(U).clone()
+        self.plan.step_(V, float(dt))
+        return V
+
+    def _record(self, history: Dict[str, List[float]]) -> None:
+        cons = self.plan.conserved(self.U).tolist()
+        history["time"].append(self.t)
+        for key, v in zip(self._history_keys, cons):
+            history[key].append(v)
+
+    def run(self, U0: Any, t0: float, t_end: float, output_interval: float = 0.1,
+            checkpoint_interval: float = 0.0, outdir: Optional[str] = None,
+            on_output: Optional[Callable[[float, Any], None]] = None,
+            on_step: Optional[Callable[[int, float, Any], None]] = None, tracers: Optional[Any] = None,
+            dt: Optional[float] = None) -> Dict[str, List[float]]:
+        """CFL-driven loop of the reference (solver.py:338-422); with ``dt``
+        given, fixed steps of that size instead."""
+        if tracers is not None:
+            raise NotImplementedError("backend 'gb300': tracers are not implemented")
+        self.U = self.grid.to_device(U0).clone()
+        self.t = float(t0)
+        next_output = self.t + output_interval
+        history: Dict[str, List[float]] = {"time": [], **{k: [] for k in self._history_keys}}
+        self._record(history)
+        if on_output is not None:
+            on_output(self.t, self.U)
+        step_dt = float(dt) if dt is not None else self.compute_dt(self.U)
+        step_count = 0
+        while self.t < t_end - 1e-12:
+            h = min(step_dt, t_end - self.t)
+            self.plan.step_(self.U, h)
+            self.t += h
+            if on_step is not None:
+                on_step(step_count, h, self.U)
+            step_count += 1
+            if dt is None:
+                step_dt = self.compute_dt(self.U)
+            if self.t + 1e-12 >= next_output:
+                self._record(history)
+                if on_output is not None:
+                    on_output(self.t, self.U)
+                next_output += output_interval
+        self._record(history)
+        if on_output is not None:
+            on_output(self.t, self.U)
+        return history
+
+
+class SpectralSolver1D(_SpectralSolverBase):
+    """phrike/solver.py:135-422; CFL dt = cfl * dx / max(|u| + a)."""
+
+    _ndim = 1
+    _history_keys = ["mass", "momentum", "energy"]
+
+    def __init__(self, grid, equations, U0=None, scheme="rk4", cfl=0.4, adaptive_config=None,
+                 artificial_viscosity_config=None, gravity_config=None):
+        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, artificial_viscosity_config,
+                         gravity_config)
+
+    def _spacing(self) -> float:
+        return self.grid.dx
+
+
+class SpectralSolver2D(_SpectralSolverBase):
+    """phrike/solver.py:527-812; CFL dt = cfl * min(dx, dy) / max(|u_x| + a)."""
+
+    _ndim = 2
+    _history_keys = ["mass", "momentum_x", "momentum_y", "energy"]
+
+    def __init__(self, grid, equations, U0=None, scheme="rk4", cfl=0.3, adaptive_config=None,
+                 artificial_viscosity_config=None, gravity_config=None):
+        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, artificial_viscosity_config,
+                         gravity_config)
+
+    def _spacing(self) -> float:
+        dx = getattr(self.grid, "dx_min", None) or self.grid.dx
+        dy = getattr(self.grid, "dy_min", None) or self.grid.dy
+        return min(dx, dy)
+
+
+class SpectralSolver3D(_SpectralSolverBase):
+    """phrike/solver.py:1237-1513; CFL dt = cfl * min(dx, dy, dz) / max(max_i |u_i| + a)."""
+
+    _ndim = 3
+    _history_keys = ["mass", "momentum_x", "momentum_y", "momentum_z", "energy"]
+
+    def __init__(self, grid, equations, U0=None, scheme="rk4", cfl=0.25, adaptive_config=None,
+                 artificial_viscosity_config=None, gravity_config=None):
+        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, None, gravity_config)
+
+    def _spacing(self) -> float:
+        return min(self.grid.dx, self.grid.dy, self.grid.dz)
