@@ -107,6 +107,13 @@ int ps_max_wave_speed(ps_plan plan, const float* U, float* d_out, void* stream);
  * solvers' record() (solver.py:372-377, 741-767, 1439-1468). */
 int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);
 
+/* Device status word of a plan, read synchronously: 0 = healthy; bit
+ * PS_STATUS_TMA_TIMEOUT = a kernel gave up waiting for a tile load (bounded
+ * wait) and its results are invalid.  No reference counterpart: the
+ * reference raises Python exceptions only (grid.py:79-84, 305-308). */
+#define PS_STATUS_TMA_TIMEOUT 1
+int ps_plan_status(ps_plan plan, int* status);
+
 /* Launch profiling: when enabled, every pass launch is bracketed by CUDA
  * events on its stream and tagged with its kind and the algorithmic bytes it
  * moves.  ps_profile_collect waits for the recorded events, fills per-kind

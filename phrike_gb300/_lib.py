@@ -53,6 +53,7 @@ _SIGNATURES = [
     ("ps_max_wave_speed", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_conserved", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_plan_ncomp", C.c_int, [C.c_void_p]),
+    ("ps_plan_status", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("ps_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),

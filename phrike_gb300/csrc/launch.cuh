@@ -5,6 +5,7 @@
 
 #include "euler1d.cuh"
 #include "euler_passes.cuh"
+#include "passes_tma.cuh"
 
 namespace ps {
 
@@ -13,6 +14,17 @@ template <int N> cudaError_t launch_ymid3(const YMidArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_last(int nd, const LastArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
+
+// TMA strided passes: columns per tile and ring depth per pencil length
+template <int N> struct TmaTile {
+  static constexpr int T = (N >= 1024) ? 8 : 16;
+  static constexpr int R = 4;
+};
+template <int N> cudaError_t launch_ymid3_t(const CUtensorMap& mG, const YMidTArgs& a, cudaStream_t s);
+template <int N>
+cudaError_t launch_last_t(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, const CUtensorMap& mAcc,
+                          const LastTArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_op_t(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s);
 
 inline bool supported_n(int n) {
   return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
@@ -103,6 +115,42 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
       if ((e = set_smem(k_op<NN, T, false>, sm)) != cudaSuccess) return e;                            \
       k_op<NN, T, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                       \
     }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_ymid3_t<NN>(const CUtensorMap& mG, const YMidTArgs& a, cudaStream_t s) {         \
+    constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_ymid3_t<NN, T, R>, sm)) != cudaSuccess) return e;                             \
+    k_ymid3_t<NN, T, R><<<grid, Shape<NN>::A * T, sm, s>>>(mG, a);                                    \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_last_t<NN>(int nd, const CUtensorMap& mAB, const CUtensorMap& mU,                \
+                                const CUtensorMap& mAcc, const LastTArgs& a, cudaStream_t s) {        \
+    constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
+    cudaError_t e;                                                                                    \
+    if (nd == 3) {                                                                                    \
+      if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;                  \
+      k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);              \
+    } else {                                                                                          \
+      if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;                   \
+      k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);               \
+    }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_op_t<NN>(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {             \
+    constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_op_t<NN, T, R>, sm)) != cudaSuccess) return e;                                \
+    k_op_t<NN, T, R><<<grid, Shape<NN>::A * T, sm, s>>>(mIn, a);                                      \
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \

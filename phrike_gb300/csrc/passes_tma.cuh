@@ -1,0 +1,541 @@
+// TMA-fed strided pencil passes (pencils along y or z).
+//
+// Same arithmetic as k_ymid3 / k_last / k_op in euler_passes.cuh, but every
+// input field tile ([N rows] x [T adjacent x columns], one 4-D tensor-map box
+// per 256 rows) is streamed by the tensor memory accelerator into a ring of R
+// shared-memory slots.  One elected thread issues the loads R tiles ahead of
+// consumption; all threads wait on the slot's mbarrier (bounded), copy their
+// pencil points out of shared memory and release the slot.  DRAM latency is
+// thereby overlapped with the FFT work of earlier tiles instead of stalling
+// the warps that need the data.
+//
+// Field buffers are described by 4-D tensor maps over [nf][Nz][Ny][Nx]
+// float32 arrays, innermost first: dims {Nx, Ny, Nz, nf}.  Boxes are
+// {T, min(N,256), 1, 1} for y pencils and {T, 1, min(N,256), 1} for z
+// pencils; either lands in shared memory as rows of T floats.
+#pragma once
+#include "euler_passes.cuh"
+#include "tma.cuh"
+
+namespace ps {
+
+// resident CTAs per SM the register allocation must allow (about 512 threads)
+template <int N, int T>
+constexpr int tma_min_blocks() {
+  return (512 / (Shape<N>::A * T)) > 0 ? (512 / (Shape<N>::A * T)) : 1;
+}
+
+template <int N, int T>
+struct TileGeom {
+  static constexpr int BOX = (N < 256) ? N : 256;  // rows per TMA box
+  static constexpr int NBOX = N / BOX;
+  static constexpr uint32_t BYTES = N * T * 4;
+};
+
+// Ring of R tile slots with one mbarrier each.  Tile i lives in slot i % R
+// and completes phase (i / R) & 1 of that slot's barrier.
+template <int N, int T, int R>
+struct Ring {
+  alignas(1024) float slot[R][N * T];
+  uint64_t bar[R];
+  int abort;
+  int sched[64];  // tile schedule: map id * 64 + field
+  int ntiles;
+};
+
+// Which axis the pencils run along: 1 = y, 2 = z.
+struct TileIssue {
+  int axis;
+  int x0;     // first column of the tile
+  int outer;  // z (axis 1) or y (axis 2)
+};
+
+template <int N, int T, int R>
+__device__ __forceinline__ void ring_issue(Ring<N, T, R>& rg, int i, const CUtensorMap* const* maps,
+                                           const TileIssue& ti) {
+  using G = TileGeom<N, T>;
+  const int s = i % R;
+  const int code = rg.sched[i];
+  const CUtensorMap* m = maps[code >> 6];
+  const int f = code & 63;
+  mbar_arrive_expect_tx(&rg.bar[s], G::BYTES);
+#pragma unroll
+  for (int b = 0; b < G::NBOX; ++b) {
+    float* dst = &rg.slot[s][b * G::BOX * T];
+    if (ti.axis == 1) tma_load_4d(dst, m, ti.x0, b * G::BOX, ti.outer, f, &rg.bar[s]);
+    else tma_load_4d(dst, m, ti.x0, ti.outer, b * G::BOX, f, &rg.bar[s]);
+  }
+}
+
+// Consumer side of the ring.  `issued` lives in thread 0 only.
+template <int N, int T, int R>
+struct RingCursor {
+  Ring<N, T, R>& rg;
+  const CUtensorMap* const* maps;
+  TileIssue ti;
+  int* status;
+  int issued;  // thread 0: tiles issued so far
+
+  __device__ void start() {
+    if (threadIdx.x == 0) {
+      issued = 0;
+      while (issued < rg.ntiles && issued < R) ring_issue<N, T, R>(rg, issued++, maps, ti);
+    }
+  }
+  // wait for tile i and return its slot
+  __device__ const float* wait(int i) {
+    const int s = i % R;
+    if (!*(volatile int*)&rg.abort) {
+      if (!mbar_wait(&rg.bar[s], (uint32_t)((i / R) & 1), status)) *(volatile int*)&rg.abort = 1;
+    }
+    return rg.slot[s];
+  }
+  // all threads are done with tiles <= i: refill freed slots
+  __device__ void release(int i) {
+    __syncthreads();
+    if (threadIdx.x == 0 && !*(volatile int*)&rg.abort) {
+      while (issued < rg.ntiles && issued <= i + R) ring_issue<N, T, R>(rg, issued++, maps, ti);
+    }
+  }
+  // before exit: every issued tile must have landed (bounded waits)
+  __device__ void drain(int consumed) {
+    if (threadIdx.x == 0) {
+      for (int i = consumed; i < issued; ++i) mbar_wait(&rg.bar[i % R], (uint32_t)((i / R) & 1), status);
+    }
+  }
+};
+
+template <int N, int T, int R>
+__device__ __forceinline__ void ring_init(Ring<N, T, R>& rg) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R; ++s) mbar_init(&rg.bar[s], 1);
+    rg.abort = 0;
+    fence_barrier_init();
+  }
+}
+
+// pair (fa, fb) of this thread's pencil points from two tiles
+template <int N, int T>
+__device__ __forceinline__ void tile_pair(float2 (&v)[Shape<N>::B], const float* ta, const float* tb, int t,
+                                          int p) {
+  constexpr int A = Shape<N>::A;
+#pragma unroll
+  for (int n2 = 0; n2 < Shape<N>::B; ++n2) {
+    const int r = (t + A * n2) * T + p;
+    v[n2] = make_float2(ta[r], tb ? tb[r] : 0.0f);
+  }
+}
+
+template <int N, int T, int R>
+struct TmaStridedSmem {
+  AxisSmem<N> ax;
+  float2 buf[Pencil<N, T, true>::BUF];
+  Ring<N, T, R> ring;
+};
+
+// ---------------------------------------------------------------------------
+// 3D y pass.  Map 0 = G buffer (15 fields: G, Hy, Hz).  Output via st.global.
+// ---------------------------------------------------------------------------
+struct YMidTArgs {
+  float* out;      // 10 fields [A(5), B(5)]
+  long fs;
+  StridedGeom g;
+  AxisOps ax;
+  int* status;
+};
+
+template <int N, int T, int R>
+__global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
+    k_ymid3_t(const __grid_constant__ CUtensorMap mG, YMidTArgs a) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  using PF = Pencil<N, T, true>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  const int p = threadIdx.x % T, t = threadIdx.x / T;
+  const int col = blockIdx.x * T + p;
+  const int outer = blockIdx.y;
+  PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
+  ring_init(S.ring);
+  if (threadIdx.x == 0) {
+    // A pairs: (G_c, Hy_c) for c = 0..4 consumed two components at a time, then Hz pairs
+    const int order[15] = {0, 5, 1, 6, 2, 7, 3, 8, 4, 9, 10, 11, 12, 13, 14};
+    for (int i = 0; i < 15; ++i) S.ring.sched[i] = order[i];
+    S.ring.ntiles = 15;
+  }
+  load_axis<N>(S.ax, a.ax);
+  __syncthreads();
+  const CUtensorMap* maps[1] = {&mG};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{1, (int)(blockIdx.x * T), outer}, a.status, 0};
+  rc.start();
+  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long step = (long)A * a.g.as;
+  const bool valid = col < a.g.ncol;
+  int ti = 0;
+#pragma unroll 1
+  for (int c = 0; c < 5; c += 2) {
+    const bool two = c + 1 < 5;
+    float2 w[B];
+    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
+    rc.release(ti + 1);
+    ti += 2;
+    pf.fwd(w);
+    combine_pd<N, T>(w, pf, S.ax, 1.0f);
+    if (two) {
+      float2 w2[B];
+      tile_pair<N, T>(w2, rc.wait(ti), rc.wait(ti + 1), t, p);
+      rc.release(ti + 1);
+      ti += 2;
+      pf.fwd(w2);
+      combine_pd<N, T>(w2, pf, S.ax, 1.0f);
+#pragma unroll
+      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
+    }
+    pf.inv(w);
+    if (valid) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        a.out[c * a.fs + base + n2 * step] = w[n2].x;
+        if (two) a.out[(c + 1) * a.fs + base + n2 * step] = w[n2].y;
+      }
+    }
+  }
+#pragma unroll 1
+  for (int c = 0; c < 5; c += 2) {
+    const bool two = c + 1 < 5;
+    float2 w[B];
+    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);
+    rc.release(ti + (two ? 1 : 0));
+    ti += two ? 2 : 1;
+    pf.fwd(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const float s = S.ax.P[pf.kidx(r)];
+      w[r].x *= s;
+      w[r].y *= s;
+    }
+    pf.inv(w);
+    if (valid) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        a.out[(5 + c) * a.fs + base + n2 * step] = w[n2].x;
+        if (two) a.out[(6 + c) * a.fs + base + n2 * step] = w[n2].y;
+      }
+    }
+  }
+  rc.drain(ti);
+}
+
+// ---------------------------------------------------------------------------
+// Last pass with TMA inputs.  Maps: 0 = a/b buffer (a_c at field fa0 + c, b_c
+// at fb0 + c), 1 = U^n, 2 = accumulator.  Writes via st.global.
+// ---------------------------------------------------------------------------
+struct LastTArgs {
+  int fa0, fb0;        // field offsets of a_0 and b_0 in map 0
+  float* acc;          // accumulator (written)
+  float* out;          // rhs / next stage input / new state
+  long fs;
+  StridedGeom g;
+  int axis;            // 1: y pencils, 2: z pencils
+  AxisOps ax;
+  int stage;           // -1 rhs only, 0..3 RK4 stage
+  const float* Un;     // U^n (global; used by the clamped variant)
+  const double* dt_dev;
+  double dt;
+  float gamma;
+  float rho_min, p_min;
+  const float* eref;
+  int filter_last;
+  int* status;
+};
+
+template <int N, int T, int ND, bool CLAMP, int R>
+__global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
+    k_last_t(const __grid_constant__ CUtensorMap mAB, const __grid_constant__ CUtensorMap mU,
+             const __grid_constant__ CUtensorMap mAcc, LastTArgs a) {
+  constexpr int NC = ND + 2;
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  using PF = Pencil<N, T, true>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  const int p = threadIdx.x % T, t = threadIdx.x / T;
+  const int col = blockIdx.x * T + p;
+  const int outer = blockIdx.y;
+  const bool valid = col < a.g.ncol;
+  PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
+  ring_init(S.ring);
+  const bool need_un = !CLAMP && a.stage >= 0 && a.stage != 3;
+  const bool need_acc = !CLAMP && a.stage >= 1;
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int c = 0; c < NC; c += 2) {
+      const int m = (c + 1 < NC) ? 2 : 1;
+      for (int q = 0; q < m; ++q) {
+        S.ring.sched[n++] = a.fa0 + c + q;
+        S.ring.sched[n++] = a.fb0 + c + q;
+      }
+      if (need_un)
+        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 64 + c + q;
+      if (need_acc)
+        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 128 + c + q;
+    }
+    S.ring.ntiles = n;
+  }
+  load_axis<N>(S.ax, a.ax);
+  __syncthreads();
+  const CUtensorMap* maps[3] = {&mAB, &mU, &mAcc};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer}, a.status, 0};
+  rc.start();
+  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long step = (long)A * a.g.as;
+  const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
+  const RKCoef rk = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
+  const float pmin_shift = a.p_min - (a.gamma - 1.0f) * (*a.eref);
+  auto addr = [&](int c, int n2) { return c * a.fs + base + n2 * step; };
+  auto filter_pair = [&](float2 (&w)[B]) {  // complementary form
+    float2 w0[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) w0[r] = w[r];
+    pf.fwd(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];
+      w[r].x *= q;
+      w[r].y *= q;
+    }
+    pf.inv(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
+  };
+  int ti = 0;
+  // spectra of -(P a_c + D b_c) for components (c, c+1), inverse-transformed
+  auto rhs_pair = [&](int c, float2 (&w)[B]) {
+    const bool two = c + 1 < NC;
+    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
+    rc.release(ti + 1);
+    ti += 2;
+    pf.fwd(w);
+    combine_pd<N, T>(w, pf, S.ax, -1.0f);
+    if (two) {
+      float2 w2[B];
+      tile_pair<N, T>(w2, rc.wait(ti), rc.wait(ti + 1), t, p);
+      rc.release(ti + 1);
+      ti += 2;
+      pf.fwd(w2);
+      combine_pd<N, T>(w2, pf, S.ax, -1.0f);
+#pragma unroll
+      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
+    }
+    pf.inv(w);
+  };
+
+  if constexpr (!CLAMP) {
+#pragma unroll 1
+    for (int c = 0; c < NC; c += 2) {
+      const bool two = c + 1 < NC;
+      const int m = two ? 2 : 1;
+      float2 w[B];
+      rhs_pair(c, w);
+      if (a.stage < 0) {
+        if (valid) {
+#pragma unroll
+          for (int n2 = 0; n2 < B; ++n2) {
+            a.out[addr(c, n2)] = w[n2].x;
+            if (two) a.out[addr(c + 1, n2)] = w[n2].y;
+          }
+        }
+        continue;
+      }
+      const float* tu[2] = {nullptr, nullptr};
+      const float* tacc[2] = {nullptr, nullptr};
+      if (need_un) {
+        for (int q = 0; q < m; ++q) tu[q] = rc.wait(ti + q);
+        ti += m;
+      }
+      if (need_acc) {
+        for (int q = 0; q < m; ++q) tacc[q] = rc.wait(ti + q);
+        ti += m;
+      }
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const int r = (t + A * n2) * T + p;
+        const float k[2] = {w[n2].x, w[n2].y};
+        float res[2] = {0.0f, 0.0f};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          if (q == 1 && !two) break;
+          if (a.stage == 3) {
+            res[q] = fmaf(rk.wacc, k[q], tacc[q][r]);
+          } else {
+            const float un = tu[q][r];
+            const float ac = fmaf(rk.wacc, k[q], (a.stage == 0) ? un : tacc[q][r]);
+            if (valid) a.acc[addr(c + q, n2)] = ac;
+            res[q] = fmaf(rk.wnext, k[q], un);
+          }
+        }
+        w[n2] = make_float2(res[0], res[1]);
+      }
+      if (need_un || need_acc) rc.release(ti - 1);
+      if (a.stage == 3 && a.filter_last) filter_pair(w);
+      if (valid) {
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          a.out[addr(c, n2)] = w[n2].x;
+          if (two) a.out[addr(c + 1, n2)] = w[n2].y;
+        }
+      }
+    }
+  } else {
+    float2 kk[(NC + 1) / 2][B];
+#pragma unroll
+    for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
+    if (a.stage < 0) {
+      if (valid) {
+#pragma unroll
+        for (int c = 0; c < NC; c += 2)
+#pragma unroll
+          for (int n2 = 0; n2 < B; ++n2) {
+            a.out[addr(c, n2)] = kk[c / 2][n2].x;
+            if (c + 1 < NC) a.out[addr(c + 1, n2)] = kk[c / 2][n2].y;
+          }
+      }
+    } else {
+      constexpr int CH = 4;  // positions per batch of epilogue loads
+#pragma unroll
+      for (int n0 = 0; n0 < B; n0 += CH) {
+        float un[CH][NC], ac[CH][NC];
+#pragma unroll
+        for (int j = 0; j < CH; ++j)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            un[j][c] = (valid && a.stage != 3) ? __ldg(a.Un + addr(c, n0 + j)) : 0.0f;
+            ac[j][c] = (valid && a.stage != 0) ? a.acc[addr(c, n0 + j)] : 0.0f;
+          }
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const int n2 = n0 + j;
+          float u[NC];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            const float k = (c & 1) ? kk[c / 2][n2].y : kk[c / 2][n2].x;
+            float res;
+            if (a.stage == 3) {
+              res = fmaf(rk.wacc, k, ac[j][c]);
+            } else {
+              ac[j][c] = fmaf(rk.wacc, k, (a.stage == 0) ? un[j][c] : ac[j][c]);
+              res = fmaf(rk.wnext, k, un[j][c]);
+            }
+            u[c] = valid ? res : ((c == 0) ? 1.0f : 0.0f);
+          }
+          clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            if (c & 1) kk[c / 2][n2].y = u[c];
+            else kk[c / 2][n2].x = u[c];
+          }
+        }
+        if (valid && a.stage != 3) {
+#pragma unroll
+          for (int j = 0; j < CH; ++j)
+#pragma unroll
+            for (int c = 0; c < NC; ++c) a.acc[addr(c, n0 + j)] = ac[j][c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NC; c += 2) {
+        if (a.stage == 3 && a.filter_last) filter_pair(kk[c / 2]);
+        if (valid) {
+#pragma unroll
+          for (int n2 = 0; n2 < B; ++n2) {
+            a.out[addr(c, n2)] = kk[c / 2][n2].x;
+            if (c + 1 < NC) a.out[addr(c + 1, n2)] = kk[c / 2][n2].y;
+          }
+        }
+      }
+    }
+  }
+  rc.drain(ti);
+}
+
+// ---------------------------------------------------------------------------
+// Strided one-axis operator (P, D or complementary P) with TMA inputs.
+// Map 0 = input buffer (fields 0..nf-1).  in and out may alias: a tile is
+// fully landed in shared memory before any point of it is written back.
+// ---------------------------------------------------------------------------
+struct OpTArgs {
+  float* out;
+  int nf;
+  long fs;
+  StridedGeom g;
+  int axis;
+  AxisOps ax;
+  int deriv;
+  float scale;
+  int complement;
+  int* status;
+};
+
+template <int N, int T, int R>
+__global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
+    k_op_t(const __grid_constant__ CUtensorMap mIn, OpTArgs a) {
+  constexpr int A = Shape<N>::A, B = Shape<N>::B;
+  using PF = Pencil<N, T, true>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  const int p = threadIdx.x % T, t = threadIdx.x / T;
+  const int col = blockIdx.x * T + p;
+  const int outer = blockIdx.y;
+  const bool valid = col < a.g.ncol;
+  PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
+  ring_init(S.ring);
+  if (threadIdx.x == 0) {
+    for (int f = 0; f < a.nf; ++f) S.ring.sched[f] = f;
+    S.ring.ntiles = a.nf;
+  }
+  load_axis<N>(S.ax, a.ax);
+  __syncthreads();
+  const CUtensorMap* maps[1] = {&mIn};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer}, a.status, 0};
+  rc.start();
+  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long step = (long)A * a.g.as;
+  const bool comp = a.complement && !a.deriv;
+  int ti = 0;
+#pragma unroll 1
+  for (int c = 0; c < a.nf; c += 2) {
+    const bool two = c + 1 < a.nf;
+    float2 w[B], w0[B];
+    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);
+    rc.release(ti + (two ? 1 : 0));
+    ti += two ? 2 : 1;
+#pragma unroll
+    for (int r = 0; r < B; ++r) w0[r] = w[r];
+    pf.fwd(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const int k = pf.kidx(r);
+      if (a.deriv) {
+        const float dd = a.scale * S.ax.d[k];
+        w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
+      } else {
+        const float s = comp ? (1.0f / N) - S.ax.P[k] : a.scale * S.ax.P[k];
+        w[r].x *= s;
+        w[r].y *= s;
+      }
+    }
+    pf.inv(w);
+    if (comp) {
+#pragma unroll
+      for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
+    }
+    if (valid) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        a.out[c * a.fs + base + n2 * step] = w[n2].x;
+        if (two) a.out[(c + 1) * a.fs + base + n2 * step] = w[n2].y;
+      }
+    }
+  }
+  rc.drain(ti);
+}
+
+}  // namespace ps

@@ -1,6 +1,8 @@
 // C ABI of the step engine: plan construction (spectral tables, scratch) and
 // the step / rhs / operator / reduction entry points declared in
 // include/phrike_gb300.h.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -68,6 +70,14 @@ struct ps_plan_s {
   float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
   float* speed = nullptr;
   float* eref = nullptr;  // E_ref of the energy-perturbation form (device scalar)
+  int* status = nullptr;  // device status word (PS_STATUS_* bits set by kernels)
+  // TMA tensor maps of the plan buffers and of the last state pointer seen
+  CUtensorMap map_G_y{};    // G, y pencils
+  CUtensorMap map_AB_z{};   // AB, z pencils (3D)
+  CUtensorMap map_acc{};    // acc, last-pass pencils
+  const float* map_U_ptr = nullptr;
+  CUtensorMap map_U_last{};  // state, last-pass pencils
+  CUtensorMap map_U_y{};     // state, y pencils (3D filter pass)
   long step_counter = 0;
   std::vector<void*> allocations;
   // launch profiling: CUDA events around every pass launch
@@ -185,6 +195,52 @@ int dalloc(ps_plan p, Tp** ptr, size_t count) {
   return PS_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// libcuda link needed).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// 4-D map over a [nf][Nz][Ny][Nx] float32 buffer with the tile box of the
+// TMA strided passes for pencils along `axis` (1 = y, 2 = z) of length naxis.
+int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int axis) {
+  auto fn = encode_fn();
+  if (!fn) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const int naxis = p->n[axis];
+  const int T = (naxis >= 1024) ? 8 : 16;
+  const cuuint32_t rows = (cuuint32_t)(naxis < 256 ? naxis : 256);
+  const cuuint64_t dims[4] = {(cuuint64_t)p->n[0], (cuuint64_t)p->n[1], (cuuint64_t)p->n[2], (cuuint64_t)nf};
+  const cuuint64_t strides[3] = {(cuuint64_t)p->n[0] * 4, (cuuint64_t)p->n[0] * p->n[1] * 4,
+                                 (cuuint64_t)p->cells * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)T, axis == 1 ? rows : 1u, axis == 2 ? rows : 1u, 1u};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return PS_OK;
+}
+
+// maps of the caller's state pointer (re-encoded when the pointer changes)
+int state_maps(ps_plan p, const float* U) {
+  if (U == p->map_U_ptr) return PS_OK;
+  int rc;
+  const int last_axis = (p->nd == 3) ? 2 : 1;
+  if ((rc = make_map(&p->map_U_last, U, p, p->nc, last_axis)) != PS_OK) return rc;
+  if (p->nd == 3 && (rc = make_map(&p->map_U_y, U, p, p->nc, 1)) != PS_OK) return rc;
+  p->map_U_ptr = U;
+  return PS_OK;
+}
+
 ps::StridedGeom geom_y(const ps_plan_s* p) {
   // pencils along y: axis stride Nx, outer slabs z (stride Nx*Ny)
   return ps::StridedGeom{p->n[0], (long)p->n[0], (long)p->n[0] * p->n[1], p->n[2]};
@@ -197,21 +253,38 @@ ps::StridedGeom geom_z(const ps_plan_s* p) {
 // One-axis operator on nf fields (P or D), axis 0 = x.
 int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s,
              bool complement = false) {
-  ps::OpArgs a{};
-  a.in = in;
-  a.out = out;
-  a.nf = nf;
-  a.fs = p->cells;
-  a.rows = (int)(p->cells / p->n[0]);
-  a.g = (axis == 1) ? geom_y(p) : geom_z(p);
-  a.ax = p->ax(axis);
-  a.deriv = deriv;
-  a.scale = scale;
-  a.complement = complement ? 1 : 0;
   ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells);
-  cudaError_t e = ps::dispatch_n(p->n[axis], [&](auto nc) {
-    return ps::launch_op<decltype(nc)::value>(axis != 0, a, s);
-  });
+  cudaError_t e;
+  if (axis == 0) {
+    ps::OpArgs a{};
+    a.in = in;
+    a.out = out;
+    a.nf = nf;
+    a.fs = p->cells;
+    a.rows = (int)(p->cells / p->n[0]);
+    a.ax = p->ax(0);
+    a.deriv = deriv;
+    a.scale = scale;
+    a.complement = complement ? 1 : 0;
+    e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_op<decltype(nc)::value>(false, a, s); });
+  } else {
+    if (nf > 63) return fail(PS_ERR_INVALID, "at most 63 fields per operator call");
+    CUtensorMap m;
+    int rc = make_map(&m, in, p, nf, axis);
+    if (rc != PS_OK) return rc;
+    ps::OpTArgs a{};
+    a.out = out;
+    a.nf = nf;
+    a.fs = p->cells;
+    a.g = (axis == 1) ? geom_y(p) : geom_z(p);
+    a.axis = axis;
+    a.ax = p->ax(axis);
+    a.deriv = deriv;
+    a.scale = scale;
+    a.complement = complement ? 1 : 0;
+    a.status = p->status;
+    e = ps::dispatch_n(p->n[axis], [&](auto nc) { return ps::launch_op_t<decltype(nc)::value>(m, a, s); });
+  }
   if (e != cudaSuccess) return cuda_fail(e, "operator pass");
   return PS_OK;
 }
@@ -237,52 +310,62 @@ int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, b
 }
 
 int ymid(ps_plan p, cudaStream_t s) {
-  ps::YMidArgs a{};
-  a.in = p->G;
+  ps::YMidTArgs a{};
   a.out = p->AB;
   a.fs = p->cells;
   a.g = geom_y(p);
   a.ax = p->ax(1);
+  a.status = p->status;
   ProfScope prof(p, s, PS_KIND_Y, 4.0 * p->cells * 25);
-  cudaError_t e = ps::dispatch_n(p->n[1], [&](auto nc) { return ps::launch_ymid3<decltype(nc)::value>(a, s); });
+  cudaError_t e = ps::dispatch_n(p->n[1], [&](auto nc) {
+    return ps::launch_ymid3_t<decltype(nc)::value>(p->map_G_y, a, s);
+  });
   if (e != cudaSuccess) return cuda_fail(e, "y pass");
   return PS_OK;
 }
 
 int last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
          cudaStream_t s) {
-  ps::LastArgs a{};
+  int rc;
+  if ((rc = state_maps(p, Un)) != PS_OK) return rc;
+  ps::LastTArgs a{};
   const int nc = p->nc;
+  const CUtensorMap* mAB;
   if (p->nd == 3) {
-    a.a = p->AB;
-    a.b = p->AB + (long)5 * p->cells;
+    a.fa0 = 0;
+    a.fb0 = 5;
     a.g = geom_z(p);
+    a.axis = 2;
     a.ax = p->ax(2);
+    mAB = &p->map_AB_z;
   } else {
-    a.a = p->G;
-    a.b = p->G + (long)nc * p->cells;
+    a.fa0 = 0;
+    a.fb0 = nc;
     a.g = geom_y(p);
+    a.axis = 1;
     a.ax = p->ax(1);
+    mAB = &p->map_G_y;
   }
+  a.acc = p->acc;
+  a.out = out;
   a.fs = p->cells;
   a.stage = stage;
   a.Un = Un;
-  a.acc = p->acc;
-  a.out = out;
   a.dt_dev = d_dt;
   a.dt = dt;
   a.gamma = (float)p->desc.gamma;
   // the 2D kernel clamps (solver.py:467-513); the 3D solver has none (1220-1230)
-  a.rho_min = 1e-8f;               // _positivity_clamp_2d floors (solver.py:467)
+  a.rho_min = 1e-8f;  // _positivity_clamp_2d floors (solver.py:467)
   a.p_min = 1e-10f;
   a.eref = p->eref;
   a.filter_last = filter_last ? 1 : 0;
+  a.status = p->status;
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
   ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * nc * (2 + st_words));
   cudaError_t e = ps::dispatch_n(naxis, [&](auto nc2) {
-    return ps::launch_last<decltype(nc2)::value>(p->nd, a, s);
+    return ps::launch_last_t<decltype(nc2)::value>(p->nd, *mAB, p->map_U_last, p->map_acc, a, s);
   });
   if (e != cudaSuccess) return cuda_fail(e, "last pass");
   return PS_OK;
@@ -429,7 +512,14 @@ int ps_plan_create(const ps_plan_desc* d, ps_plan* out) {
   }
   if ((rc = dalloc(p, &p->speed, 1)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->eref, 1)) != PS_OK) return cleanup(rc);
-  PS_CU(cudaMemset(p->eref, 0, sizeof(float)), "eref init");
+  if ((rc = dalloc(p, &p->status, 1)) != PS_OK) return cleanup(rc);
+  if (cudaMemset(p->eref, 0, sizeof(float)) != cudaSuccess || cudaMemset(p->status, 0, sizeof(int)) != cudaSuccess)
+    return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
+  if (p->nd >= 2) {
+    if ((rc = make_map(&p->map_G_y, p->G, p, (p->nd == 3) ? 15 : 8, 1)) != PS_OK) return cleanup(rc);
+    if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
+    if ((rc = make_map(&p->map_acc, p->acc, p, p->nc, (p->nd == 3) ? 2 : 1)) != PS_OK) return cleanup(rc);
+  }
   *out = p;
   return PS_OK;
 }
@@ -447,6 +537,14 @@ int ps_plan_destroy(ps_plan p) {
 }
 
 int ps_plan_ncomp(ps_plan p) { return p ? p->nc : -1; }
+
+int ps_plan_status(ps_plan p, int* status) {
+  if (!p || !status) return fail(PS_ERR_INVALID, "null argument");
+  int v = 0;
+  PS_CU(cudaMemcpy(&v, p->status, sizeof(int), cudaMemcpyDeviceToHost), "status read");
+  *status = v;
+  return PS_OK;
+}
 
 int ps_profile_enable(ps_plan p, int enable) {
   if (!p) return fail(PS_ERR_INVALID, "null plan");

@@ -4,8 +4,10 @@
 // One elected thread issues cp.async.bulk.tensor loads of [rows x 16]-float
 // boxes into a shared-memory ring; every consumer waits on the slot's
 // mbarrier with a bounded number of polls.  A wait that runs out records
-// PS_STATUS_TMA_TIMEOUT in the plan's device status word and the kernel
-// returns early instead of spinning (there is no unbounded wait anywhere).
+// the timeout bit in the plan's device status word; the kernel then stops
+// waiting and issuing, drains its copies in flight (again bounded) and runs
+// to its end with results the status word marks invalid.  There is no
+// unbounded wait anywhere.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -13,7 +15,7 @@
 
 namespace ps {
 
-constexpr int PS_STATUS_TMA_TIMEOUT = 1;
+constexpr int kStatusTmaTimeout = 1;  // PS_STATUS_TMA_TIMEOUT in the C ABI
 // polls of mbarrier.try_wait (each poll already suspends for a
 // hardware-defined interval) before a wait is declared failed: seconds of GPU
 // time, orders of magnitude above a healthy tile latency (~microseconds)
@@ -55,7 +57,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
   for (uint32_t i = 0; i < kMaxPolls; ++i)
     if (mbar_try_wait(bar, parity)) return true;
-  if (status) atomicOr(status, PS_STATUS_TMA_TIMEOUT);
+  if (status) atomicOr(status, kStatusTmaTimeout);
   return false;
 }
 

@@ -152,6 +152,12 @@ class Plan:
         _lib.check(self._lib.ps_conserved(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
         return out
 
+    def status(self) -> int:
+        """Device status word (0 = healthy; 1 = a kernel's bounded TMA wait ran out)."""
+        v = C.c_int()
+        _lib.check(self._lib.ps_plan_status(self._handle, C.byref(v)))
+        return int(v.value)
+
     # -- launch profiling -------------------------------------------------
     def profile(self, enable: bool = True) -> None:
         """Bracket every pass launch with CUDA events (kind, algorithmic bytes)."""

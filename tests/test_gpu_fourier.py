@@ -187,6 +187,7 @@ def test_tgv_256_full_size_properties(cuda_device):
     for _ in range(4):
         plan.step_(V, 1e-3)
     assert torch.isfinite(U).all()
+    assert plan.status() == 0
     m1 = host(plan.conserved(U))
     assert abs(m1[0] - m0[0]) / m0[0] < 1e-6
     assert abs(m1[4] - m0[4]) / m0[4] < 1e-6
@@ -206,4 +207,5 @@ def test_tgv_200_steps_vs_oracle(cuda_device):
     U = dev(U0, cuda_device)
     plan.run_(U, 200, 1e-3)
     out = host(U)
+    assert plan.status() == 0
     assert max(field_errors(out, ref)) < STATE_TOL, field_errors(out, ref)
