@@ -85,120 +85,146 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   }
   __syncthreads();
 
-  if (a.Uw != nullptr) {  // fused end-of-step filter along x
-#pragma unroll 1
-    for (int c = 0; c < NC; c += 2) {
-      float2 v[B];
+  // flux component F^dir_c at this thread's points (branches outside the point loop)
+  auto flux_vals = [&](int dir, int c, float (&o)[B]) {
+    if (c == 0) {
 #pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(slot(c, n2), (c + 1 < NC) ? slot(c + 1, n2) : 0.0f);
-      pf.fwd(v);
-#pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];  // complementary symbol
-        v[r].x *= q;
-        v[r].y *= q;
-      }
-      pf.inv(v);
+      for (int n2 = 0; n2 < B; ++n2) o[n2] = slot(0, n2) * slot(1 + dir, n2);
+    } else if (c == NC - 1) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        const float f0 = slot(c, n2) - v[n2].x;
-        slot(c, n2) = f0;
-        if (valid) a.Uw[c * a.fs + rbase + A * n2] = f0;
-        if (c + 1 < NC) {
-          const float f1 = slot(c + 1, n2) - v[n2].y;
-          slot(c + 1, n2) = f1;
-          if (valid) a.Uw[(c + 1) * a.fs + rbase + A * n2] = f1;
-        }
+        const float rho = slot(0, n2), pr = slot(NC - 1, n2);
+        float kin = 0.0f;
+#pragma unroll
+        for (int d = 0; d < ND; ++d) kin = fmaf(slot(1 + d, n2), slot(1 + d, n2), kin);
+        const float Ep = pr / (a.gamma - 1.0f) + 0.5f * rho * kin;  // E' = E - E_ref
+        o[n2] = ((Ep + pr) + href) * slot(1 + dir, n2);             // (E + p) u_dir
+      }
+    } else {
+      const bool diag = (c - 1 == dir);
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const float rv = slot(0, n2) * slot(1 + dir, n2) * slot(c, n2);
+        o[n2] = diag ? rv + slot(NC - 1, n2) : rv;
       }
     }
-  }
-
-  // conservative -> primitive (rho, u_1..u_ND, p) in place; CFL speed
-  float smax = 0.0f;
-#pragma unroll
-  for (int n2 = 0; n2 < B; ++n2) {
-    const float rho = slot(0, n2);
-    const float rinv = 1.0f / rho;
-    float kin = 0.0f;
-    float vel[ND];
-#pragma unroll
-    for (int d = 0; d < ND; ++d) {
-      vel[d] = slot(1 + d, n2) * rinv;
-      kin = fmaf(vel[d], vel[d], kin);
-      slot(1 + d, n2) = vel[d];
-    }
-    const float pr = (a.gamma - 1.0f) * (slot(NC - 1, n2) - 0.5f * rho * kin);
-    slot(NC - 1, n2) = pr;
-    if (a.speed != nullptr && valid) {
-      const float cs = sqrtf(a.gamma * (pr + pref) / rho);
-      float um = fabsf(vel[0]);
-      if (ND == 3) um = fmaxf(um, fmaxf(fabsf(vel[1]), fabsf(vel[ND - 1])));
-      // 2D keeps |u_x| + a only (equations.py:137-147)
-      smax = fmaxf(smax, um + cs);
-    }
-  }
-  if (a.speed != nullptr) {
-    const float m = block_max(smax, S.red);
-    if (threadIdx.x == 0) atomic_max_nonneg(a.speed, m);
-  }
-
-  // flux component value at slot n2: direction dir (0=x), component c
-  auto flux = [&](int dir, int c, int n2) -> float {
-    const float rho = slot(0, n2);
-    const float ua = slot(1 + dir, n2);
-    const float pr = slot(NC - 1, n2);
-    if (c == 0) return rho * ua;
-    if (c == NC - 1) {
-      float kin = 0.0f;
-#pragma unroll
-      for (int d = 0; d < ND; ++d) kin = fmaf(slot(1 + d, n2), slot(1 + d, n2), kin);
-      const float Ep = pr / (a.gamma - 1.0f) + 0.5f * rho * kin;  // E' = E - E_ref
-      return ((Ep + pr) + href) * ua;                               // (E + p) u_a
-    }
-    const float ub = slot(c, n2);  // c in 1..ND -> velocity component c-1
-    return rho * ua * ub + ((c - 1 == dir) ? pr : 0.0f);
   };
 
-  // jobs: D_x on F^x pairs; P_x on (F^y_c, F^z_c) [3D] or F^y pairs [2D]
-  auto run_job = [&](int dirA, int cA, int dirB, int cB, bool deriv, int fA, int fB) {
+  // Jobs, one FFT body for all of them:
+  //   [0, nfx)        complementary filter P_x of state pairs (fused end-of-step filter)
+  //   then            D_x on F^x pairs, P_x on (F^y_c, F^z_c) [3D] or F^y pairs [2D]
+  constexpr int nD = (NC + 1) / 2;
+  constexpr int nP = (ND == 3) ? NC : NC / 2;
+  const int nfx = (a.Uw != nullptr) ? (NC + 1) / 2 : 0;
+  const int njobs = nfx + nD + nP;
+#pragma unroll 1
+  for (int j = 0; j < njobs; ++j) {
+    if (j == nfx) {
+      // conservative -> primitive (rho, u_1..u_ND, p') in place; CFL speed
+      float smax = 0.0f;
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const float rho = slot(0, n2);
+        const float rinv = 1.0f / rho;
+        float kin = 0.0f;
+        float vel[ND];
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          vel[d] = slot(1 + d, n2) * rinv;
+          kin = fmaf(vel[d], vel[d], kin);
+          slot(1 + d, n2) = vel[d];
+        }
+        const float pr = (a.gamma - 1.0f) * (slot(NC - 1, n2) - 0.5f * rho * kin);
+        slot(NC - 1, n2) = pr;
+        if (a.speed != nullptr && valid) {
+          const float cs = sqrtf(a.gamma * (pr + pref) / rho);
+          float um = fabsf(vel[0]);
+          if (ND == 3) um = fmaxf(um, fmaxf(fabsf(vel[1]), fabsf(vel[ND - 1])));
+          // 2D keeps |u_x| + a only (equations.py:137-147)
+          smax = fmaxf(smax, um + cs);
+        }
+      }
+      if (a.speed != nullptr) {
+        const float m = block_max(smax, S.red);
+        if (threadIdx.x == 0) atomic_max_nonneg(a.speed, m);
+      }
+    }
+    int mode, fA, fB;  // mode 0: complementary filter, 1: D, 2: P
     float2 v[B];
+    if (j < nfx) {
+      const int c = 2 * j;
+      mode = 0;
+      fA = c;
+      fB = (c + 1 < NC) ? c + 1 : -1;
 #pragma unroll
-    for (int n2 = 0; n2 < B; ++n2)
-      v[n2] = make_float2(flux(dirA, cA, n2), (cB >= 0) ? flux(dirB, cB, n2) : 0.0f);
-    pf.fwd(v);
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-      const int k = pf.kidx(r);
-      if (deriv) {
-        const float dd = S.ax.d[k];
-        v[r] = make_float2(-v[r].y * dd, v[r].x * dd);
+      for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(slot(fA, n2), fB >= 0 ? slot(fB, n2) : 0.0f);
+    } else {
+      const int jj = j - nfx;
+      int dirA, cA, dirB, cB;
+      if (jj < nD) {
+        mode = 1;
+        dirA = dirB = 0;
+        cA = 2 * jj;
+        cB = (cA + 1 < NC) ? cA + 1 : -1;
+        fA = cA;
+        fB = cB;
       } else {
-        const float s = S.ax.P[k];
+        const int k = jj - nD;
+        mode = 2;
+        if (ND == 3) {
+          dirA = 1, cA = k, dirB = 2, cB = k;
+          fA = NC + k;
+          fB = 2 * NC + k;
+        } else {
+          dirA = dirB = 1;
+          cA = 2 * k;
+          cB = 2 * k + 1;
+          fA = NC + cA;
+          fB = NC + cB;
+        }
+      }
+      float oa[B], ob[B];
+      flux_vals(dirA, cA, oa);
+      if (cB >= 0) flux_vals(dirB, cB, ob);
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(oa[n2], cB >= 0 ? ob[n2] : 0.0f);
+    }
+    pf.fwd(v);
+    if (mode == 1) {
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float dd = S.ax.d[pf.kidx(r)];
+        v[r] = make_float2(-v[r].y * dd, v[r].x * dd);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float P = S.ax.P[pf.kidx(r)];
+        const float s = (mode == 0) ? (1.0f / N) - P : P;
         v[r].x *= s;
         v[r].y *= s;
       }
     }
     pf.inv(v);
-    if (valid) {
+    if (mode == 0) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const float f0 = slot(fA, n2) - v[n2].x;
+        slot(fA, n2) = f0;
+        if (valid) a.Uw[fA * a.fs + rbase + A * n2] = f0;
+        if (fB >= 0) {
+          const float f1 = slot(fB, n2) - v[n2].y;
+          slot(fB, n2) = f1;
+          if (valid) a.Uw[fB * a.fs + rbase + A * n2] = f1;
+        }
+      }
+    } else if (valid) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
         a.out[fA * a.fs + rbase + A * n2] = v[n2].x;
         if (fB >= 0) a.out[fB * a.fs + rbase + A * n2] = v[n2].y;
       }
     }
-  };
-
-#pragma unroll 1
-  for (int c = 0; c < NC; c += 2) {
-    const bool two = c + 1 < NC;
-    run_job(0, c, 0, two ? c + 1 : -1, true, c, two ? c + 1 : -1);
-  }
-  if constexpr (ND == 3) {
-#pragma unroll 1
-    for (int c = 0; c < NC; ++c) run_job(1, c, 2, c, false, NC + c, 2 * NC + c);
-  } else {
-#pragma unroll 1
-    for (int c = 0; c < NC; c += 2) run_job(1, c, 1, c + 1, false, NC + c, NC + c + 1);
   }
 }
 
