@@ -17,10 +17,11 @@
 // followed in the last pass by the RK4 stage update (plus the positivity clamp
 // in 2D) and, after the final stage, the last axis of the end-of-step filter.
 //
-// Two real pencils are packed into one complex transform.  When the two
-// packed signals need different operators (a with symbol P, b with symbol
-// i d) and only their sum is wanted, the sum's spectrum is recovered from the
-// packed spectrum Z as  C(k) = ((P+d) Z(k) + (P-d) conj Z(-k)) / 2.
+// Two real pencils are packed into one complex transform: P and i d are
+// real-to-real operators, so they act on the real and imaginary halves of a
+// packed pencil independently.  The strided passes (passes_tma.cuh) evaluate
+// P a_c + D b_c for two components at once as
+// IFFT(P FFT(a_c + i a_c') + i d FFT(b_c + i b_c')).
 #pragma once
 #include "pass_common.cuh"
 
@@ -257,300 +258,6 @@ __device__ __forceinline__ void load_pair(float2 (&v)[Shape<N>::B], const float*
       if (fb) y = fb[base + n2 * step];
     }
     v[n2] = make_float2(x, y);
-  }
-}
-
-// C(k) = ((P+d) Z(k) + (P-d) conj Z(-k)) / 2 : spectrum of P a + D b for z = a + i b
-template <int N, int T>
-__device__ __forceinline__ void combine_pd(float2 (&v)[Shape<N>::B], const Pencil<N, T, true>& pf,
-                                           const AxisSmem<N>& ax, float sign) {
-  constexpr int B = Shape<N>::B;
-  float2 vn[B];
-  pf.negk(v, vn);
-#pragma unroll
-  for (int r = 0; r < B; ++r) {
-    const int k = pf.kidx(r);
-    const float P = ax.P[k], d = ax.d[k];
-    const float al = 0.5f * sign * (P + d), be = 0.5f * sign * (P - d);
-    v[r] = make_float2(al * v[r].x + be * vn[r].x, al * v[r].y - be * vn[r].y);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 3D Y pass: A_c = P_y G_c + D_y Hy_c, B_c = P_y Hz_c.
-// in: 15 fields [G(5), Hy(5), Hz(5)];  out: 10 fields [A(5), B(5)]
-// ---------------------------------------------------------------------------
-struct YMidArgs {
-  const float* in;
-  float* out;
-  long fs;
-  StridedGeom g;
-  AxisOps ax;
-};
-
-template <int N, int T>
-__global__ void __launch_bounds__(Shape<N>::A * T, (Shape<N>::A * T <= 256) ? 2 : 1) k_ymid3(YMidArgs a) {
-  constexpr int A = Shape<N>::A, B = Shape<N>::B;
-  using PF = Pencil<N, T, true>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& S = *reinterpret_cast<StridedSmem<N, T>*>(smem_raw);
-  const int p = threadIdx.x % T;
-  const int t = threadIdx.x / T;
-  const int col = blockIdx.x * T + p;
-  const int outer = blockIdx.y;
-  const bool valid = col < a.g.ncol;
-  PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
-  load_axis<N>(S.ax, a.ax);
-  __syncthreads();
-  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
-  const long step = (long)A * a.g.as;
-
-  auto store = [&](float* f, int n2, float v) {
-    if (valid) f[base + n2 * step] = v;
-  };
-  // A outputs: pairs of combined spectra
-#pragma unroll 1
-  for (int c = 0; c < 5; c += 2) {
-    float2 w[B];
-    load_pair<N>(w, a.in + c * a.fs, a.in + (5 + c) * a.fs, base, step, valid);
-    pf.fwd(w);
-    combine_pd<N, T>(w, pf, S.ax, 1.0f);
-    if (c + 1 < 5) {
-      float2 w2[B];
-      load_pair<N>(w2, a.in + (c + 1) * a.fs, a.in + (6 + c) * a.fs, base, step, valid);
-      pf.fwd(w2);
-      combine_pd<N, T>(w2, pf, S.ax, 1.0f);
-#pragma unroll
-      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
-    }
-    pf.inv(w);
-#pragma unroll
-    for (int n2 = 0; n2 < B; ++n2) {
-      store(a.out + c * a.fs, n2, w[n2].x);
-      if (c + 1 < 5) store(a.out + (c + 1) * a.fs, n2, w[n2].y);
-    }
-  }
-  // B outputs: P_y on Hz pairs
-#pragma unroll 1
-  for (int c = 0; c < 5; c += 2) {
-    float2 w[B];
-    load_pair<N>(w, a.in + (10 + c) * a.fs, (c + 1 < 5) ? a.in + (11 + c) * a.fs : nullptr, base, step, valid);
-    pf.fwd(w);
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-      const float s = S.ax.P[pf.kidx(r)];
-      w[r].x *= s;
-      w[r].y *= s;
-    }
-    pf.inv(w);
-#pragma unroll
-    for (int n2 = 0; n2 < B; ++n2) {
-      store(a.out + (5 + c) * a.fs, n2, w[n2].x);
-      if (c + 1 < 5) store(a.out + (6 + c) * a.fs, n2, w[n2].y);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Last pass: rhs_c = -(P a_c + D b_c) along the pass axis, then
-//   mode RHS   : write rhs
-//   mode STAGE : RK4 stage update (clamp if enabled); after stage 3 the filter
-//                P along this axis is applied to the new state when requested.
-// ---------------------------------------------------------------------------
-struct LastArgs {
-  const float* a;      // a_c fields base (NC fields)
-  const float* b;      // b_c fields base (NC fields)
-  long fs;
-  StridedGeom g;
-  AxisOps ax;
-  int stage;           // -1: rhs only; 0..3 RK4 stage
-  const float* Un;     // state at the start of the step
-  float* acc;          // RK accumulator
-  float* out;          // rhs (stage -1), next stage input (0..2), new state (3)
-  const double* dt_dev;
-  double dt;
-  float gamma;
-  float rho_min, p_min;
-  const float* eref;   // E_ref of the energy-perturbation form (clamp floor shift)
-  int filter_last;     // stage 3: apply P along this axis to the new state
-};
-
-template <int N, int T, int ND, bool CLAMP>
-__global__ void __launch_bounds__(Shape<N>::A * T, (Shape<N>::A * T <= 256) ? 2 : 1) k_last(LastArgs a) {
-  constexpr int NC = ND + 2;
-  constexpr int A = Shape<N>::A, B = Shape<N>::B;
-  using PF = Pencil<N, T, true>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& S = *reinterpret_cast<StridedSmem<N, T>*>(smem_raw);
-  const int p = threadIdx.x % T;
-  const int t = threadIdx.x / T;
-  const int col = blockIdx.x * T + p;
-  const int outer = blockIdx.y;
-  const bool valid = col < a.g.ncol;
-  PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
-  load_axis<N>(S.ax, a.ax);
-  __syncthreads();
-  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
-  const long step = (long)A * a.g.as;
-  const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
-  const RKCoef rc = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
-
-  // rhs for components (c, c+1) packed in one inverse transform
-  auto rhs_pair = [&](int c, float2 (&w)[B]) {
-    load_pair<N>(w, a.a + c * a.fs, a.b + c * a.fs, base, step, valid);
-    pf.fwd(w);
-    combine_pd<N, T>(w, pf, S.ax, -1.0f);
-    if (c + 1 < NC) {
-      float2 w2[B];
-      load_pair<N>(w2, a.a + (c + 1) * a.fs, a.b + (c + 1) * a.fs, base, step, valid);
-      pf.fwd(w2);
-      combine_pd<N, T>(w2, pf, S.ax, -1.0f);
-#pragma unroll
-      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
-    }
-    pf.inv(w);
-  };
-  auto filter_pair = [&](float2 (&w)[B]) {  // complementary form, see AxisOps
-    float2 w0[B];
-#pragma unroll
-    for (int r = 0; r < B; ++r) w0[r] = w[r];
-    pf.fwd(w);
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-      const float q = (1.0f / N) - S.ax.P[pf.kidx(r)];
-      w[r].x *= q;
-      w[r].y *= q;
-    }
-    pf.inv(w);
-#pragma unroll
-    for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
-  };
-  auto addr = [&](int c, int n2) { return c * a.fs + base + n2 * step; };
-  const float pmin_shift = a.p_min - (a.gamma - 1.0f) * (*a.eref);
-
-  if (!CLAMP || a.stage < 0) {
-    // components are independent: process pair by pair
-#pragma unroll 1
-    for (int c = 0; c < NC; c += 2) {
-      float2 w[B];
-      rhs_pair(c, w);
-      const bool two = c + 1 < NC;
-      if (a.stage < 0) {
-        if (valid) {
-#pragma unroll
-          for (int n2 = 0; n2 < B; ++n2) {
-            a.out[addr(c, n2)] = w[n2].x;
-            if (two) a.out[addr(c + 1, n2)] = w[n2].y;
-          }
-        }
-        continue;
-      }
-      // batch the epilogue loads (U^n, accumulator) before any store so the
-      // DRAM latencies overlap instead of serialising behind the acc writes
-      float un[2][B], ac[2][B];
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-#pragma unroll
-        for (int n2 = 0; n2 < B; ++n2) {
-          const bool live = valid && (q == 0 || two);
-          un[q][n2] = (live && a.stage != 3) ? __ldg(a.Un + addr(c + q, n2)) : 0.0f;
-          ac[q][n2] = (live && a.stage != 0) ? a.acc[addr(c + q, n2)] : 0.0f;
-        }
-      }
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) {
-        const float k[2] = {w[n2].x, w[n2].y};
-        float res[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          if (a.stage == 3) {
-            res[q] = fmaf(rc.wacc, k[q], ac[q][n2]);
-          } else {
-            const float base_acc = (a.stage == 0) ? un[q][n2] : ac[q][n2];
-            ac[q][n2] = fmaf(rc.wacc, k[q], base_acc);
-            res[q] = fmaf(rc.wnext, k[q], un[q][n2]);
-          }
-        }
-        w[n2] = make_float2(res[0], res[1]);
-      }
-      if (valid && a.stage != 3) {
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          if (q == 1 && !two) break;
-#pragma unroll
-          for (int n2 = 0; n2 < B; ++n2) a.acc[addr(c + q, n2)] = ac[q][n2];
-        }
-      }
-      if (a.stage == 3 && a.filter_last) filter_pair(w);
-      if (valid) {
-#pragma unroll
-        for (int n2 = 0; n2 < B; ++n2) {
-          a.out[addr(c, n2)] = w[n2].x;
-          if (two) a.out[addr(c + 1, n2)] = w[n2].y;
-        }
-      }
-    }
-    return;
-  }
-
-  if constexpr (CLAMP) {
-  // clamped update: all components of a cell are needed together
-  float2 kk[(NC + 1) / 2][B];
-#pragma unroll
-  for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
-  constexpr int CH = 4;  // positions per batch of epilogue loads
-#pragma unroll
-  for (int n0 = 0; n0 < B; n0 += CH) {
-    float un[CH][NC], ac[CH][NC];
-#pragma unroll
-    for (int j = 0; j < CH; ++j)
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        un[j][c] = (valid && a.stage != 3) ? __ldg(a.Un + addr(c, n0 + j)) : 0.0f;
-        ac[j][c] = (valid && a.stage != 0) ? a.acc[addr(c, n0 + j)] : 0.0f;
-      }
-#pragma unroll
-    for (int j = 0; j < CH; ++j) {
-      const int n2 = n0 + j;
-      float u[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const float k = (c & 1) ? kk[c / 2][n2].y : kk[c / 2][n2].x;
-        float res;
-        if (a.stage == 3) {
-          res = fmaf(rc.wacc, k, ac[j][c]);
-        } else {
-          const float base_acc = (a.stage == 0) ? un[j][c] : ac[j][c];
-          ac[j][c] = fmaf(rc.wacc, k, base_acc);
-          res = fmaf(rc.wnext, k, un[j][c]);
-        }
-        u[c] = valid ? res : ((c == 0) ? 1.0f : 0.0f);
-      }
-      clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        if (c & 1) kk[c / 2][n2].y = u[c];
-        else kk[c / 2][n2].x = u[c];
-      }
-    }
-    if (valid && a.stage != 3) {
-#pragma unroll
-      for (int j = 0; j < CH; ++j)
-#pragma unroll
-        for (int c = 0; c < NC; ++c) a.acc[addr(c, n0 + j)] = ac[j][c];
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < NC; c += 2) {
-    if (a.stage == 3 && a.filter_last) filter_pair(kk[c / 2]);
-    if (valid) {
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) {
-        a.out[addr(c, n2)] = kk[c / 2][n2].x;
-        if (c + 1 < NC) a.out[addr(c + 1, n2)] = kk[c / 2][n2].y;
-      }
-    }
-  }
   }
 }
 

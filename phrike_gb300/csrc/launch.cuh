@@ -10,8 +10,6 @@
 namespace ps {
 
 template <int N> cudaError_t launch_xfirst(int nd, const XFirstArgs& a, cudaStream_t s);
-template <int N> cudaError_t launch_ymid3(const YMidArgs& a, cudaStream_t s);
-template <int N> cudaError_t launch_last(int nd, const LastArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
 
@@ -75,46 +73,14 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \
-  cudaError_t launch_ymid3<NN>(const YMidArgs& a, cudaStream_t s) {                                   \
-    constexpr int T = Tile<NN>::TS;                                                                   \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
-    const size_t sm = sizeof(StridedSmem<NN, T>);                                                     \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_ymid3<NN, T>, sm)) != cudaSuccess) return e;                                  \
-    k_ymid3<NN, T><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                             \
-    return cudaGetLastError();                                                                        \
-  }                                                                                                   \
-  template <>                                                                                         \
-  cudaError_t launch_last<NN>(int nd, const LastArgs& a, cudaStream_t s) {                            \
-    constexpr int T = Tile<NN>::TS;                                                                   \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
-    const size_t sm = sizeof(StridedSmem<NN, T>);                                                     \
-    cudaError_t e;                                                                                    \
-    if (nd == 3) {                                                                                    \
-      if ((e = set_smem(k_last<NN, T, 3, false>, sm)) != cudaSuccess) return e;                       \
-      k_last<NN, T, 3, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                  \
-    } else {                                                                                          \
-      if ((e = set_smem(k_last<NN, T, 2, true>, sm)) != cudaSuccess) return e;                        \
-      k_last<NN, T, 2, true><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                   \
-    }                                                                                                 \
-    return cudaGetLastError();                                                                        \
-  }                                                                                                   \
-  template <>                                                                                         \
   cudaError_t launch_op<NN>(bool strided, const OpArgs& a, cudaStream_t s) {                          \
+    if (strided) return cudaErrorInvalidValue; /* strided axes use launch_op_t */                     \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const dim3 grid((a.rows + T - 1) / T);                                                            \
+    const size_t sm = sizeof(StridedSmem<NN, T, false>);                                              \
     cudaError_t e;                                                                                    \
-    if (strided) {                                                                                    \
-      constexpr int T = Tile<NN>::TS;                                                                 \
-      const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                            \
-      const size_t sm = sizeof(StridedSmem<NN, T, true>);                                             \
-      if ((e = set_smem(k_op<NN, T, true>, sm)) != cudaSuccess) return e;                             \
-      k_op<NN, T, true><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                        \
-    } else {                                                                                          \
-      constexpr int T = Tile<NN>::TC;                                                                 \
-      const dim3 grid((a.rows + T - 1) / T);                                                          \
-      const size_t sm = sizeof(StridedSmem<NN, T, false>);                                            \
-      if ((e = set_smem(k_op<NN, T, false>, sm)) != cudaSuccess) return e;                            \
-      k_op<NN, T, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                       \
-    }                                                                                                 \
+    if ((e = set_smem(k_op<NN, T, false>, sm)) != cudaSuccess) return e;                              \
+    k_op<NN, T, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                         \
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \

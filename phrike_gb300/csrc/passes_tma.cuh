@@ -1,6 +1,6 @@
 // TMA-fed strided pencil passes (pencils along y or z).
 //
-// Same arithmetic as k_ymid3 / k_last / k_op in euler_passes.cuh, but every
+// Pencils along a strided axis need whole columns of the field.  Every
 // input field tile ([N rows] x [T adjacent x columns], one 4-D tensor-map box
 // per 256 rows) is streamed by the tensor memory accelerator into a ring of R
 // shared-memory slots.  One elected thread issues the loads R tiles ahead of
@@ -126,6 +126,22 @@ __device__ __forceinline__ void tile_pair(float2 (&v)[Shape<N>::B], const float*
   }
 }
 
+// w <- sign * (P[k] z1 + i d[k] z2) for two packed spectra in spectral layout.
+// P and i*d are real-to-real operators, so they act on the real and imaginary
+// halves of a packed pencil independently: with z1 = FFT(a_c + i a_c') and
+// z2 = FFT(b_c + i b_c') the inverse transform of w holds
+// P a_c + D b_c in its real part and P a_c' + D b_c' in its imaginary part.
+template <int N, int T>
+__device__ __forceinline__ void apply_pd(float2 (&w)[Shape<N>::B], const float2 (&z2)[Shape<N>::B],
+                                         const Pencil<N, T, true>& pf, const AxisSmem<N>& ax, float sign) {
+#pragma unroll
+  for (int r = 0; r < Shape<N>::B; ++r) {
+    const int k = pf.kidx(r);
+    const float P = sign * ax.P[k], d = sign * ax.d[k];
+    w[r] = make_float2(fmaf(P, w[r].x, -d * z2[r].y), fmaf(P, w[r].y, d * z2[r].x));
+  }
+}
+
 template <int N, int T, int R>
 struct TmaStridedSmem {
   AxisSmem<N> ax;
@@ -157,8 +173,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   ring_init(S.ring);
   if (threadIdx.x == 0) {
-    // A pairs: (G_c, Hy_c) for c = 0..4 consumed two components at a time, then Hz pairs
-    const int order[15] = {0, 5, 1, 6, 2, 7, 3, 8, 4, 9, 10, 11, 12, 13, 14};
+    // A pairs (c, c+1): G_c, G_c+1, Hy_c, Hy_c+1 (last pair single), then Hz pairs
+    const int order[15] = {0, 1, 5, 6, 2, 3, 7, 8, 4, 9, 10, 11, 12, 13, 14};
     for (int i = 0; i < 15; ++i) S.ring.sched[i] = order[i];
     S.ring.ntiles = 15;
   }
@@ -174,22 +190,15 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 #pragma unroll 1
   for (int c = 0; c < 5; c += 2) {
     const bool two = c + 1 < 5;
-    float2 w[B];
-    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
-    rc.release(ti + 1);
-    ti += 2;
+    float2 w[B], z2[B];
+    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);  // G_c + i G_c+1
+    const int tb = ti + (two ? 2 : 1);
+    tile_pair<N, T>(z2, rc.wait(tb), two ? rc.wait(tb + 1) : nullptr, t, p);  // Hy_c + i Hy_c+1
+    ti = tb + (two ? 2 : 1);
+    rc.release(ti - 1);
     pf.fwd(w);
-    combine_pd<N, T>(w, pf, S.ax, 1.0f);
-    if (two) {
-      float2 w2[B];
-      tile_pair<N, T>(w2, rc.wait(ti), rc.wait(ti + 1), t, p);
-      rc.release(ti + 1);
-      ti += 2;
-      pf.fwd(w2);
-      combine_pd<N, T>(w2, pf, S.ax, 1.0f);
-#pragma unroll
-      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
-    }
+    pf.fwd(z2);
+    apply_pd<N, T>(w, z2, pf, S.ax, 1.0f);
     pf.inv(w);
     if (valid) {
 #pragma unroll
@@ -269,10 +278,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
     int n = 0;
     for (int c = 0; c < NC; c += 2) {
       const int m = (c + 1 < NC) ? 2 : 1;
-      for (int q = 0; q < m; ++q) {
-        S.ring.sched[n++] = a.fa0 + c + q;
-        S.ring.sched[n++] = a.fb0 + c + q;
-      }
+      for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fa0 + c + q;
+      for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fb0 + c + q;
       if (need_un)
         for (int q = 0; q < m; ++q) S.ring.sched[n++] = 64 + c + q;
       if (need_acc)
@@ -307,24 +314,18 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
     for (int r = 0; r < B; ++r) w[r] = make_float2(w0[r].x - w[r].x, w0[r].y - w[r].y);
   };
   int ti = 0;
-  // spectra of -(P a_c + D b_c) for components (c, c+1), inverse-transformed
+  // -(P a_c + D b_c) for components (c, c+1), real and imaginary part
   auto rhs_pair = [&](int c, float2 (&w)[B]) {
     const bool two = c + 1 < NC;
-    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
-    rc.release(ti + 1);
-    ti += 2;
+    const int m = two ? 2 : 1;
+    float2 z2[B];
+    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);
+    tile_pair<N, T>(z2, rc.wait(ti + m), two ? rc.wait(ti + m + 1) : nullptr, t, p);
+    ti += 2 * m;
+    rc.release(ti - 1);
     pf.fwd(w);
-    combine_pd<N, T>(w, pf, S.ax, -1.0f);
-    if (two) {
-      float2 w2[B];
-      tile_pair<N, T>(w2, rc.wait(ti), rc.wait(ti + 1), t, p);
-      rc.release(ti + 1);
-      ti += 2;
-      pf.fwd(w2);
-      combine_pd<N, T>(w2, pf, S.ax, -1.0f);
-#pragma unroll
-      for (int r = 0; r < B; ++r) w[r] = make_float2(w[r].x - w2[r].y, w[r].y + w2[r].x);
-    }
+    pf.fwd(z2);
+    apply_pd<N, T>(w, z2, pf, S.ax, -1.0f);
     pf.inv(w);
   };
 

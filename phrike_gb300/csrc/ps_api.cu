@@ -210,17 +210,21 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 4-D map over a [nf][Nz][Ny][Nx] float32 buffer with the tile box of the
-// TMA strided passes for pencils along `axis` (1 = y, 2 = z) of length naxis.
-int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int axis) {
+}  // namespace
+
+namespace ps {
+// 4-D map over a [nf][Nz][Ny][Nx] float32 buffer (n = {Nx, Ny, Nz}) with the
+// tile box of the TMA strided passes for pencils along `axis` (1 = y, 2 = z).
+// Host-only: fills the 128-byte map, allocates nothing.
+int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis) {
   auto fn = encode_fn();
   if (!fn) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  const int naxis = p->n[axis];
+  const int naxis = n[axis];
   const int T = (naxis >= 1024) ? 8 : 16;
   const cuuint32_t rows = (cuuint32_t)(naxis < 256 ? naxis : 256);
-  const cuuint64_t dims[4] = {(cuuint64_t)p->n[0], (cuuint64_t)p->n[1], (cuuint64_t)p->n[2], (cuuint64_t)nf};
-  const cuuint64_t strides[3] = {(cuuint64_t)p->n[0] * 4, (cuuint64_t)p->n[0] * p->n[1] * 4,
-                                 (cuuint64_t)p->cells * 4};
+  const cuuint64_t cells = (cuuint64_t)n[0] * n[1] * n[2];
+  const cuuint64_t dims[4] = {(cuuint64_t)n[0], (cuuint64_t)n[1], (cuuint64_t)n[2], (cuuint64_t)nf};
+  const cuuint64_t strides[3] = {(cuuint64_t)n[0] * 4, (cuuint64_t)n[0] * n[1] * 4, cells * 4};
   const cuuint32_t box[4] = {(cuuint32_t)T, axis == 1 ? rows : 1u, axis == 2 ? rows : 1u, 1u};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
@@ -228,6 +232,13 @@ int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int 
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return PS_OK;
+}
+}  // namespace ps
+
+namespace {
+
+int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int axis) {
+  return ps::encode_field_map(m, base, p->n, nf, axis);
 }
 
 // maps of the caller's state pointer (re-encoded when the pointer changes)

@@ -37,6 +37,7 @@
 
 namespace ps {
 int record_error(int code, const char* msg);
+int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis);
 }
 
 namespace {
@@ -164,34 +165,43 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   e = ps::dispatch_n(nx, [&](auto n) { return ps::launch_xfirst<decltype(n)::value>(nd, xa, s); });
   if (e != cudaSuccess) return fail_cuda(e, "x pass");
 
+  // tensor maps of the scratch intermediates and of U (host structs, no allocation)
+  const int n3[3] = {nx, ny, nz};
+  CUtensorMap mG, mAB, mU;
+  int rc;
+  if ((rc = ps::encode_field_map(&mG, G, n3, (nd == 3) ? 15 : 8, 1)) != PS_OK) return rc;
+  if (nd == 3 && (rc = ps::encode_field_map(&mAB, AB, n3, 10, 2)) != PS_OK) return rc;
+  if ((rc = ps::encode_field_map(&mU, U, n3, nc, (nd == 3) ? 2 : 1)) != PS_OK) return rc;
   const ps::StridedGeom gy{nx, (long)nx, (long)nx * ny, nz};
   if (nd == 3) {
-    ps::YMidArgs ya{};
-    ya.in = G;
+    ps::YMidTArgs ya{};
     ya.out = AB;
     ya.fs = cells;
     ya.g = gy;
     ya.ax = ax[1];
-    e = ps::dispatch_n(ny, [&](auto n) { return ps::launch_ymid3<decltype(n)::value>(ya, s); });
+    ya.status = nullptr;
+    e = ps::dispatch_n(ny, [&](auto n) { return ps::launch_ymid3_t<decltype(n)::value>(mG, ya, s); });
     if (e != cudaSuccess) return fail_cuda(e, "y pass");
   }
-  ps::LastArgs la{};
+  ps::LastTArgs la{};
   if (nd == 3) {
-    la.a = AB;
-    la.b = AB + 5 * cells;
+    la.fa0 = 0;
+    la.fb0 = 5;
     la.g = ps::StridedGeom{nx, (long)nx * ny, (long)nx, ny};
+    la.axis = 2;
     la.ax = ax[2];
   } else {
-    la.a = G;
-    la.b = G + (long)nc * cells;
+    la.fa0 = 0;
+    la.fb0 = nc;
     la.g = gy;
+    la.axis = 1;
     la.ax = ax[1];
   }
+  la.acc = nullptr;
+  la.out = rhs;
   la.fs = cells;
   la.stage = -1;
   la.Un = U;
-  la.acc = nullptr;
-  la.out = rhs;
   la.dt_dev = nullptr;
   la.dt = 0.0;
   la.gamma = (float)desc->gamma;
@@ -199,8 +209,12 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   la.p_min = 1e-10f;
   la.eref = eref;
   la.filter_last = 0;
+  la.status = nullptr;
   const int nlast = (nd == 3) ? nz : ny;
-  e = ps::dispatch_n(nlast, [&](auto n) { return ps::launch_last<decltype(n)::value>(nd, la, s); });
+  // rhs mode reads no U^n or accumulator tiles; U's map fills those slots
+  e = ps::dispatch_n(nlast, [&](auto n) {
+    return ps::launch_last_t<decltype(n)::value>(nd, (nd == 3) ? mAB : mG, mU, mU, la, s);
+  });
   if (e != cudaSuccess) return fail_cuda(e, "last pass");
   return PS_OK;
 }
