@@ -48,10 +48,12 @@ template <int N, int T, int ND>
 struct XFirstSmem {
   AxisSmem<N> ax;
   float2 buf[Pencil<N, T, false>::BUF];
-  float tile[(ND + 2) * N * T];
   float red[32];
 };
 
+// The thread's B points of all NC components stay in registers (q[c][n2]);
+// a switch over the job index gives every job compile-time register indices
+// while a single FFT body serves all jobs (keeps the kernel's code small).
 template <int N, int T, int ND>
 __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   constexpr int NC = ND + 2;
@@ -67,13 +69,13 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   load_axis<N>(S.ax, a.ax);
 
-  // per-thread private slots of the tile: ((c*B + n2)*T + p)*A + t
-  auto slot = [&](int c, int n2) -> float& { return S.tile[((c * B + n2) * T + p) * A + t]; };
   const long rbase = (long)row * N + t;
   const float er = *a.eref;
   const float eshift = a.shift_in ? er : 0.0f;
   const float pref = (a.gamma - 1.0f) * er;
   const float href = a.gamma * er;
+  const float g1 = a.gamma - 1.0f;
+  float q[NC][B];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
 #pragma unroll
@@ -81,62 +83,56 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
       float v = (c == 0) ? 1.0f : 0.0f;
       if (valid) v = a.U[c * a.fs + rbase + A * n2];  // may alias a.Uw: plain load
       if (c == NC - 1 && valid) v -= eshift;
-      slot(c, n2) = v;
+      q[c][n2] = v;
     }
   }
   __syncthreads();
 
-  // flux component F^dir_c at this thread's points (branches outside the point loop)
-  auto flux_vals = [&](int dir, int c, float (&o)[B]) {
-    if (c == 0) {
+  // F^dir_c at point n2 from primitives q = (rho, u_1..u_ND, p')
+  auto fx = [&](int dir, int c, int n2) -> float {
+    const float rho = q[0][n2], ua = q[1 + dir][n2], pr = q[NC - 1][n2];
+    if (c == 0) return rho * ua;
+    if (c == NC - 1) {
+      float kin = 0.0f;
 #pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) o[n2] = slot(0, n2) * slot(1 + dir, n2);
-    } else if (c == NC - 1) {
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) {
-        const float rho = slot(0, n2), pr = slot(NC - 1, n2);
-        float kin = 0.0f;
-#pragma unroll
-        for (int d = 0; d < ND; ++d) kin = fmaf(slot(1 + d, n2), slot(1 + d, n2), kin);
-        const float Ep = pr / (a.gamma - 1.0f) + 0.5f * rho * kin;  // E' = E - E_ref
-        o[n2] = ((Ep + pr) + href) * slot(1 + dir, n2);             // (E + p) u_dir
-      }
-    } else {
-      const bool diag = (c - 1 == dir);
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) {
-        const float rv = slot(0, n2) * slot(1 + dir, n2) * slot(c, n2);
-        o[n2] = diag ? rv + slot(NC - 1, n2) : rv;
-      }
+      for (int d = 0; d < ND; ++d) kin = fmaf(q[1 + d][n2], q[1 + d][n2], kin);
+      const float Ep = pr / g1 + 0.5f * rho * kin;  // E' = E - E_ref
+      return ((Ep + pr) + href) * ua;              // (E + p) u_dir
     }
+    const float rv = rho * ua * q[c][n2];
+    return (c - 1 == dir) ? rv + pr : rv;
+  };
+  auto fill = [&](float2 (&v)[B], int dA, int cA, int dB, int cB) {
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(fx(dA, cA, n2), cB >= 0 ? fx(dB, cB, n2) : 0.0f);
   };
 
-  // Jobs, one FFT body for all of them:
-  //   [0, nfx)        complementary filter P_x of state pairs (fused end-of-step filter)
-  //   then            D_x on F^x pairs, P_x on (F^y_c, F^z_c) [3D] or F^y pairs [2D]
+  // jobs: [0, nfx) complementary filter P_x of state pairs (fused end-of-step
+  // filter), then D_x on F^x pairs, then P_x on (F^y_c, F^z_c) [3D] or F^y pairs [2D]
+  constexpr int nFX = (NC + 1) / 2;
   constexpr int nD = (NC + 1) / 2;
   constexpr int nP = (ND == 3) ? NC : NC / 2;
-  const int nfx = (a.Uw != nullptr) ? (NC + 1) / 2 : 0;
+  const int nfx = (a.Uw != nullptr) ? nFX : 0;
   const int njobs = nfx + nD + nP;
 #pragma unroll 1
   for (int j = 0; j < njobs; ++j) {
     if (j == nfx) {
-      // conservative -> primitive (rho, u_1..u_ND, p') in place; CFL speed
+      // conservative -> primitive (rho, u_1..u_ND, p') in registers; CFL speed
       float smax = 0.0f;
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        const float rho = slot(0, n2);
+        const float rho = q[0][n2];
         const float rinv = 1.0f / rho;
         float kin = 0.0f;
         float vel[ND];
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
-          vel[d] = slot(1 + d, n2) * rinv;
+          vel[d] = q[1 + d][n2] * rinv;
           kin = fmaf(vel[d], vel[d], kin);
-          slot(1 + d, n2) = vel[d];
+          q[1 + d][n2] = vel[d];
         }
-        const float pr = (a.gamma - 1.0f) * (slot(NC - 1, n2) - 0.5f * rho * kin);
-        slot(NC - 1, n2) = pr;
+        const float pr = g1 * (q[NC - 1][n2] - 0.5f * rho * kin);
+        q[NC - 1][n2] = pr;
         if (a.speed != nullptr && valid) {
           const float cs = sqrtf(a.gamma * (pr + pref) / rho);
           float um = fabsf(vel[0]);
@@ -150,45 +146,66 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
         if (threadIdx.x == 0) atomic_max_nonneg(a.speed, m);
       }
     }
+    // job -> (mode, output fields); the switch fills v with constant register indices
+    // job kind: 0.. filter pairs, 10.. D_x pairs, 20.. P_x jobs
+    const int k = (j < nfx) ? j : (j - nfx < nD) ? 10 + (j - nfx) : 20 + (j - nfx - nD);
     int mode, fA, fB;  // mode 0: complementary filter, 1: D, 2: P
     float2 v[B];
-    if (j < nfx) {
-      const int c = 2 * j;
-      mode = 0;
-      fA = c;
-      fB = (c + 1 < NC) ? c + 1 : -1;
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(slot(fA, n2), fB >= 0 ? slot(fB, n2) : 0.0f);
-    } else {
-      const int jj = j - nfx;
-      int dirA, cA, dirB, cB;
-      if (jj < nD) {
-        mode = 1;
-        dirA = dirB = 0;
-        cA = 2 * jj;
-        cB = (cA + 1 < NC) ? cA + 1 : -1;
-        fA = cA;
-        fB = cB;
-      } else {
-        const int k = jj - nD;
+    switch (k) {
+#define PS_FX_CASE(K)                                                                                   \
+  case K: {                                                                                             \
+    constexpr int c = (2 * (K) < NC) ? 2 * (K) : 0;                                                     \
+    constexpr int c1 = (c + 1 < NC) ? c + 1 : c;                                                        \
+    mode = 0;                                                                                           \
+    fA = c;                                                                                             \
+    fB = (c + 1 < NC) ? c + 1 : -1;                                                                     \
+    _Pragma("unroll") for (int n2 = 0; n2 < B; ++n2) v[n2] =                                            \
+        make_float2(q[c][n2], (c + 1 < NC) ? q[c1][n2] : 0.0f);                                         \
+    break;                                                                                              \
+  }
+      PS_FX_CASE(0)
+      PS_FX_CASE(1)
+      PS_FX_CASE(2)
+#undef PS_FX_CASE
+#define PS_D_CASE(K)                                                                                    \
+  case 10 + (K): {                                                                                      \
+    constexpr int c = (2 * (K) < NC) ? 2 * (K) : 0;                                                     \
+    mode = 1;                                                                                           \
+    fA = c;                                                                                             \
+    fB = (c + 1 < NC) ? c + 1 : -1;                                                                     \
+    fill(v, 0, c, 0, (c + 1 < NC) ? c + 1 : -1);                                                        \
+    break;                                                                                              \
+  }
+      PS_D_CASE(0)
+      PS_D_CASE(1)
+      PS_D_CASE(2)
+#undef PS_D_CASE
+#define PS_P_CASE(K)                                                                                    \
+  case 20 + (K): {                                                                                      \
+    mode = 2;                                                                                           \
+    if constexpr (ND == 3) {                                                                            \
+      fA = NC + (K);                                                                                    \
+      fB = 2 * NC + (K);                                                                                \
+      fill(v, 1, (K), 2, (K));                                                                          \
+    } else {                                                                                            \
+      constexpr int c = (2 * (K) + 1 < NC) ? 2 * (K) : 0;                                               \
+      fA = NC + c;                                                                                      \
+      fB = NC + c + 1;                                                                                  \
+      fill(v, 1, c, 1, c + 1);                                                                          \
+    }                                                                                                   \
+    break;                                                                                              \
+  }
+      PS_P_CASE(0)
+      PS_P_CASE(1)
+      PS_P_CASE(2)
+      PS_P_CASE(3)
+      PS_P_CASE(4)
+#undef PS_P_CASE
+      default:
         mode = 2;
-        if (ND == 3) {
-          dirA = 1, cA = k, dirB = 2, cB = k;
-          fA = NC + k;
-          fB = 2 * NC + k;
-        } else {
-          dirA = dirB = 1;
-          cA = 2 * k;
-          cB = 2 * k + 1;
-          fA = NC + cA;
-          fB = NC + cB;
-        }
-      }
-      float oa[B], ob[B];
-      flux_vals(dirA, cA, oa);
-      if (cB >= 0) flux_vals(dirB, cB, ob);
+        fA = fB = -1;
 #pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(oa[n2], cB >= 0 ? ob[n2] : 0.0f);
+        for (int n2 = 0; n2 < B; ++n2) v[n2] = make_float2(0.0f, 0.0f);
     }
     pf.fwd(v);
     if (mode == 1) {
@@ -201,25 +218,36 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
 #pragma unroll
       for (int r = 0; r < B; ++r) {
         const float P = S.ax.P[pf.kidx(r)];
-        const float s = (mode == 0) ? (1.0f / N) - P : P;
-        v[r].x *= s;
-        v[r].y *= s;
+        const float sc = (mode == 0) ? (1.0f / N) - P : P;
+        v[r].x *= sc;
+        v[r].y *= sc;
       }
     }
     pf.inv(v);
     if (mode == 0) {
-#pragma unroll
-      for (int n2 = 0; n2 < B; ++n2) {
-        const float f0 = slot(fA, n2) - v[n2].x;
-        slot(fA, n2) = f0;
-        if (valid) a.Uw[fA * a.fs + rbase + A * n2] = f0;
-        if (fB >= 0) {
-          const float f1 = slot(fB, n2) - v[n2].y;
-          slot(fB, n2) = f1;
-          if (valid) a.Uw[fB * a.fs + rbase + A * n2] = f1;
-        }
+      switch (k) {
+#define PS_FX_BACK(K)                                                                                   \
+  case K: {                                                                                             \
+    constexpr int c = (2 * (K) < NC) ? 2 * (K) : 0;                                                     \
+    constexpr int c1 = (c + 1 < NC) ? c + 1 : c;                                                        \
+    _Pragma("unroll") for (int n2 = 0; n2 < B; ++n2) {                                                  \
+      q[c][n2] -= v[n2].x;                                                                              \
+      if (valid) a.Uw[c * a.fs + rbase + A * n2] = q[c][n2];                                            \
+      if constexpr (c + 1 < NC) {                                                                       \
+        q[c1][n2] -= v[n2].y;                                                                           \
+        if (valid) a.Uw[c1 * a.fs + rbase + A * n2] = q[c1][n2];                                        \
+      }                                                                                                 \
+    }                                                                                                   \
+    break;                                                                                              \
+  }
+        PS_FX_BACK(0)
+        PS_FX_BACK(1)
+        PS_FX_BACK(2)
+#undef PS_FX_BACK
+        default:
+          break;
       }
-    } else if (valid) {
+    } else if (valid && fA >= 0) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
         a.out[fA * a.fs + rbase + A * n2] = v[n2].x;

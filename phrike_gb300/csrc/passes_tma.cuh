@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
     k_ymid3_t(const __grid_constant__ CUtensorMap mG, YMidTArgs a) {
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  extern __shared__ __align__(1024) unsigned char smem_tma[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
   const int outer = blockIdx.y;
@@ -264,8 +264,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   constexpr int NC = ND + 2;
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  extern __shared__ __align__(1024) unsigned char smem_tma[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
   const int outer = blockIdx.y;
@@ -480,8 +480,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
     k_op_t(const __grid_constant__ CUtensorMap mIn, OpTArgs a) {
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_raw);
+  extern __shared__ __align__(1024) unsigned char smem_tma[];
+  auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
   const int outer = blockIdx.y;
