@@ -65,12 +65,21 @@ int ps_plan_desc_init(ps_plan_desc* desc, int ndim);
 
 /* Device scratch a plan allocates at creation (bytes), for HBM admission. */
 int ps_plan_scratch_bytes(const ps_plan_desc* desc, size_t* bytes);
+int ps_batch_scratch_bytes(const ps_plan_desc* desc, int nsolve, size_t* bytes);
 
 /* Build spectral tables and allocate scratch on the current device.
  * Replaces Grid*.__post_init__ + _setup_fourier_backend (grid.py:183-383,
  * 806-992, 1378-1495) and solver construction (solver.py:156-232). */
 int ps_plan_create(const ps_plan_desc* desc, ps_plan* out);
 int ps_plan_destroy(ps_plan plan);
+
+/* A batch: nsolve independent solves of the same grid in one plan.  Every
+ * field argument of the calls below then holds all solves back to back,
+ * [nsolve][ncomp][cells], and per-solve outputs are arrays of nsolve entries.
+ * A plain plan is a batch of one.  Replaces a Python loop over independent
+ * SpectralSolver*.run calls (solver.py:338-422 per solve). */
+int ps_batch_create(const ps_plan_desc* desc, int nsolve, ps_plan* out);
+int ps_plan_nsolve(ps_plan plan);
 
 /* rhs = -(sum_a d/dx_a F_a(U)) for U (ncomp fields).  Replaces
  * _compute_rhs / _compute_rhs_2d / _compute_rhs_3d (solver.py:62-93,
@@ -80,13 +89,22 @@ int ps_rhs(ps_plan plan, const float* U, float* rhs, void* stream);
 /* One fixed-dt RK4 step in place, including the positivity clamp (1D/2D)
  * and the end-of-step filter with the reference cadence.  Replaces
  * SpectralSolver*.step / _fixed_step (solver.py:242-269, 623-648,
- * 1313-1337).  If d_dt is non-NULL the step size is read from device memory
- * (one double) and `dt` is ignored, so the call can be captured in a graph. */
+ * 1313-1337).  If d_dt is non-NULL the step sizes are read from device memory
+ * (one double per solve) and `dt` is ignored, so the call can be captured in
+ * a graph. */
 int ps_step_rk4(ps_plan plan, float* U, double dt, const double* d_dt, void* stream);
 
 /* nsteps fixed-dt RK4 steps in place (same semantics as nsteps calls of
  * ps_step_rk4; consecutive steps share fused filter passes). */
 int ps_run_steps(ps_plan plan, float* U, int nsteps, double dt, const double* d_dt, void* stream);
+
+/* Up to nsteps CFL-driven RK4 steps with the time loop on the device: per
+ * solve, dt = min(cfl * h_min / max wave speed, t_end - t) from the state at
+ * the start of each step, t advances in d_t (nsolve doubles, updated in
+ * place), and a solve stops once t >= t_end - 1e-12.  No host
+ * synchronisation, so the call can be captured in a CUDA graph.  Replaces the
+ * while-loop of SpectralSolver*.run (solver.py:384-417, 773-800, 1480-1505). */
+int ps_run_cfl(ps_plan plan, float* U, int nsteps, double* d_t, const double* d_tend, void* stream);
 
 /* out = dx1/dy1/dz1(f) for nfields fields (axis 0 = x).  Replaces
  * Grid1D.dx1 (grid.py:512-522), Grid2D.dx1/dy1 (grid.py:1226-1252),
@@ -97,12 +115,12 @@ int ps_derivative(ps_plan plan, int axis, const float* f, float* out, int nfield
  * Grid*.apply_spectral_filter (grid.py:524-538, 1254-1287, 1723-1726). */
 int ps_filter(ps_plan plan, const float* f, float* out, int nfields, void* stream);
 
-/* *d_out (device float) = max wave speed of U with the reference's
+/* d_out (device floats, one per solve) = max wave speed of U with the reference's
  * per-dimension rule.  Replaces Euler*.max_wave_speed (equations.py:297-301,
  * 365-370, 609-620).  The result stays on the device. */
 int ps_max_wave_speed(ps_plan plan, const float* U, float* d_out, void* stream);
 
-/* d_out (device doubles, ncomp values: mass, momenta..., energy) = plain
+/* d_out (device doubles, ncomp values per solve: mass, momenta..., energy) = plain
  * sums of the conserved quantities, accumulated in float64.  Replaces the
  * solvers' record() (solver.py:372-377, 741-767, 1439-1468). */
 int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);

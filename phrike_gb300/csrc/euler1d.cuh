@@ -21,13 +21,20 @@ struct Step1DArgs {
   long solve_stride;  // elements between solves
   AxisOps ax;
   int nsteps;
-  const double* dt_dev;  // if non-null, dt = *dt_dev (one value for all solves)
+  const double* dt_dev;  // if non-null, per-solve step sizes dt_dev[solve]
   double dt;
+  const int* active;     // per-solve flags (null: all active)
   float gamma;
   float rho_min, p_min;
   int filter_interval;
   int step_counter0;     // cadence counter value before the first step
   float gx;              // gravity along x (0 when disabled)
+  // CFL mode (t != null): before each step dt = min(cfl dx / max(|u| + a),
+  // t_end - t) per solve; a solve stops once t >= t_end - 1e-12 (solver.py:384-417)
+  double* t;             // per-solve simulation time, advanced in place
+  const double* tend;    // per-solve end time
+  float cfl, dx;
+  int* steps_done;       // per-solve count of steps taken (CFL mode; may be null)
 };
 
 template <int N>
@@ -37,6 +44,7 @@ struct Step1DSmem {
   float un[3 * N];
   float us[3 * N];
   float acc[3 * N];
+  float red[32];
 };
 
 template <int N>
@@ -46,6 +54,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& S = *reinterpret_cast<Step1DSmem<N>*>(smem_raw);
   const int t = threadIdx.x;
+  if (a.active != nullptr && a.active[blockIdx.x] == 0) return;
   PF pf{0, t, S.buf, S.ax.twf, S.ax.twi};
   load_axis<N>(S.ax, a.ax);
   float* U = a.U + (long)blockIdx.x * a.solve_stride;
@@ -62,8 +71,12 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
       S.us[sl(c, n2)] = v;
     }
   __syncthreads();
-  const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
+  float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[blockIdx.x] : (float)a.dt;
   const float g1 = a.gamma - 1.0f;
+  double tl = (a.t != nullptr) ? a.t[blockIdx.x] : 0.0;
+  const double te = (a.tend != nullptr) ? a.tend[blockIdx.x] : 0.0;
+  int taken = 0;
+  const int cad0 = (a.steps_done != nullptr) ? a.steps_done[blockIdx.x] : a.step_counter0;
   const float href = a.gamma * er;
   const float pmin_shift = a.p_min - g1 * er;
 
@@ -85,6 +98,26 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
 
 #pragma unroll 1
   for (int step = 0; step < a.nsteps; ++step) {
+    double dtd = dt;
+    if (a.t != nullptr) {  // CFL step size from the current state (uniform across the CTA)
+      if (tl >= te - 1e-12) break;
+      float sm = 0.0f;
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const float rho = S.un[sl(0, n2)];
+        const float u = S.un[sl(1, n2)] / rho;
+        const float pp = g1 * (S.un[sl(2, n2)] - 0.5f * rho * u * u) + g1 * er;  // true pressure
+        sm = fmaxf(sm, fabsf(u) + sqrtf(a.gamma * pp / rho));
+      }
+      sm = block_max(sm, S.red);
+      if (threadIdx.x == 0) S.red[0] = sm;
+      __syncthreads();
+      const double spd = (double)S.red[0];
+      __syncthreads();
+      dtd = (spd <= 0.0) ? 1e-6 : (double)a.cfl * (double)a.dx / spd;
+      dtd = fmin(dtd, te - tl);
+      dt = (float)dtd;
+    }
 #pragma unroll 1
     for (int stage = 0; stage < 4; ++stage) {
       const RKCoef rc = rk4_coef(stage, dt);
@@ -141,7 +174,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
       }
     }
     // end of step: filter inside the RK step, then again by cadence
-    const bool second = ((a.step_counter0 + step) % a.filter_interval) == 0;
+    const bool second = ((cad0 + step) % a.filter_interval) == 0;
     float2 w01[B], w2[B];
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) {
@@ -163,6 +196,12 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
         S.us[sl(c, n2)] = v[c];
       }
     }
+    tl += dtd;
+    ++taken;
+  }
+  if (threadIdx.x == 0) {
+    if (a.t != nullptr) a.t[blockIdx.x] = tl;
+    if (a.steps_done != nullptr) a.steps_done[blockIdx.x] += taken;
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c)

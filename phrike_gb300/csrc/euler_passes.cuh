@@ -31,16 +31,21 @@ namespace ps {
 // X pass (pencils along the contiguous axis): optional fused filter P_x of the
 // incoming state, optional CFL speed, flux assembly, D_x / P_x.
 // ---------------------------------------------------------------------------
+// Batches: every buffer is [nsolve][nfields][cells]; a solve's fields are
+// contiguous and solves follow each other at the buffer's solve stride.
 struct XFirstArgs {
-  const float* U;    // [NC][rows][N]
-  float* Uw;         // if non-null: U after P_x is written here (fused filter)
-  float* out;        // [ND*NC][rows][N]: D_x F^x (NC), P_x F^y (NC), P_x F^z (NC)
-  long fs;           // elements per field
-  int rows;          // rows of the x-pencils (Ny*Nz)
+  const float* U;    // [nsolve][NC][rows_per_solve][N]
+  float* Uw;         // if non-null: U after P_x is written here (fused filter), same layout as U
+  float* out;        // [nsolve][ND*NC][..]: D_x F^x (NC), P_x F^y (NC), P_x F^z (NC)
+  long fs;           // elements per field (cells of one solve)
+  long ssU, ssOut;   // solve strides of U / Uw and of out
+  int rows;          // x-pencil rows of all solves
+  int rps;           // rows per solve (Ny*Nz)
   AxisOps ax;
   float gamma;
-  float* speed;      // if non-null: atomic max of the CFL wave speed
-  const float* eref; // device scalar E_ref of the energy-perturbation form
+  float* speed;      // if non-null: per-solve atomic max of the CFL wave speed
+  const float* eref; // per-solve E_ref of the energy-perturbation form
+  const int* active; // per-solve flags (null: all active); inactive solves are not written
   int shift_in;      // 1: U holds E (subtract E_ref on load); 0: U holds E'
 };
 
@@ -65,12 +70,22 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   const int t = threadIdx.x % A;
   const int p = threadIdx.x / A;
   const int row = blockIdx.x * T + p;
-  const bool valid = row < a.rows;
+  const int sol = (row < a.rows ? row : a.rows - 1) / a.rps;
+  const bool live = a.active == nullptr || a.active[sol] != 0;
+  const bool valid = row < a.rows && live;
+  {  // a CTA whose rows all belong to inactive solves has nothing to do
+    const int r0 = blockIdx.x * T, r1 = min(r0 + T, a.rows) - 1;
+    bool any = a.active == nullptr;
+    for (int s2 = r0 / a.rps; !any && s2 <= r1 / a.rps; ++s2) any = a.active[s2] != 0;
+    if (!any) return;
+  }
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   load_axis<N>(S.ax, a.ax);
 
-  const long rbase = (long)row * N + t;
-  const float er = *a.eref;
+  const long rloc = (long)(row % a.rps) * N + t;
+  const long rbase = (long)sol * a.ssU + rloc;    // U / Uw
+  const long obase = (long)sol * a.ssOut + rloc;  // out
+  const float er = a.eref[sol];
   const float eshift = a.shift_in ? er : 0.0f;
   const float pref = (a.gamma - 1.0f) * er;
   const float href = a.gamma * er;
@@ -142,8 +157,14 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
         }
       }
       if (a.speed != nullptr) {
-        const float m = block_max(smax, S.red);
-        if (threadIdx.x == 0) atomic_max_nonneg(a.speed, m);
+        const int s0 = (blockIdx.x * T) / a.rps;
+        const int s1 = (min(blockIdx.x * T + T, a.rows) - 1) / a.rps;
+        if (s0 == s1) {
+          const float m = block_max(smax, S.red);
+          if (threadIdx.x == 0) atomic_max_nonneg(a.speed + s0, m);
+        } else if (valid) {  // rows of several small solves in one CTA
+          atomic_max_nonneg(a.speed + sol, smax);
+        }
       }
     }
     // job -> (mode, output fields); the switch fills v with constant register indices
@@ -250,8 +271,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
     } else if (valid && fA >= 0) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        a.out[fA * a.fs + rbase + A * n2] = v[n2].x;
-        if (fB >= 0) a.out[fB * a.fs + rbase + A * n2] = v[n2].y;
+        a.out[fA * a.fs + obase + A * n2] = v[n2].x;
+        if (fB >= 0) a.out[fB * a.fs + obase + A * n2] = v[n2].y;
       }
     }
   }
@@ -298,7 +319,9 @@ struct OpArgs {
   float* out;
   int nf;
   long fs;
-  int rows;          // contiguous: number of rows
+  long ss;           // solve stride of in and out
+  int rows;          // contiguous: rows of all solves
+  int rps;           // rows per solve
   StridedGeom g;     // strided geometry
   AxisOps ax;
   int deriv;         // 0: P, 1: D
@@ -327,7 +350,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
     p = threadIdx.x / A;
     const int row = blockIdx.x * T + p;
     valid = row < a.rows;
-    base = (long)row * N + t;
+    const int r = valid ? row : 0;
+    base = (long)(r / a.rps) * a.ss + (long)(r % a.rps) * N + t;
     step = A;
   }
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};

@@ -39,15 +39,16 @@ struct Ring {
   alignas(1024) float slot[R][N * T];
   uint64_t bar[R];
   int abort;
-  int sched[64];  // tile schedule: map id * 64 + field
+  int sched[64];  // tile schedule: map id * 256 + field within the solve
   int ntiles;
 };
 
-// Which axis the pencils run along: 1 = y, 2 = z.
+// Which axis the pencils run along (1 = y, 2 = z), and where the tile sits.
 struct TileIssue {
   int axis;
-  int x0;     // first column of the tile
-  int outer;  // z (axis 1) or y (axis 2)
+  int x0;        // first column of the tile
+  int outer;     // z (axis 1) or y (axis 2)
+  int fbase[3];  // per map: field coordinate of this solve's first field (solve * fields per solve)
 };
 
 template <int N, int T, int R>
@@ -56,8 +57,8 @@ __device__ __forceinline__ void ring_issue(Ring<N, T, R>& rg, int i, const CUten
   using G = TileGeom<N, T>;
   const int s = i % R;
   const int code = rg.sched[i];
-  const CUtensorMap* m = maps[code >> 6];
-  const int f = code & 63;
+  const CUtensorMap* m = maps[code >> 8];
+  const int f = ti.fbase[code >> 8] + (code & 255);
   mbar_arrive_expect_tx(&rg.bar[s], G::BYTES);
 #pragma unroll
   for (int b = 0; b < G::NBOX; ++b) {
@@ -153,10 +154,12 @@ struct TmaStridedSmem {
 // 3D y pass.  Map 0 = G buffer (15 fields: G, Hy, Hz).  Output via st.global.
 // ---------------------------------------------------------------------------
 struct YMidTArgs {
-  float* out;      // 10 fields [A(5), B(5)]
+  float* out;      // 10 fields per solve [A(5), B(5)]
   long fs;
-  StridedGeom g;
+  long ssOut;      // solve stride of out (10 * cells)
+  StridedGeom g;   // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   AxisOps ax;
+  const int* active;
   int* status;
 };
 
@@ -169,7 +172,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
-  const int outer = blockIdx.y;
+  const int sol = blockIdx.y / a.g.nouter;
+  const int outer = blockIdx.y % a.g.nouter;
+  if (a.active != nullptr && a.active[sol] == 0) return;
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   ring_init(S.ring);
   if (threadIdx.x == 0) {
@@ -181,9 +186,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
   const CUtensorMap* maps[1] = {&mG};
-  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{1, (int)(blockIdx.x * T), outer}, a.status, 0};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{1, (int)(blockIdx.x * T), outer, {sol * 15, 0, 0}}, a.status, 0};
   rc.start();
-  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long base = (long)sol * a.ssOut + (long)outer * a.g.os + col + (long)t * a.g.as;
   const long step = (long)A * a.g.as;
   const bool valid = col < a.g.ncol;
   int ti = 0;
@@ -239,20 +244,23 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 // at fb0 + c), 1 = U^n, 2 = accumulator.  Writes via st.global.
 // ---------------------------------------------------------------------------
 struct LastTArgs {
-  int fa0, fb0;        // field offsets of a_0 and b_0 in map 0
+  int fa0, fb0;        // field offsets of a_0 and b_0 in map 0 (within a solve)
+  int nfAB;            // fields per solve in map 0
   float* acc;          // accumulator (written)
   float* out;          // rhs / next stage input / new state
   long fs;
-  StridedGeom g;
+  long ssAcc, ssOut, ssUn;  // solve strides of acc, out and Un
+  const int* active;   // per-solve flags (null: all active)
+  StridedGeom g;       // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   int axis;            // 1: y pencils, 2: z pencils
   AxisOps ax;
   int stage;           // -1 rhs only, 0..3 RK4 stage
   const float* Un;     // U^n (global; used by the clamped variant)
-  const double* dt_dev;
+  const double* dt_dev;  // per-solve step sizes (null: dt for every solve)
   double dt;
   float gamma;
   float rho_min, p_min;
-  const float* eref;
+  const float* eref;     // per-solve E_ref
   int filter_last;
   int* status;
 };
@@ -268,7 +276,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
-  const int outer = blockIdx.y;
+  const int sol = blockIdx.y / a.g.nouter;
+  const int outer = blockIdx.y % a.g.nouter;
+  if (a.active != nullptr && a.active[sol] == 0) return;
   const bool valid = col < a.g.ncol;
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   ring_init(S.ring);
@@ -281,22 +291,27 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
       for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fa0 + c + q;
       for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fb0 + c + q;
       if (need_un)
-        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 64 + c + q;
+        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 256 + c + q;
       if (need_acc)
-        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 128 + c + q;
+        for (int q = 0; q < m; ++q) S.ring.sched[n++] = 512 + c + q;
     }
     S.ring.ntiles = n;
   }
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
   const CUtensorMap* maps[3] = {&mAB, &mU, &mAcc};
-  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer}, a.status, 0};
+  RingCursor<N, T, R> rc{S.ring, maps,
+                         TileIssue{a.axis, (int)(blockIdx.x * T), outer, {sol * a.nfAB, sol * NC, sol * NC}},
+                         a.status, 0};
   rc.start();
-  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;  // within a solve
   const long step = (long)A * a.g.as;
-  const float dt = (a.dt_dev != nullptr) ? (float)(*a.dt_dev) : (float)a.dt;
+  const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
   const RKCoef rk = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
-  const float pmin_shift = a.p_min - (a.gamma - 1.0f) * (*a.eref);
+  const float pmin_shift = a.p_min - (a.gamma - 1.0f) * a.eref[sol];
+  float* const acc_s = (a.acc != nullptr) ? a.acc + (long)sol * a.ssAcc : nullptr;
+  float* const out_s = a.out + (long)sol * a.ssOut;
+  const float* const un_s = a.Un + (long)sol * a.ssUn;
   auto addr = [&](int c, int n2) { return c * a.fs + base + n2 * step; };
   auto filter_pair = [&](float2 (&w)[B]) {  // complementary form
     float2 w0[B];
@@ -340,8 +355,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
         if (valid) {
 #pragma unroll
           for (int n2 = 0; n2 < B; ++n2) {
-            a.out[addr(c, n2)] = w[n2].x;
-            if (two) a.out[addr(c + 1, n2)] = w[n2].y;
+            out_s[addr(c, n2)] = w[n2].x;
+            if (two) out_s[addr(c + 1, n2)] = w[n2].y;
           }
         }
         continue;
@@ -369,7 +384,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
           } else {
             const float un = tu[q][r];
             const float ac = fmaf(rk.wacc, k[q], (a.stage == 0) ? un : tacc[q][r]);
-            if (valid) a.acc[addr(c + q, n2)] = ac;
+            if (valid) acc_s[addr(c + q, n2)] = ac;
             res[q] = fmaf(rk.wnext, k[q], un);
           }
         }
@@ -380,8 +395,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
       if (valid) {
 #pragma unroll
         for (int n2 = 0; n2 < B; ++n2) {
-          a.out[addr(c, n2)] = w[n2].x;
-          if (two) a.out[addr(c + 1, n2)] = w[n2].y;
+          out_s[addr(c, n2)] = w[n2].x;
+          if (two) out_s[addr(c + 1, n2)] = w[n2].y;
         }
       }
     }
@@ -395,8 +410,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
         for (int c = 0; c < NC; c += 2)
 #pragma unroll
           for (int n2 = 0; n2 < B; ++n2) {
-            a.out[addr(c, n2)] = kk[c / 2][n2].x;
-            if (c + 1 < NC) a.out[addr(c + 1, n2)] = kk[c / 2][n2].y;
+            out_s[addr(c, n2)] = kk[c / 2][n2].x;
+            if (c + 1 < NC) out_s[addr(c + 1, n2)] = kk[c / 2][n2].y;
           }
       }
     } else {
@@ -408,8 +423,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
         for (int j = 0; j < CH; ++j)
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
-            un[j][c] = (valid && a.stage != 3) ? __ldg(a.Un + addr(c, n0 + j)) : 0.0f;
-            ac[j][c] = (valid && a.stage != 0) ? a.acc[addr(c, n0 + j)] : 0.0f;
+            un[j][c] = (valid && a.stage != 3) ? __ldg(un_s + addr(c, n0 + j)) : 0.0f;
+            ac[j][c] = (valid && a.stage != 0) ? acc_s[addr(c, n0 + j)] : 0.0f;
           }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
@@ -438,7 +453,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 #pragma unroll
           for (int j = 0; j < CH; ++j)
 #pragma unroll
-            for (int c = 0; c < NC; ++c) a.acc[addr(c, n0 + j)] = ac[j][c];
+            for (int c = 0; c < NC; ++c) acc_s[addr(c, n0 + j)] = ac[j][c];
         }
       }
 #pragma unroll
@@ -447,8 +462,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
         if (valid) {
 #pragma unroll
           for (int n2 = 0; n2 < B; ++n2) {
-            a.out[addr(c, n2)] = kk[c / 2][n2].x;
-            if (c + 1 < NC) a.out[addr(c + 1, n2)] = kk[c / 2][n2].y;
+            out_s[addr(c, n2)] = kk[c / 2][n2].x;
+            if (c + 1 < NC) out_s[addr(c + 1, n2)] = kk[c / 2][n2].y;
           }
         }
       }
@@ -464,9 +479,11 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 // ---------------------------------------------------------------------------
 struct OpTArgs {
   float* out;
-  int nf;
+  int nf;          // fields per solve (map fields per solve as well)
   long fs;
-  StridedGeom g;
+  long ss;         // solve stride of out
+  const int* active;
+  StridedGeom g;   // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   int axis;
   AxisOps ax;
   int deriv;
@@ -484,7 +501,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   auto& S = *reinterpret_cast<TmaStridedSmem<N, T, R>*>(smem_tma);
   const int p = threadIdx.x % T, t = threadIdx.x / T;
   const int col = blockIdx.x * T + p;
-  const int outer = blockIdx.y;
+  const int sol = blockIdx.y / a.g.nouter;
+  const int outer = blockIdx.y % a.g.nouter;
+  if (a.active != nullptr && a.active[sol] == 0) return;
   const bool valid = col < a.g.ncol;
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   ring_init(S.ring);
@@ -495,9 +514,10 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
   const CUtensorMap* maps[1] = {&mIn};
-  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer}, a.status, 0};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer, {sol * a.nf, 0, 0}},
+                         a.status, 0};
   rc.start();
-  const long base = (long)outer * a.g.os + col + (long)t * a.g.as;
+  const long base = (long)sol * a.ss + (long)outer * a.g.os + col + (long)t * a.g.as;
   const long step = (long)A * a.g.as;
   const bool comp = a.complement && !a.deriv;
   int ti = 0;

@@ -54,30 +54,34 @@ int record_error(int code, const char* msg) {
 struct ps_plan_s {
   ps_plan_desc desc;
   int nd = 0;
+  int nsolve = 1;  // independent solves of the same grid (a batch)
   int n[3] = {1, 1, 1};
-  long cells = 0;
+  long cells = 0;  // cells of one solve
   int nc = 0;
   // per-axis spectral tables (device): P, d, twf, twi
   float* P[3] = {nullptr, nullptr, nullptr};
   float* d[3] = {nullptr, nullptr, nullptr};
   float2* twf[3] = {nullptr, nullptr, nullptr};
   float2* twi[3] = {nullptr, nullptr, nullptr};
-  // scratch
-  float* G = nullptr;    // X-pass outputs (2D: 8 fields, 3D: 15)
-  float* AB = nullptr;   // 3D Y-pass outputs (10 fields)
+  // scratch, [nsolve][nfields][cells] each
+  float* G = nullptr;    // x-pass outputs (2D: 8 fields, 3D: 15)
+  float* AB = nullptr;   // 3D y-pass outputs (10 fields)
   float* acc = nullptr;  // RK accumulator (nc fields)
   float* Us = nullptr;   // stage input (nc fields)
   float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
-  float* speed = nullptr;
-  float* eref = nullptr;  // E_ref of the energy-perturbation form (device scalar)
-  int* status = nullptr;  // device status word (PS_STATUS_* bits set by kernels)
+  // per-solve device scalars
+  float* speed = nullptr;  // CFL wave speed maxima
+  float* eref = nullptr;   // E_ref of the energy-perturbation form
+  double* dt = nullptr;    // step sizes (CFL runs)
+  int* active = nullptr;   // 1 while a solve advances (CFL runs)
+  int* steps_done = nullptr;
+  int* status = nullptr;   // device status word (PS_STATUS_* bits set by kernels)
   // TMA tensor maps of the plan buffers and of the last state pointer seen
   CUtensorMap map_G_y{};    // G, y pencils
   CUtensorMap map_AB_z{};   // AB, z pencils (3D)
   CUtensorMap map_acc{};    // acc, last-pass pencils
   const float* map_U_ptr = nullptr;
   CUtensorMap map_U_last{};  // state, last-pass pencils
-  CUtensorMap map_U_y{};     // state, y pencils (3D filter pass)
   long step_counter = 0;
   std::vector<void*> allocations;
   // launch profiling: CUDA events around every pass launch
@@ -91,7 +95,13 @@ struct ps_plan_s {
   std::vector<cudaEvent_t> event_pool;
 
   ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
-  float* field(float* base, int i) const { return base + (long)i * cells; }
+  long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
+  int rows() const { return (int)(cells / n[0]); }     // x-pencil rows of one solve
+  double hmin() const {                                 // smallest grid spacing (CFL)
+    double h = desc.length[0] / n[0];
+    for (int a = 1; a < nd; ++a) h = fmin(h, desc.length[a] / n[a]);
+    return h;
+  }
 };
 
 namespace {
@@ -237,8 +247,10 @@ int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, 
 
 namespace {
 
+
+// maps over the batch: a buffer of nsolve solves x nf fields is nsolve*nf fields
 int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int axis) {
-  return ps::encode_field_map(m, base, p->n, nf, axis);
+  return ps::encode_field_map(m, base, p->n, p->nsolve * nf, axis);
 }
 
 // maps of the caller's state pointer (re-encoded when the pointer changes)
@@ -247,7 +259,6 @@ int state_maps(ps_plan p, const float* U) {
   int rc;
   const int last_axis = (p->nd == 3) ? 2 : 1;
   if ((rc = make_map(&p->map_U_last, U, p, p->nc, last_axis)) != PS_OK) return rc;
-  if (p->nd == 3 && (rc = make_map(&p->map_U_y, U, p, p->nc, 1)) != PS_OK) return rc;
   p->map_U_ptr = U;
   return PS_OK;
 }
@@ -261,18 +272,21 @@ ps::StridedGeom geom_z(const ps_plan_s* p) {
   return ps::StridedGeom{p->n[0], (long)p->n[0] * p->n[1], (long)p->n[0], p->n[1]};
 }
 
-// One-axis operator on nf fields (P or D), axis 0 = x.
+// One-axis operator on nf fields per solve (P, D or complementary P), axis 0 = x.
 int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s,
-             bool complement = false) {
-  ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells);
+             bool complement = false, const int* active = nullptr) {
+  ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells * p->nsolve);
   cudaError_t e;
   if (axis == 0) {
+    if (active != nullptr) return fail(PS_ERR_INVALID, "internal: masked x operator");
     ps::OpArgs a{};
     a.in = in;
     a.out = out;
     a.nf = nf;
     a.fs = p->cells;
-    a.rows = (int)(p->cells / p->n[0]);
+    a.ss = p->ss(nf);
+    a.rows = p->rows() * p->nsolve;
+    a.rps = p->rows();
     a.ax = p->ax(0);
     a.deriv = deriv;
     a.scale = scale;
@@ -287,6 +301,8 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
     a.out = out;
     a.nf = nf;
     a.fs = p->cells;
+    a.ss = p->ss(nf);
+    a.active = active;
     a.g = (axis == 1) ? geom_y(p) : geom_z(p);
     a.axis = axis;
     a.ax = p->ax(axis);
@@ -300,19 +316,25 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
   return PS_OK;
 }
 
-int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, bool shift_in = false) {
+int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, bool shift_in = false,
+           const int* active = nullptr) {
   ps::XFirstArgs a{};
   a.U = U;
   a.Uw = Uw;
   a.out = p->G;
   a.fs = p->cells;
-  a.rows = (int)(p->cells / p->n[0]);
+  a.ssU = p->ss(p->nc);
+  a.ssOut = p->ss(p->nd * p->nc);
+  a.rows = p->rows() * p->nsolve;
+  a.rps = p->rows();
   a.ax = p->ax(0);
   a.gamma = (float)p->desc.gamma;
   a.speed = speed;
   a.eref = p->eref;
+  a.active = active;
   a.shift_in = shift_in ? 1 : 0;
-  ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * (p->nc * (Uw ? 2 : 1) + p->nd * p->nc));
+  ProfScope prof(p, s, PS_KIND_X,
+                 4.0 * p->cells * p->nsolve * (p->nc * (Uw ? 2 : 1) + p->nd * p->nc));
   cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
     return ps::launch_xfirst<decltype(nc)::value>(p->nd, a, s);
   });
@@ -320,14 +342,16 @@ int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, b
   return PS_OK;
 }
 
-int ymid(ps_plan p, cudaStream_t s) {
+int ymid(ps_plan p, cudaStream_t s, const int* active) {
   ps::YMidTArgs a{};
   a.out = p->AB;
   a.fs = p->cells;
+  a.ssOut = p->ss(10);
   a.g = geom_y(p);
   a.ax = p->ax(1);
+  a.active = active;
   a.status = p->status;
-  ProfScope prof(p, s, PS_KIND_Y, 4.0 * p->cells * 25);
+  ProfScope prof(p, s, PS_KIND_Y, 4.0 * p->cells * p->nsolve * 25);
   cudaError_t e = ps::dispatch_n(p->n[1], [&](auto nc) {
     return ps::launch_ymid3_t<decltype(nc)::value>(p->map_G_y, a, s);
   });
@@ -336,7 +360,7 @@ int ymid(ps_plan p, cudaStream_t s) {
 }
 
 int last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
-         cudaStream_t s) {
+         cudaStream_t s, const int* active) {
   int rc;
   if ((rc = state_maps(p, Un)) != PS_OK) return rc;
   ps::LastTArgs a{};
@@ -345,6 +369,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   if (p->nd == 3) {
     a.fa0 = 0;
     a.fb0 = 5;
+    a.nfAB = 10;
     a.g = geom_z(p);
     a.axis = 2;
     a.ax = p->ax(2);
@@ -352,6 +377,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   } else {
     a.fa0 = 0;
     a.fb0 = nc;
+    a.nfAB = 2 * nc;
     a.g = geom_y(p);
     a.axis = 1;
     a.ax = p->ax(1);
@@ -360,6 +386,10 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   a.acc = p->acc;
   a.out = out;
   a.fs = p->cells;
+  a.ssAcc = p->ss(nc);
+  a.ssOut = p->ss(nc);
+  a.ssUn = p->ss(nc);
+  a.active = active;
   a.stage = stage;
   a.Un = Un;
   a.dt_dev = d_dt;
@@ -374,7 +404,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
-  ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * nc * (2 + st_words));
+  ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * p->nsolve * nc * (2 + st_words));
   cudaError_t e = ps::dispatch_n(naxis, [&](auto nc2) {
     return ps::launch_last_t<decltype(nc2)::value>(p->nd, *mAB, p->map_U_last, p->map_acc, a, s);
   });
@@ -387,54 +417,151 @@ bool filter_due(ps_plan p, long counter) {
   return (counter % p->desc.filter_interval) == 0;
 }
 
-int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cudaStream_t s) {
+int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+            cudaStream_t s) {
   ps::Step1DArgs a{};
   a.U = U;
-  a.solve_stride = 0;
+  a.solve_stride = p->ss(3);
   a.ax = p->ax(0);
   a.nsteps = nsteps;
   a.dt_dev = d_dt;
   a.dt = dt;
+  a.active = nullptr;
   a.gamma = (float)p->desc.gamma;
   a.rho_min = 1e-10f;  // _positivity_clamp floors (solver.py:32)
   a.p_min = 1e-12f;
   a.filter_interval = p->desc.filter_interval;
   a.step_counter0 = (int)(p->step_counter % p->desc.filter_interval);
   a.gx = (float)p->desc.gravity[0];
-  ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3);
-  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_step1d<decltype(nc)::value>(a, 1, s); });
+  a.t = d_t;
+  a.tend = d_tend;
+  a.cfl = (float)p->desc.cfl;
+  a.dx = (float)(p->desc.length[0] / p->n[0]);
+  a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
+  ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3 * p->nsolve);
+  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
+    return ps::launch_step1d<decltype(nc)::value>(a, p->nsolve, s);
+  });
   if (e != cudaSuccess) return cuda_fail(e, "1D step");
-  p->step_counter += nsteps;
+  if (d_t == nullptr) p->step_counter += nsteps;
   return PS_OK;
 }
 
-// nsteps RK4 steps for 2D/3D; the x axis of the end-of-step filter of step i
-// is fused into the first x pass of step i+1.
-int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, cudaStream_t s) {
+// nsteps RK4 steps for 2D/3D batches.  Fixed step: dt (or per-solve d_dt).
+// CFL mode (d_t != null): per-solve dt from the fused x-pass speed, solves
+// stop at their end time.  The x axis of the end-of-step filter of step i is
+// fused into the first x pass of step i+1.
+int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+             cudaStream_t s) {
   int rc;
+  const bool cfl = d_t != nullptr;
+  const int* act = cfl ? p->active : nullptr;
+  const double* dtp = cfl ? p->dt : d_dt;
   bool pending_px = false;
   float* UE = U + (long)(p->nc - 1) * p->cells;
-  PS_CU(ps::launch_eref_set(UE, p->eref, s), "energy reference");
-  PS_CU(ps::launch_energy_shift(UE, p->cells, p->eref, -1.0f, s), "energy shift");
+  const long ssU = p->ss(p->nc);
+  PS_CU(ps::launch_eref_set(UE, ssU, p->nsolve, p->eref, s), "energy reference");
+  PS_CU(ps::launch_energy_shift(UE, p->cells, ssU, p->nsolve, p->eref, -1.0f, s), "energy shift");
+  if (cfl) {
+    PS_CU(cudaMemsetAsync(p->speed, 0, sizeof(float) * p->nsolve, s), "speed reset");
+    PS_CU(ps::launch_fill_int(p->active, p->nsolve, 1, s), "active reset");
+  }
   for (int it = 0; it < nsteps; ++it) {
     const bool filt = filter_due(p, p->step_counter);
     for (int stage = 0; stage < 4; ++stage) {
       const float* src = (stage == 0) ? U : p->Us;
       float* Uw = (stage == 0 && pending_px) ? U : nullptr;
-      if ((rc = xfirst(p, src, Uw, nullptr, s)) != PS_OK) return rc;
-      if (p->nd == 3 && (rc = ymid(p, s)) != PS_OK) return rc;
+      if ((rc = xfirst(p, src, Uw, (cfl && stage == 0) ? p->speed : nullptr, s, false, act)) != PS_OK) return rc;
+      if (cfl && stage == 0)
+        PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
+              "step control");
+      if (p->nd == 3 && (rc = ymid(p, s, act)) != PS_OK) return rc;
       float* out = (stage < 3) ? p->Us : U;
-      if ((rc = last(p, stage, U, out, dt, d_dt, filt && stage == 3, s)) != PS_OK) return rc;
+      if ((rc = last(p, stage, U, out, dt, dtp, filt && stage == 3, s, act)) != PS_OK) return rc;
     }
     pending_px = false;
     if (filt) {
-      if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s, true)) != PS_OK) return rc;
+      if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s, true, act)) != PS_OK) return rc;
       pending_px = true;
     }
+    if (cfl) PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->nsolve, s), "step advance");
     p->step_counter += 1;
   }
-  if (pending_px && (rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s, true)) != PS_OK) return rc;
-  PS_CU(ps::launch_energy_shift(UE, p->cells, p->eref, 1.0f, s), "energy shift");
+  if (pending_px) {
+    if (act != nullptr) {
+      // solves that took the last step still owe the x factor of its filter
+      if ((rc = xfirst(p, U, U, nullptr, s, false, act)) != PS_OK) return rc;
+    } else if ((rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s, true)) != PS_OK) {
+      return rc;
+    }
+  }
+  PS_CU(ps::launch_energy_shift(UE, p->cells, ssU, p->nsolve, p->eref, 1.0f, s), "energy shift");
+  return PS_OK;
+}
+
+int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
+  int rc = validate(d);
+  if (rc != PS_OK) return rc;
+  if (!out) return fail(PS_ERR_INVALID, "null output handle");
+  if (nsolve < 1) return fail(PS_ERR_INVALID, "nsolve must be >= 1");
+  ps_plan p = new ps_plan_s();
+  p->desc = *d;
+  p->nd = d->ndim;
+  p->nc = d->ndim + 2;
+  p->nsolve = nsolve;
+  p->cells = 1;
+  for (int a = 0; a < p->nd; ++a) {
+    p->n[a] = d->n[a];
+    p->cells *= d->n[a];
+  }
+  if ((long)nsolve * p->nc > (1L << 30)) return fail(PS_ERR_INVALID, "batch too large");
+  auto cleanup = [&](int code) {
+    ps_plan_destroy(p);
+    return code;
+  };
+  for (int a = 0; a < p->nd; ++a) {
+    std::vector<float> P, dd;
+    std::vector<float2> twf, twi;
+    build_axis(p->n[a], d->length[a], d->dealias, d->filter_enabled, d->filter_p, d->filter_alpha, P, dd, twf, twi);
+    const int N = p->n[a];
+    if ((rc = dalloc(p, &p->P[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->d[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->twf[a], N)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->twi[a], N)) != PS_OK) return cleanup(rc);
+    cudaError_t e;
+    if ((e = cudaMemcpy(p->P[a], P.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->d[a], dd.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->twf[a], twf.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->twi[a], twi.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cleanup(cuda_fail(e, "table upload"));
+  }
+  const long c = p->cells * nsolve;
+  if (p->nd == 1) {
+    if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
+  } else {
+    const int ng = (p->nd == 3) ? 15 : 8;
+    if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
+    if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
+    if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
+  }
+  if ((rc = dalloc(p, &p->speed, nsolve)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->eref, nsolve)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->dt, nsolve)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->active, nsolve)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->steps_done, nsolve)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->status, 1)) != PS_OK) return cleanup(rc);
+  if (cudaMemset(p->eref, 0, sizeof(float) * nsolve) != cudaSuccess ||
+      cudaMemset(p->speed, 0, sizeof(float) * nsolve) != cudaSuccess ||
+      cudaMemset(p->steps_done, 0, sizeof(int) * nsolve) != cudaSuccess ||
+      cudaMemset(p->status, 0, sizeof(int)) != cudaSuccess)
+    return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
+  if (p->nd >= 2) {
+    if ((rc = make_map(&p->map_G_y, p->G, p, (p->nd == 3) ? 15 : 8, 1)) != PS_OK) return cleanup(rc);
+    if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
+    if ((rc = make_map(&p->map_acc, p->acc, p, p->nc, (p->nd == 3) ? 2 : 1)) != PS_OK) return cleanup(rc);
+  }
+  *out = p;
   return PS_OK;
 }
 
@@ -444,7 +571,7 @@ extern "C" {
 
 const char* ps_last_error(void) { return g_err.c_str(); }
 
-const char* ps_version(void) { return "phrike_gb300 0.1.0 (sm_103a)"; }
+const char* ps_version(void) { return "phrike_gb300 0.2.0 (sm_103a)"; }
 
 int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
@@ -466,74 +593,24 @@ int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   return PS_OK;
 }
 
-int ps_plan_scratch_bytes(const ps_plan_desc* d, size_t* bytes) {
+int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   int rc = validate(d);
   if (rc != PS_OK) return rc;
   if (!bytes) return fail(PS_ERR_INVALID, "null output");
+  if (nsolve < 1) return fail(PS_ERR_INVALID, "nsolve must be >= 1");
   long cells = 1;
   for (int a = 0; a < d->ndim; ++a) cells *= d->n[a];
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
-  *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) + tables + 64;
+  *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
 
-int ps_plan_create(const ps_plan_desc* d, ps_plan* out) {
-  int rc = validate(d);
-  if (rc != PS_OK) return rc;
-  if (!out) return fail(PS_ERR_INVALID, "null output handle");
-  ps_plan p = new ps_plan_s();
-  p->desc = *d;
-  p->nd = d->ndim;
-  p->nc = d->ndim + 2;
-  p->cells = 1;
-  for (int a = 0; a < p->nd; ++a) {
-    p->n[a] = d->n[a];
-    p->cells *= d->n[a];
-  }
-  auto cleanup = [&](int code) {
-    ps_plan_destroy(p);
-    return code;
-  };
-  for (int a = 0; a < p->nd; ++a) {
-    std::vector<float> P, dd;
-    std::vector<float2> twf, twi;
-    build_axis(p->n[a], d->length[a], d->dealias, d->filter_enabled, d->filter_p, d->filter_alpha, P, dd, twf, twi);
-    const int N = p->n[a];
-    if ((rc = dalloc(p, &p->P[a], N)) != PS_OK) return cleanup(rc);
-    if ((rc = dalloc(p, &p->d[a], N)) != PS_OK) return cleanup(rc);
-    if ((rc = dalloc(p, &p->twf[a], N)) != PS_OK) return cleanup(rc);
-    if ((rc = dalloc(p, &p->twi[a], N)) != PS_OK) return cleanup(rc);
-    cudaError_t e;
-    if ((e = cudaMemcpy(p->P[a], P.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(p->d[a], dd.data(), N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(p->twf[a], twf.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(p->twi[a], twi.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
-      return cleanup(cuda_fail(e, "table upload"));
-  }
-  const long c = p->cells;
-  if (p->nd == 1) {
-    if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
-  } else {
-    const int ng = (p->nd == 3) ? 15 : 8;
-    if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
-    if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
-    if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
-    if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
-  }
-  if ((rc = dalloc(p, &p->speed, 1)) != PS_OK) return cleanup(rc);
-  if ((rc = dalloc(p, &p->eref, 1)) != PS_OK) return cleanup(rc);
-  if ((rc = dalloc(p, &p->status, 1)) != PS_OK) return cleanup(rc);
-  if (cudaMemset(p->eref, 0, sizeof(float)) != cudaSuccess || cudaMemset(p->status, 0, sizeof(int)) != cudaSuccess)
-    return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
-  if (p->nd >= 2) {
-    if ((rc = make_map(&p->map_G_y, p->G, p, (p->nd == 3) ? 15 : 8, 1)) != PS_OK) return cleanup(rc);
-    if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
-    if ((rc = make_map(&p->map_acc, p->acc, p, p->nc, (p->nd == 3) ? 2 : 1)) != PS_OK) return cleanup(rc);
-  }
-  *out = p;
-  return PS_OK;
-}
+int ps_plan_scratch_bytes(const ps_plan_desc* d, size_t* bytes) { return ps_batch_scratch_bytes(d, 1, bytes); }
+
+int ps_plan_create(const ps_plan_desc* d, ps_plan* out) { return create(d, 1, out); }
+
+int ps_batch_create(const ps_plan_desc* d, int nsolve, ps_plan* out) { return create(d, nsolve, out); }
 
 int ps_plan_destroy(ps_plan p) {
   if (!p) return PS_OK;
@@ -548,6 +625,8 @@ int ps_plan_destroy(ps_plan p) {
 }
 
 int ps_plan_ncomp(ps_plan p) { return p ? p->nc : -1; }
+
+int ps_plan_nsolve(ps_plan p) { return p ? p->nsolve : -1; }
 
 int ps_plan_status(ps_plan p, int* status) {
   if (!p || !status) return fail(PS_ERR_INVALID, "null argument");
@@ -592,13 +671,14 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   int rc;
   if (p->nd == 1) {
-    PS_CU(ps::launch_flux1d(U, p->cells, (float)p->desc.gamma, p->F1, s), "1D flux");
+    PS_CU(ps::launch_flux1d(U, p->cells, p->ss(3), p->nsolve, (float)p->desc.gamma, p->F1, s), "1D flux");
     return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
   }
-  PS_CU(ps::launch_eref_set(U + (long)(p->nc - 1) * p->cells, p->eref, s), "energy reference");
+  PS_CU(ps::launch_eref_set(U + (long)(p->nc - 1) * p->cells, p->ss(p->nc), p->nsolve, p->eref, s),
+        "energy reference");
   if ((rc = xfirst(p, U, nullptr, nullptr, s, true)) != PS_OK) return rc;
-  if (p->nd == 3 && (rc = ymid(p, s)) != PS_OK) return rc;
-  return last(p, -1, U, rhs, 0.0, nullptr, false, s);
+  if (p->nd == 3 && (rc = ymid(p, s, nullptr)) != PS_OK) return rc;
+  return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
 }
 
 int ps_step_rk4(ps_plan p, float* U, double dt, const double* d_dt, void* stream) {
@@ -610,8 +690,17 @@ int ps_run_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt,
   if (nsteps < 0) return fail(PS_ERR_INVALID, "nsteps must be >= 0");
   if (nsteps == 0) return PS_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  if (p->nd == 1) return step_1d(p, U, nsteps, dt, d_dt, s);
-  return steps_nd(p, U, nsteps, dt, d_dt, s);
+  if (p->nd == 1) return step_1d(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
+  return steps_nd(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
+}
+
+int ps_run_cfl(ps_plan p, float* U, int nsteps, double* d_t, const double* d_tend, void* stream) {
+  if (!p || !U || !d_t || !d_tend) return fail(PS_ERR_INVALID, "null argument");
+  if (nsteps < 0) return fail(PS_ERR_INVALID, "nsteps must be >= 0");
+  if (nsteps == 0) return PS_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->nd == 1) return step_1d(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
+  return steps_nd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
 }
 
 int ps_derivative(ps_plan p, int axis, const float* f, float* out, int nf, void* stream) {
@@ -643,13 +732,17 @@ int ps_filter(ps_plan p, const float* f, float* out, int nf, void* stream) {
 
 int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
   if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
-  PS_CU(ps::launch_speed(p->nd, U, p->cells, (float)p->desc.gamma, d_out, (cudaStream_t)stream), "max wave speed");
+  PS_CU(ps::launch_speed(p->nd, U, p->cells, p->ss(p->nc), p->nsolve, (float)p->desc.gamma, d_out,
+                         (cudaStream_t)stream),
+        "max wave speed");
   return PS_OK;
 }
 
 int ps_conserved(ps_plan p, const float* U, double* d_out, void* stream) {
   if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
-  PS_CU(ps::launch_conserved(p->nd, U, p->cells, p->desc.gamma, d_out, (cudaStream_t)stream), "conserved sums");
+  PS_CU(ps::launch_conserved(p->nd, U, p->cells, p->ss(p->nc), p->nsolve, p->desc.gamma, d_out,
+                             (cudaStream_t)stream),
+        "conserved sums");
   return PS_OK;
 }
 

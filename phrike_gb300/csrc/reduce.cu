@@ -10,8 +10,10 @@ namespace ps {
 // Max wave speed with the reference's per-dimension rule
 // (equations.py:89-98 1D |u|+a, 137-147 2D |u_x|+a, 199-211 3D max|u_i|+a).
 template <int ND>
-__global__ void k_speed(const float* __restrict__ U, long cells, float gamma, float* out) {
+__global__ void k_speed(const float* __restrict__ U, long cells, long ss, float gamma, float* out) {
   __shared__ float red[32];
+  U += (long)blockIdx.y * ss;
+  out += blockIdx.y;
   float m = 0.0f;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
     const float rho = U[i];
@@ -33,9 +35,11 @@ __global__ void k_speed(const float* __restrict__ U, long cells, float gamma, fl
 // Plain sums of rho, rho u_i and p/(gamma-1) + rho|u|^2/2 from primitives, in
 // float64 (solver.py:372-377, 741-767, 1439-1468).
 template <int ND>
-__global__ void k_conserved(const float* __restrict__ U, long cells, double gamma, double* out) {
+__global__ void k_conserved(const float* __restrict__ U, long cells, long ss, double gamma, double* out) {
   constexpr int NC = ND + 2;
   __shared__ double red[NC][32];
+  U += (long)blockIdx.y * ss;
+  out += (long)blockIdx.y * NC;
   double s[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) s[c] = 0.0;
@@ -86,66 +90,108 @@ __global__ void k_flux1d(const float* __restrict__ U, long n, float gamma, float
   }
 }
 
-// dt = cfl * hmin / speed (1e-6 when speed <= 0), clipped to t_end - t
-// (solver.py:235-240, 386-389).
-__global__ void k_cfl_dt(const float* speed, double cfl, double hmin, const double* t, double t_end,
-                         double* dt) {
-  const double s = (double)(*speed);
-  double d = (s <= 0.0) ? 1e-6 : cfl * hmin / s;
-  if (t != nullptr) d = fmin(d, t_end - *t);
-  *dt = d;
+// E_ref of the energy-perturbation form: the energy of each solve's first cell.
+__global__ void k_eref_set(const float* E, long ss, int nsolve, float* eref) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsolve) eref[s] = E[(long)s * ss];
 }
 
-// E_ref of the energy-perturbation form: the energy of the first cell.
-__global__ void k_eref_set(const float* E, float* eref) { *eref = E[0]; }
-
-// E <- E + sign * E_ref (sign -1: to perturbation form, +1: back)
-__global__ void k_energy_shift(float* E, long n, const float* eref, float sign) {
-  const float s = sign * (*eref);
+// E <- E + sign * E_ref[solve] (sign -1: to perturbation form, +1: back)
+__global__ void k_energy_shift(float* E, long n, long ss, const float* eref, float sign) {
+  const float s = sign * eref[blockIdx.y];
+  E += (long)blockIdx.y * ss;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) E[i] += s;
 }
 
-cudaError_t launch_eref_set(const float* E, float* eref, cudaStream_t s) {
-  k_eref_set<<<1, 1, 0, s>>>(E, eref);
+// Per-solve CFL step control before a step (solver.py:386-389, 235-240):
+// active = t < t_end - 1e-12; dt = active ? min(cfl h / speed, t_end - t) : 0.
+__global__ void k_step_control(const float* speed, double cfl, double hmin, const double* t, const double* tend,
+                               int nsolve, double* dt, int* active) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsolve) return;
+  const bool on = t[s] < tend[s] - 1e-12;
+  const double sp = (double)speed[s];
+  double d = (sp <= 0.0) ? 1e-6 : cfl * hmin / sp;
+  d = fmin(d, tend[s] - t[s]);
+  dt[s] = on ? d : 0.0;
+  active[s] = on ? 1 : 0;
+}
+
+// After a step: t += dt; clear the speed maxima for the next step.
+__global__ void k_step_advance(double* t, const double* dt, float* speed, int nsolve) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsolve) return;
+  t[s] += dt[s];
+  speed[s] = 0.0f;
+}
+
+__global__ void k_fill_int(int* a, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+cudaError_t launch_fill_int(int* a, int n, int v, cudaStream_t s) {
+  k_fill_int<<<(n + 127) / 128, 128, 0, s>>>(a, n, v);
   return cudaGetLastError();
 }
 
-cudaError_t launch_energy_shift(float* E, long n, const float* eref, float sign, cudaStream_t s) {
+cudaError_t launch_eref_set(const float* E, long ss, int nsolve, float* eref, cudaStream_t s) {
+  k_eref_set<<<(nsolve + 127) / 128, 128, 0, s>>>(E, ss, nsolve, eref);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy_shift(float* E, long n, long ss, int nsolve, const float* eref, float sign,
+                                cudaStream_t s) {
   const long want = (n + 255) / 256;
-  const int blocks = (int)(want < 4096 ? want : 4096);
-  k_energy_shift<<<blocks, 256, 0, s>>>(E, n, eref, sign);
+  const int blocks = (int)(want < 1024 ? want : 1024);
+  k_energy_shift<<<dim3(blocks, nsolve), 256, 0, s>>>(E, n, ss, eref, sign);
   return cudaGetLastError();
 }
 
-cudaError_t launch_speed(int nd, const float* U, long cells, float gamma, float* out, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float), s);
+cudaError_t launch_step_control(const float* speed, double cfl, double hmin, const double* t, const double* tend,
+                                int nsolve, double* dt, int* active, cudaStream_t s) {
+  k_step_control<<<(nsolve + 127) / 128, 128, 0, s>>>(speed, cfl, hmin, t, tend, nsolve, dt, active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_advance(double* t, const double* dt, float* speed, int nsolve, cudaStream_t s) {
+  k_step_advance<<<(nsolve + 127) / 128, 128, 0, s>>>(t, dt, speed, nsolve);
+  return cudaGetLastError();
+}
+
+static int reduce_blocks(long cells, int nsolve) {
+  const long per = (1184 + nsolve - 1) / nsolve;  // about 1184 blocks in total
+  const long want = (cells + 255) / 256;
+  return (int)(want < per ? want : (per > 0 ? per : 1));
+}
+
+cudaError_t launch_speed(int nd, const float* U, long cells, long ss, int nsolve, float gamma, float* out,
+                         cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * nsolve, s);
   if (e != cudaSuccess) return e;
-  const int blocks = (int)((cells + 255) / 256 < 1184 ? (cells + 255) / 256 : 1184);
-  if (nd == 1) k_speed<1><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
-  else if (nd == 2) k_speed<2><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
-  else k_speed<3><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
+  const dim3 grid(reduce_blocks(cells, nsolve), nsolve);
+  if (nd == 1) k_speed<1><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
+  else if (nd == 2) k_speed<2><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
+  else k_speed<3><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_conserved(int nd, const float* U, long cells, double gamma, double* out, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * (nd + 2), s);
+cudaError_t launch_conserved(int nd, const float* U, long cells, long ss, int nsolve, double gamma, double* out,
+                             cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * (nd + 2) * nsolve, s);
   if (e != cudaSuccess) return e;
-  const int blocks = (int)((cells + 255) / 256 < 1184 ? (cells + 255) / 256 : 1184);
-  if (nd == 1) k_conserved<1><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
-  else if (nd == 2) k_conserved<2><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
-  else k_conserved<3><<<blocks, 256, 0, s>>>(U, cells, gamma, out);
+  const dim3 grid(reduce_blocks(cells, nsolve), nsolve);
+  if (nd == 1) k_conserved<1><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
+  else if (nd == 2) k_conserved<2><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
+  else k_conserved<3><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_flux1d(const float* U, long n, float gamma, float* F, cudaStream_t s) {
+cudaError_t launch_flux1d(const float* U, long n, long ss, int nsolve, float gamma, float* F, cudaStream_t s) {
   const int blocks = (int)((n + 255) / 256);
-  k_flux1d<<<blocks, 256, 0, s>>>(U, n, gamma, F);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_cfl_dt(const float* speed, double cfl, double hmin, const double* t, double t_end, double* dt,
-                          cudaStream_t s) {
-  k_cfl_dt<<<1, 1, 0, s>>>(speed, cfl, hmin, t, t_end, dt);
+  for (int q = 0; q < nsolve; ++q) {
+    k_flux1d<<<blocks, 256, 0, s>>>(U + (long)q * ss, n, gamma, F + (long)q * 3 * n);
+  }
   return cudaGetLastError();
 }
 

@@ -148,7 +148,7 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   float* G = base + kGOffset;
   float* AB = base + kABOffset;
   const int nx = desc->n[0], ny = desc->n[1], nz = (nd == 3) ? desc->n[2] : 1;
-  if ((e = ps::launch_eref_set(U + (long)(nc - 1) * cells, eref, s)) != cudaSuccess)
+  if ((e = ps::launch_eref_set(U + (long)(nc - 1) * cells, (long)nc * cells, 1, eref, s)) != cudaSuccess)
     return fail_cuda(e, "energy reference");
 
   ps::XFirstArgs xa{};
@@ -156,7 +156,11 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   xa.Uw = nullptr;
   xa.out = G;
   xa.fs = cells;
+  xa.ssU = (long)nc * cells;
+  xa.ssOut = (long)nd * nc * cells;
   xa.rows = (int)(cells / nx);
+  xa.rps = xa.rows;
+  xa.active = nullptr;
   xa.ax = ax[0];
   xa.gamma = (float)desc->gamma;
   xa.speed = nullptr;
@@ -177,6 +181,8 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
     ps::YMidTArgs ya{};
     ya.out = AB;
     ya.fs = cells;
+    ya.ssOut = 10 * cells;
+    ya.active = nullptr;
     ya.g = gy;
     ya.ax = ax[1];
     ya.status = nullptr;
@@ -197,9 +203,12 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
     la.axis = 1;
     la.ax = ax[1];
   }
+  la.nfAB = (nd == 3) ? 10 : 2 * nc;
   la.acc = nullptr;
   la.out = rhs;
   la.fs = cells;
+  la.ssAcc = la.ssOut = la.ssUn = (long)nc * cells;
+  la.active = nullptr;
   la.stage = -1;
   la.Un = U;
   la.dt_dev = nullptr;

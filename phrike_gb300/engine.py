@@ -23,16 +23,18 @@ def _ptr(t: torch.Tensor) -> C.c_void_p:
 
 
 class Plan:
-    """One Fourier pseudo-spectral Euler solve (1-3 dimensions).
+    """A batch of ``nsolve`` Fourier pseudo-spectral Euler solves of one grid
+    (1-3 dimensions); ``nsolve=1`` is a single solve.
 
     ``shape`` is the spatial shape in array order ((N,), (Ny, Nx) or
-    (Nz, Ny, Nx)); ``lengths`` follows the same order.
+    (Nz, Ny, Nx)); ``lengths`` follows the same order.  State tensors have
+    shape (ncomp, *shape) for one solve and (nsolve, ncomp, *shape) for a batch.
     """
 
     def __init__(self, shape: Sequence[int], lengths: Sequence[float], gamma: float = 1.4,
                  dealias: bool = True, filter_params: Optional[Dict] = None,
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
-                 device: Optional[torch.device] = None):
+                 device: Optional[torch.device] = None, nsolve: int = 1):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -60,9 +62,10 @@ class Plan:
             for a, g in enumerate(gravity):
                 desc.gravity[a] = float(g)
         self.desc = desc
+        self.nsolve = int(nsolve)
         self._handle = C.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(lib.ps_plan_create(C.byref(desc), C.byref(self._handle)))
+            _lib.check(lib.ps_batch_create(C.byref(desc), self.nsolve, C.byref(self._handle)))
         self._lib = lib
 
     # -- lifetime ---------------------------------------------------------
@@ -87,8 +90,8 @@ class Plan:
             raise RuntimeError(f"expected float32 fields, got {U.dtype}")
         if not U.is_contiguous():
             raise RuntimeError("fields must be C-contiguous")
-        if tuple(U.shape[-self.ndim:]) != self.shape or U.numel() != nf * self.cells:
-            raise RuntimeError(f"expected shape ({nf}, {self.shape}), got {tuple(U.shape)}")
+        if tuple(U.shape[-self.ndim:]) != self.shape or U.numel() != nf * self.cells * self.nsolve:
+            raise RuntimeError(f"expected {self.nsolve} solve(s) x {nf} fields of {self.shape}, got {tuple(U.shape)}")
 
     @property
     def cells(self) -> int:
@@ -99,7 +102,7 @@ class Plan:
 
     def scratch_bytes(self) -> int:
         b = C.c_size_t()
-        _lib.check(self._lib.ps_plan_scratch_bytes(C.byref(self.desc), C.byref(b)))
+        _lib.check(self._lib.ps_batch_scratch_bytes(C.byref(self.desc), self.nsolve, C.byref(b)))
         return int(b.value)
 
     # -- operations -------------------------------------------------------
@@ -110,7 +113,7 @@ class Plan:
         return out
 
     def step_(self, U: torch.Tensor, dt: float = 0.0, dt_dev: Optional[torch.Tensor] = None) -> torch.Tensor:
-        """One RK4 step in place (dt from ``dt_dev`` if given: a float64 device scalar)."""
+        """One RK4 step in place (dt from ``dt_dev`` if given: float64 device array, one per solve)."""
         self._check_state(U)
         dptr = _ptr(dt_dev) if dt_dev is not None else None
         _lib.check(self._lib.ps_step_rk4(self._handle, _ptr(U), float(dt), dptr, _stream(self.device)))
@@ -124,9 +127,21 @@ class Plan:
                                           _stream(self.device)))
         return U
 
+    def run_cfl_(self, U: torch.Tensor, nsteps: int, t: torch.Tensor, t_end: torch.Tensor) -> torch.Tensor:
+        """Up to nsteps CFL steps with the time loop on the device; ``t`` and
+        ``t_end`` are float64 device tensors of nsolve entries (``t`` advances
+        in place, a solve stops at its t_end)."""
+        self._check_state(U)
+        for x in (t, t_end):
+            if x.dtype != torch.float64 or x.device != self.device or x.numel() != self.nsolve:
+                raise RuntimeError("t and t_end must be float64 device tensors with one entry per solve")
+        _lib.check(self._lib.ps_run_cfl(self._handle, _ptr(U), int(nsteps), _ptr(t), _ptr(t_end),
+                                        _stream(self.device)))
+        return U
+
     def derivative(self, f: torch.Tensor, axis: int, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """axis 0 = x (last array axis)."""
-        nf = f.numel() // self.cells
+        nf = f.numel() // (self.cells * self.nsolve)
         self._check_state(f, nf)
         out = torch.empty_like(f) if out is None else out
         _lib.check(self._lib.ps_derivative(self._handle, int(axis), _ptr(f), _ptr(out), nf,
@@ -134,7 +149,7 @@ class Plan:
         return out
 
     def filter(self, f: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
-        nf = f.numel() // self.cells
+        nf = f.numel() // (self.cells * self.nsolve)
         self._check_state(f, nf)
         out = torch.empty_like(f) if out is None else out
         _lib.check(self._lib.ps_filter(self._handle, _ptr(f), _ptr(out), nf, _stream(self.device)))
@@ -142,13 +157,15 @@ class Plan:
 
     def max_wave_speed(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)
-        out = torch.empty(1, dtype=torch.float32, device=self.device) if out is None else out
+        out = torch.empty(self.nsolve, dtype=torch.float32, device=self.device) if out is None else out
         _lib.check(self._lib.ps_max_wave_speed(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
         return out
 
     def conserved(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)
-        out = torch.empty(self.ncomp, dtype=torch.float64, device=self.device) if out is None else out
+        if out is None:
+            shape = (self.ncomp,) if self.nsolve == 1 else (self.nsolve, self.ncomp)
+            out = torch.empty(shape, dtype=torch.float64, device=self.device)
         _lib.check(self._lib.ps_conserved(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
         return out
 
