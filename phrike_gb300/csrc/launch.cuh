@@ -86,7 +86,7 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   template <>                                                                                         \
   cudaError_t launch_ymid3_t<NN>(const CUtensorMap& mG, const YMidTArgs& a, cudaStream_t s) {         \
     constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
     const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_ymid3_t<NN, T, R>, sm)) != cudaSuccess) return e;                             \
@@ -97,7 +97,7 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   cudaError_t launch_last_t<NN>(int nd, const CUtensorMap& mAB, const CUtensorMap& mU,                \
                                 const CUtensorMap& mAcc, const LastTArgs& a, cudaStream_t s) {        \
     constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
     const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
     cudaError_t e;                                                                                    \
     if (nd == 3) {                                                                                    \
@@ -112,7 +112,7 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   template <>                                                                                         \
   cudaError_t launch_op_t<NN>(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {             \
     constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter);                                              \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
     const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_op_t<NN, T, R>, sm)) != cudaSuccess) return e;                                \

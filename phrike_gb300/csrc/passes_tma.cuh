@@ -157,6 +157,7 @@ struct YMidTArgs {
   float* out;      // 10 fields per solve [A(5), B(5)]
   long fs;
   long ssOut;      // solve stride of out (10 * cells)
+  int nsolve;
   StridedGeom g;   // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   AxisOps ax;
   const int* active;
@@ -251,6 +252,7 @@ struct LastTArgs {
   long fs;
   long ssAcc, ssOut, ssUn;  // solve strides of acc, out and Un
   const int* active;   // per-solve flags (null: all active)
+  int nsolve;
   StridedGeom g;       // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   int axis;            // 1: y pencils, 2: z pencils
   AxisOps ax;
@@ -483,6 +485,7 @@ struct OpTArgs {
   long fs;
   long ss;         // solve stride of out
   const int* active;
+  int nsolve;
   StridedGeom g;   // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   int axis;
   AxisOps ax;

@@ -303,6 +303,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
     a.fs = p->cells;
     a.ss = p->ss(nf);
     a.active = active;
+    a.nsolve = p->nsolve;
     a.g = (axis == 1) ? geom_y(p) : geom_z(p);
     a.axis = axis;
     a.ax = p->ax(axis);
@@ -347,6 +348,7 @@ int ymid(ps_plan p, cudaStream_t s, const int* active) {
   a.out = p->AB;
   a.fs = p->cells;
   a.ssOut = p->ss(10);
+  a.nsolve = p->nsolve;
   a.g = geom_y(p);
   a.ax = p->ax(1);
   a.active = active;
@@ -390,6 +392,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   a.ssOut = p->ss(nc);
   a.ssUn = p->ss(nc);
   a.active = active;
+  a.nsolve = p->nsolve;
   a.stage = stage;
   a.Un = Un;
   a.dt_dev = d_dt;

@@ -183,6 +183,7 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
     ya.fs = cells;
     ya.ssOut = 10 * cells;
     ya.active = nullptr;
+    ya.nsolve = 1;
     ya.g = gy;
     ya.ax = ax[1];
     ya.status = nullptr;
@@ -209,6 +210,7 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   la.fs = cells;
   la.ssAcc = la.ssOut = la.ssUn = (long)nc * cells;
   la.active = nullptr;
+  la.nsolve = 1;
   la.stage = -1;
   la.Un = U;
   la.dt_dev = nullptr;
