@@ -46,19 +46,29 @@ struct Ring {
 // Which axis the pencils run along (1 = y, 2 = z), and where the tile sits.
 struct TileIssue {
   int axis;
-  int x0;        // first column of the tile
-  int outer;     // z (axis 1) or y (axis 2)
-  int fbase[3];  // per map: field coordinate of this solve's first field (solve * fields per solve)
+  int x0;     // first column of the tile
+  int outer;  // z (axis 1) or y (axis 2)
+  // per map: field coordinate of this solve's first field (solve * fields per
+  // solve); separate members, not an array, so they stay in registers
+  int fb0, fb1, fb2;
+};
+
+// The (up to three) tensor maps a pass reads, as separate members so that no
+// runtime-indexed array lands in local memory.
+struct MapSet {
+  const CUtensorMap* m0;
+  const CUtensorMap* m1;
+  const CUtensorMap* m2;
 };
 
 template <int N, int T, int R>
-__device__ __forceinline__ void ring_issue(Ring<N, T, R>& rg, int i, const CUtensorMap* const* maps,
-                                           const TileIssue& ti) {
+__device__ __forceinline__ void ring_issue(Ring<N, T, R>& rg, int i, const MapSet& maps, const TileIssue& ti) {
   using G = TileGeom<N, T>;
   const int s = i % R;
   const int code = rg.sched[i];
-  const CUtensorMap* m = maps[code >> 8];
-  const int f = ti.fbase[code >> 8] + (code & 255);
+  const int mi = code >> 8;
+  const CUtensorMap* m = (mi == 0) ? maps.m0 : (mi == 1) ? maps.m1 : maps.m2;
+  const int f = ((mi == 0) ? ti.fb0 : (mi == 1) ? ti.fb1 : ti.fb2) + (code & 255);
   mbar_arrive_expect_tx(&rg.bar[s], G::BYTES);
 #pragma unroll
   for (int b = 0; b < G::NBOX; ++b) {
@@ -72,7 +82,7 @@ __device__ __forceinline__ void ring_issue(Ring<N, T, R>& rg, int i, const CUten
 template <int N, int T, int R>
 struct RingCursor {
   Ring<N, T, R>& rg;
-  const CUtensorMap* const* maps;
+  MapSet maps;
   TileIssue ti;
   int* status;
   int issued;  // thread 0: tiles issued so far
@@ -186,8 +196,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   }
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
-  const CUtensorMap* maps[1] = {&mG};
-  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{1, (int)(blockIdx.x * T), outer, {sol * 15, 0, 0}}, a.status, 0};
+  const MapSet maps{&mG, &mG, &mG};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{1, (int)(blockIdx.x * T), outer, sol * 15, 0, 0}, a.status, 0};
   rc.start();
   const long base = (long)sol * a.ssOut + (long)outer * a.g.os + col + (long)t * a.g.as;
   const long step = (long)A * a.g.as;
@@ -301,9 +311,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   }
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
-  const CUtensorMap* maps[3] = {&mAB, &mU, &mAcc};
+  const MapSet maps{&mAB, &mU, &mAcc};
   RingCursor<N, T, R> rc{S.ring, maps,
-                         TileIssue{a.axis, (int)(blockIdx.x * T), outer, {sol * a.nfAB, sol * NC, sol * NC}},
+                         TileIssue{a.axis, (int)(blockIdx.x * T), outer, sol * a.nfAB, sol * NC, sol * NC},
                          a.status, 0};
   rc.start();
   const long base = (long)outer * a.g.os + col + (long)t * a.g.as;  // within a solve
@@ -516,8 +526,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   }
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
-  const CUtensorMap* maps[1] = {&mIn};
-  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer, {sol * a.nf, 0, 0}},
+  const MapSet maps{&mIn, &mIn, &mIn};
+  RingCursor<N, T, R> rc{S.ring, maps, TileIssue{a.axis, (int)(blockIdx.x * T), outer, sol * a.nf, 0, 0},
                          a.status, 0};
   rc.start();
   const long base = (long)sol * a.ss + (long)outer * a.g.os + col + (long)t * a.g.as;
