@@ -283,8 +283,92 @@ def run_gb300(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def khi_ensemble_specs(nsolve: int, seed: int = 20261203, t_end: float = 1.0):
+    """The batching workload: KHI solves on [0,1)^2 with N uniform on
+    {64,128,256,512}, U0 ~ U[0.5,1.5], A ~ U[0.005,0.02], seeded."""
+    from phrike_gb300 import problems
+    from phrike_gb300.ensemble import SolveSpec
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(nsolve):
+        n = int(rng.choice([64, 128, 256, 512]))
+        u0 = float(rng.uniform(0.5, 1.5))
+        amp = float(rng.uniform(0.005, 0.02))
+        specs.append(SolveSpec((n, n), (1.0, 1.0), problems.kelvin_helmholtz_2d(n, n, U0=u0, A=amp), t_end))
+    return specs
+
+
+def run_ensemble(args):
+    """Ensemble solves/s: every solve to t_end in one batched, graph-captured
+    run, against the same solves run one at a time (a per-size sample,
+    extrapolated by the size counts)."""
+    import torch
+    from phrike_gb300 import _build
+    from phrike_gb300.engine import Plan
+    from phrike_gb300.ensemble import Ensemble
+    from phrike_gb300.equations import EulerEquations2D
+    from phrike_gb300.grid import Grid2D
+    from phrike_gb300.solver import SpectralSolver2D
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    specs = khi_ensemble_specs(args.nsolve, t_end=args.t_end)
+    ens = Ensemble(specs, cfl=0.4, device=device)
+    sampler = ClockSampler(0)
+    sampler.start()
+    stats = ens.run(chunk=args.chunk, use_graphs=True)
+    clocks = sampler.stop()
+    # plain: one solve at a time, (a) device time loop, (b) host CFL loop as the reference's run()
+    counts = {}
+    for sp in specs:
+        counts[sp.shape[0]] = counts.get(sp.shape[0], 0) + 1
+    plain_dev, plain_host = 0.0, 0.0
+    sample = {}
+    for n, cnt in sorted(counts.items()):
+        sp = next(x for x in specs if x.shape[0] == n)
+        plan = Plan(sp.shape, sp.lengths, cfl=0.4, device=device)
+        U = torch.as_tensor(sp.U0, dtype=torch.float32, device=device).contiguous()
+        t = torch.zeros(1, dtype=torch.float64, device=device)
+        te = torch.tensor([sp.t_end], dtype=torch.float64, device=device)
+        plan.run_cfl_(U.clone(), 1, t.clone(), te)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan.run_cfl_(U, 1 << 30, t, te)
+        torch.cuda.synchronize()
+        td = time.perf_counter() - t0
+        grid = Grid2D(Nx=n, Ny=n, Lx=1.0, Ly=1.0, backend="gb300")
+        solver = SpectralSolver2D(grid, EulerEquations2D(gamma=1.4), cfl=0.4)
+        solver.run(sp.U0, 0.0, min(sp.t_end, 1e-3), output_interval=1e9)  # warm-up
+        t0 = time.perf_counter()
+        solver.run(sp.U0, 0.0, sp.t_end, output_interval=1e9)
+        torch.cuda.synchronize()
+        th = time.perf_counter() - t0
+        plain_dev += cnt * td
+        plain_host += cnt * th
+        sample[str(n)] = {"solves": cnt, "device_loop_s": td, "host_loop_s": th}
+    line = {
+        "metric": "ensemble solves/s (batched vs plain, same GPU)", "value": stats["solves_per_s"],
+        "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (seeded KHI initial conditions)",
+        "config": {"workload": f"{args.nsolve} KHI 2D solves, N uniform on 64..512, CFL 0.4, t_end={args.t_end}",
+                   "chunk_steps_per_graph": args.chunk},
+        "seconds": stats["seconds"], "cell_updates_per_s": stats["cell_updates_per_s"],
+        "status": stats["status"],
+        "plain_device_loop_solves_per_s": args.nsolve / plain_dev,
+        "plain_host_loop_solves_per_s": args.nsolve / plain_host,
+        "speedup_vs_plain_device_loop": plain_dev / stats["seconds"],
+        "speedup_vs_plain_host_loop": plain_host / stats["seconds"],
+        "plain_sample": sample, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", choices=["tgv", "ensemble"], default="tgv")
+    ap.add_argument("--nsolve", type=int, default=512)
+    ap.add_argument("--t-end", type=float, default=1.0)
+    ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
@@ -302,7 +386,10 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group(backend=backend)
     try:
-        if args.impl == "reference":
+        if args.workload == "ensemble":
+            if rank == 0:
+                run_ensemble(args)
+        elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
             run_gb300(args, rank, world)

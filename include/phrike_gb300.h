@@ -80,6 +80,9 @@ int ps_plan_destroy(ps_plan plan);
  * SpectralSolver*.run calls (solver.py:338-422 per solve). */
 int ps_batch_create(const ps_plan_desc* desc, int nsolve, ps_plan* out);
 int ps_plan_nsolve(ps_plan plan);
+/* Steps taken by each solve in ps_run_cfl calls so far (host array of
+ * nsolve ints, read synchronously). */
+int ps_plan_steps_done(ps_plan plan, int* host_steps);
 
 /* rhs = -(sum_a d/dx_a F_a(U)) for U (ncomp fields).  Replaces
  * _compute_rhs / _compute_rhs_2d / _compute_rhs_3d (solver.py:62-93,

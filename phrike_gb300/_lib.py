@@ -48,6 +48,7 @@ _SIGNATURES = [
     ("ps_batch_create", C.c_int, [C.POINTER(PlanDesc), C.c_int, C.POINTER(C.c_void_p)]),
     ("ps_batch_scratch_bytes", C.c_int, [C.POINTER(PlanDesc), C.c_int, C.POINTER(C.c_size_t)]),
     ("ps_plan_nsolve", C.c_int, [C.c_void_p]),
+    ("ps_plan_steps_done", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("ps_run_cfl", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_rhs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_step_rk4", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),

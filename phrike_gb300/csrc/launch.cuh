@@ -3,6 +3,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <unordered_set>
+
 #include "euler1d.cuh"
 #include "euler_passes.cuh"
 #include "passes_tma.cuh"
@@ -46,12 +49,20 @@ cudaError_t dispatch_n(int n, F&& f) {
 
 // Dynamic shared memory above 48 KB needs an opt-in; every pass kernel also
 // asks for the largest shared-memory carveout so that several CTAs fit per SM.
+// Attributes are set once per kernel (the first launch, which must not be
+// inside a stream capture); later launches, captured or not, skip the calls.
 template <typename K>
 inline cudaError_t set_smem(K kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_set<const void*> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(reinterpret_cast<const void*>(kernel))) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                        (int)cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess || bytes <= 48 * 1024) return e;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess && bytes > 48 * 1024)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done.insert(reinterpret_cast<const void*>(kernel));
+  return e;
 }
 
 #define PS_DEFINE_LAUNCHERS(NN)                                                                       \

@@ -487,7 +487,8 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
       if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s, true, act)) != PS_OK) return rc;
       pending_px = true;
     }
-    if (cfl) PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->nsolve, s), "step advance");
+    if (cfl)
+      PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->active, p->steps_done, p->nsolve, s), "step advance");
     p->step_counter += 1;
   }
   if (pending_px) {
@@ -630,6 +631,12 @@ int ps_plan_destroy(ps_plan p) {
 int ps_plan_ncomp(ps_plan p) { return p ? p->nc : -1; }
 
 int ps_plan_nsolve(ps_plan p) { return p ? p->nsolve : -1; }
+
+int ps_plan_steps_done(ps_plan p, int* host_steps) {
+  if (!p || !host_steps) return fail(PS_ERR_INVALID, "null argument");
+  PS_CU(cudaMemcpy(host_steps, p->steps_done, sizeof(int) * p->nsolve, cudaMemcpyDeviceToHost), "steps read");
+  return PS_OK;
+}
 
 int ps_plan_status(ps_plan p, int* status) {
   if (!p || !status) return fail(PS_ERR_INVALID, "null argument");

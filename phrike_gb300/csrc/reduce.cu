@@ -117,11 +117,14 @@ __global__ void k_step_control(const float* speed, double cfl, double hmin, cons
   active[s] = on ? 1 : 0;
 }
 
-// After a step: t += dt; clear the speed maxima for the next step.
-__global__ void k_step_advance(double* t, const double* dt, float* speed, int nsolve) {
+// After a step: t += dt, count the step of every solve that advanced, clear
+// the speed maxima for the next step.
+__global__ void k_step_advance(double* t, const double* dt, float* speed, const int* active, int* steps,
+                               int nsolve) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsolve) return;
   t[s] += dt[s];
+  if (active[s]) steps[s] += 1;
   speed[s] = 0.0f;
 }
 
@@ -154,8 +157,9 @@ cudaError_t launch_step_control(const float* speed, double cfl, double hmin, con
   return cudaGetLastError();
 }
 
-cudaError_t launch_step_advance(double* t, const double* dt, float* speed, int nsolve, cudaStream_t s) {
-  k_step_advance<<<(nsolve + 127) / 128, 128, 0, s>>>(t, dt, speed, nsolve);
+cudaError_t launch_step_advance(double* t, const double* dt, float* speed, const int* active, int* steps,
+                                int nsolve, cudaStream_t s) {
+  k_step_advance<<<(nsolve + 127) / 128, 128, 0, s>>>(t, dt, speed, active, steps, nsolve);
   return cudaGetLastError();
 }
 

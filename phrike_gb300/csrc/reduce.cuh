@@ -10,7 +10,8 @@ cudaError_t launch_energy_shift(float* E, long n, long ss, int nsolve, const flo
                                 cudaStream_t s);
 cudaError_t launch_step_control(const float* speed, double cfl, double hmin, const double* t, const double* tend,
                                 int nsolve, double* dt, int* active, cudaStream_t s);
-cudaError_t launch_step_advance(double* t, const double* dt, float* speed, int nsolve, cudaStream_t s);
+cudaError_t launch_step_advance(double* t, const double* dt, float* speed, const int* active, int* steps,
+                                int nsolve, cudaStream_t s);
 cudaError_t launch_speed(int nd, const float* U, long cells, long ss, int nsolve, float gamma, float* out,
                          cudaStream_t s);
 cudaError_t launch_conserved(int nd, const float* U, long cells, long ss, int nsolve, double gamma, double* out,

@@ -169,6 +169,12 @@ class Plan:
         _lib.check(self._lib.ps_conserved(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
         return out
 
+    def steps_done(self):
+        """Steps taken per solve by run_cfl_ calls (list of nsolve ints)."""
+        arr = (C.c_int * self.nsolve)()
+        _lib.check(self._lib.ps_plan_steps_done(self._handle, arr))
+        return list(arr)
+
     def status(self) -> int:
         """Device status word (0 = healthy; 1 = a kernel's bounded TMA wait ran out)."""
         v = C.c_int()

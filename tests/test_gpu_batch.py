@@ -97,3 +97,25 @@ def test_solve_alone_vs_in_the_mix_2d(cuda_device):
         t1 = torch.zeros(1, dtype=torch.float64, device=cuda_device)
         one.run_cfl_(U1, 500, t1, torch.as_tensor(tend[s:s + 1], device=cuda_device))
         assert rel_l2(mix[s], U1.double().cpu().numpy()) < 1e-6
+
+
+def test_ensemble_uneven_sizes_graphs(cuda_device):
+    """Ensemble of KHI solves on two grids advanced with captured CUDA graphs:
+    every solve reaches its own end time and equals the solve run alone."""
+    from phrike_gb300.ensemble import Ensemble, SolveSpec
+    rng = np.random.default_rng(3)
+    specs = []
+    for n in (32, 64, 32, 64, 32):
+        specs.append(SolveSpec((n, n), (1.0, 1.0),
+                               problems.kelvin_helmholtz_2d(n, n, U0=0.5 + rng.random(), A=0.01),
+                               t_end=0.004 + 0.006 * rng.random()))
+    ens = Ensemble(specs, cfl=0.4, device=cuda_device)
+    stats = ens.run(chunk=7, use_graphs=True)
+    assert stats["status"] == 0
+    for i, sp in enumerate(specs):
+        assert abs(ens.time(i) - sp.t_end) < 1e-12
+        alone = Plan(sp.shape, sp.lengths, cfl=0.4, device=cuda_device)
+        U1 = dev(sp.U0, cuda_device)
+        t1 = torch.zeros(1, dtype=torch.float64, device=cuda_device)
+        alone.run_cfl_(U1, 10000, t1, torch.tensor([sp.t_end], dtype=torch.float64, device=cuda_device))
+        assert rel_l2(ens.state(i).double().cpu().numpy(), U1.double().cpu().numpy()) < 1e-6
