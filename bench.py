@@ -333,7 +333,10 @@ def run_ensemble(args):
         plan.run_cfl_(U.clone(), 1, t.clone(), te)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        plan.run_cfl_(U, 1 << 30, t, te)
+        # the 2D/3D step loop is driven from the host: advance in chunks and
+        # stop once the device-side time has reached t_end
+        while float(t.item()) < sp.t_end - 1e-12:
+            plan.run_cfl_(U, args.chunk, t, te)
         torch.cuda.synchronize()
         td = time.perf_counter() - t0
         grid = Grid2D(Nx=n, Ny=n, Lx=1.0, Ly=1.0, backend="gb300")

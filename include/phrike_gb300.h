@@ -105,7 +105,10 @@ int ps_run_steps(ps_plan plan, float* U, int nsteps, double dt, const double* d_
  * solve, dt = min(cfl * h_min / max wave speed, t_end - t) from the state at
  * the start of each step, t advances in d_t (nsolve doubles, updated in
  * place), and a solve stops once t >= t_end - 1e-12.  No host
- * synchronisation, so the call can be captured in a CUDA graph.  Replaces the
+ * synchronisation, so the call can be captured in a CUDA graph.  For 2D/3D
+ * grids the step loop is issued from the host, so nsteps is also the number
+ * of steps launched (finished solves skip their work but the launches still
+ * happen): advance in chunks and read d_t between chunks.  Replaces the
  * while-loop of SpectralSolver*.run (solver.py:384-417, 773-800, 1480-1505). */
 int ps_run_cfl(ps_plan plan, float* U, int nsteps, double* d_t, const double* d_tend, void* stream);
 
