@@ -144,8 +144,9 @@ template <> struct Shape<32> { static constexpr int A = 4, B = 8; };
 template <> struct Shape<64> { static constexpr int A = 8, B = 8; };
 template <> struct Shape<128> { static constexpr int A = 8, B = 16; };
 template <> struct Shape<256> { static constexpr int A = 16, B = 16; };
-template <> struct Shape<512> { static constexpr int A = 16, B = 32; };
-template <> struct Shape<1024> { static constexpr int A = 32, B = 32; };
+// N > 256: G = N/256 groups of 16 threads (see PencilGrp)
+template <> struct Shape<512> { static constexpr int A = 32, B = 16; };
+template <> struct Shape<1024> { static constexpr int A = 64, B = 16; };
 
 // Exchange-buffer layout for T pencils.  Element (q, s) of pencil p, with
 // q in [0,B) and s in [0,A).  In the contiguous-lane layout (the A threads of
@@ -153,7 +154,7 @@ template <> struct Shape<1024> { static constexpr int A = 32, B = 32; };
 // layout (lanes run over pencils) pencils are interleaved innermost.  Both are
 // bank-conflict free for the access patterns below.
 template <int N, int T, bool STRIDED>
-struct Pencil {
+struct PencilBase {
   static constexpr int A = Shape<N>::A;
   static constexpr int B = Shape<N>::B;
   static constexpr int J = B / A;
@@ -239,5 +240,110 @@ struct Pencil {
     });
   }
 };
+
+// Pencils of N = G * 256 points (G = 2 or 4).  Pencil thread t' = G*t + g
+// (t in [0,16), group g in [0,G)) holds positions t' + 16G*n2, i.e. point
+// t + 16*n2 of the decimated sub-pencil x_g[m] = x[G*m + g].  The forward
+// transform runs the 256-point PencilBase transform on every sub-pencil,
+// multiplies S_g[k] by W_N^{g k} and finishes with a G-point DFT across the
+// groups (radix-2 decimation in frequency over warp shuffles: every group of
+// a pencil lives in the same warp).  Group g then holds
+// X[k + 256 * bitrev(g)], k = t + 16 r.  The inverse runs the same steps in
+// reverse (decimation in time with conjugate twiddles).
+//
+// Tables (N entries each, shared layout): twf/twi[0..255] are the 256-point
+// sub-pencil twiddles, twf[256*g + k] = W_N^{g k} and twi[256*g + k] =
+// W_N^{-g k} for g = 1..G-1, k < 256.
+template <int N, int T, bool STRIDED>
+struct PencilGrp {
+  static constexpr int G = N / 256;
+  static constexpr int A = Shape<N>::A;  // 16 * G
+  static constexpr int B = Shape<N>::B;  // 16
+  static constexpr int LG = ilog2(G);
+  using Sub = PencilBase<256, T * G, STRIDED>;
+  static constexpr int BUF = Sub::BUF;
+  static_assert(!STRIDED || T * G <= 32, "all groups of a pencil must share a warp");
+
+  int p;   // pencil within the tile
+  int t;   // pencil thread t' = G * t_sub + g
+  float2* buf;
+  const float2* twf;
+  const float2* twi;
+
+  __device__ __forceinline__ int g() const { return t % G; }
+  __device__ __forceinline__ int ts() const { return t / G; }
+  __device__ __forceinline__ Sub sub() const { return Sub{p * G + g(), ts(), buf, twf, twi}; }
+  // lane distance between groups g and g ^ 1 of the same pencil thread
+  __device__ __forceinline__ int lane_step() const { return STRIDED ? T : 1; }
+  __device__ __forceinline__ int kidx(int r) const {
+    return ts() + 16 * r + 256 * bitrev(g(), LG);
+  }
+
+  __device__ __forceinline__ void fwd(float2 (&v)[B]) const {
+    sub().fwd(v);
+    const int gg = g(), t0 = ts();
+    if (gg > 0) {
+#pragma unroll
+      for (int r = 0; r < B; ++r) v[r] = cmul(v[r], twf[256 * gg + t0 + 16 * r]);
+    }
+    // G-point DFT across the groups, decimation in frequency
+#pragma unroll
+    for (int h = G / 2; h >= 1; h /= 2) {
+      const int lane_x = h * lane_step();
+      const bool upper = (gg & h) != 0;
+      const int j = gg % h;  // position inside the 2h block
+      float c = 1.0f, sn = 0.0f;
+      if (h > 1) {  // W_{2h}^{j}: only h = 2 (G = 4) needs a non-trivial factor
+        c = (j == 0) ? 1.0f : 0.0f;
+        sn = (j == 0) ? 0.0f : -1.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[r].x, lane_x),
+                                     __shfl_xor_sync(0xffffffffu, v[r].y, lane_x));
+        if (!upper) {
+          v[r] = cadd(v[r], o);
+        } else {
+          const float2 d = csub(o, v[r]);  // lower - upper
+          v[r] = make_float2(d.x * c - d.y * sn, d.x * sn + d.y * c);
+        }
+      }
+    }
+  }
+
+  __device__ __forceinline__ void inv(float2 (&v)[B]) const {
+    const int gg = g(), t0 = ts();
+    // G-point inverse DFT across the groups, decimation in time (bit-reversed in)
+#pragma unroll
+    for (int h = 1; h <= G / 2; h *= 2) {
+      const int lane_x = h * lane_step();
+      const bool upper = (gg & h) != 0;
+      const int j = gg % h;
+      float c = 1.0f, sn = 0.0f;
+      if (h > 1) {  // conj(W_{2h}^{j})
+        c = (j == 0) ? 1.0f : 0.0f;
+        sn = (j == 0) ? 0.0f : 1.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[r].x, lane_x),
+                                     __shfl_xor_sync(0xffffffffu, v[r].y, lane_x));
+        // lower holds x[i], upper holds x[i+h]; t = x[i+h] * w
+        const float2 up = upper ? v[r] : o;
+        const float2 lo = upper ? o : v[r];
+        const float2 tw = make_float2(up.x * c - up.y * sn, up.x * sn + up.y * c);
+        v[r] = upper ? csub(lo, tw) : cadd(lo, tw);
+      }
+    }
+    if (gg > 0) {
+#pragma unroll
+      for (int r = 0; r < B; ++r) v[r] = cmul(v[r], twi[256 * gg + t0 + 16 * r]);
+    }
+    sub().inv(v);
+  }
+};
+
+template <int N, int T, bool STRIDED>
+using Pencil = typename std::conditional<(N > 256), PencilGrp<N, T, STRIDED>, PencilBase<N, T, STRIDED>>::type;
 
 }  // namespace ps

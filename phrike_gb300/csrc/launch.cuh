@@ -18,7 +18,7 @@ template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cuda
 
 // TMA strided passes: columns per tile and ring depth per pencil length
 template <int N> struct TmaTile {
-  static constexpr int T = (N >= 1024) ? 8 : 16;
+  static constexpr int T = (N >= 1024) ? 8 : 16;  // T * (N / 256) <= 32 for grouped pencils
   static constexpr int R = 4;
 };
 template <int N> cudaError_t launch_ymid3_t(const CUtensorMap& mG, const YMidTArgs& a, cudaStream_t s);

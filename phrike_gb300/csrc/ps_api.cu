@@ -181,14 +181,22 @@ void build_axis(int N, double L, int dealias, int fon, int fp, double falpha, st
     const double kphys = 2.0 * M_PI * kk / L;
     d[k] = (k == N / 2) ? 0.0f : (float)(kphys * m / N);
   }
-  // threads per pencil, as ps::Shape<N>::A in fft_pencil.cuh
-  const int A = (N == 8) ? 2 : (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
-  const int B = N / A;
+  // pencil FFT twiddles (layouts of fft_pencil.cuh): N <= 256 two-step
+  // pencils with A threads x B points; N > 256 groups of 256-point pencils
+  const int base = (N > 256) ? 256 : N;
+  const int A = (base == 8) ? 2 : (base == 16 || base == 32) ? 4 : (base == 64 || base == 128) ? 8 : 16;
+  const int B = base / A;
   for (int k2 = 0; k2 < B; ++k2)
     for (int n1 = 0; n1 < A; ++n1) {
-      const double ang = -2.0 * M_PI * (double)((long)n1 * k2 % N) / N;
+      const double ang = -2.0 * M_PI * (double)((long)n1 * k2 % base) / base;
       twf[k2 * A + n1] = make_float2((float)cos(ang), (float)sin(ang));
       twi[n1 * B + k2] = make_float2((float)cos(ang), (float)-sin(ang));
+    }
+  for (int g = 1; g < N / 256; ++g)  // group twiddles W_N^{g k}, k < 256
+    for (int k = 0; k < 256; ++k) {
+      const double ang = -2.0 * M_PI * (double)((long)g * k % N) / N;
+      twf[256 * g + k] = make_float2((float)cos(ang), (float)sin(ang));
+      twi[256 * g + k] = make_float2((float)cos(ang), (float)-sin(ang));
     }
 }
 

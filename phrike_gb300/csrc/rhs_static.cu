@@ -64,13 +64,21 @@ int fail_cuda(cudaError_t e, const char* what) {
   return ps::record_error(PS_ERR_CUDA, msg);
 }
 
+__host__ __device__ inline int threads_per_pencil(int N) {  // two-step pencils, N <= 256
+  return (N == 8) ? 2 : (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : 16;
+}
+
 // Spectral tables of one axis, built on the device in float64 (same
 // definitions as the plan's host-built tables: 2/3 mask, exponential filter,
-// 1/N folded in, Nyquist derivative term zeroed, twiddles of the pencil FFT).
-__global__ void k_static_axis(int N, int A, double L, int dealias, int fon, int fp, double falpha, float* P,
-                              float* d, float2* twf, float2* twi) {
-  const int B = N / A;
+// 1/N folded in, Nyquist derivative term zeroed, twiddles of the pencil FFT:
+// the two-step layout for N <= 256; for N > 256 the 256-point sub-pencil
+// tables followed by the group twiddles W_N^{g j}).
+__global__ void k_static_axis(int N, double L, int dealias, int fon, int fp, double falpha, float* P, float* d,
+                              float2* twf, float2* twi) {
   const double kmax = N / 2;
+  const int base = (N > 256) ? 256 : N;
+  const int A = threads_per_pencil(base);
+  const int B = base / A;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
     const int kk = (k < N / 2) ? k : k - N;
     const double ak = fabs((double)kk);
@@ -78,17 +86,19 @@ __global__ void k_static_axis(int N, int A, double L, int dealias, int fon, int 
     if (fon) m *= exp(-falpha * pow(ak / (kmax > 1.0 ? kmax : 1.0), (double)fp));
     P[k] = (float)(m / N);
     d[k] = (k == N / 2) ? 0.0f : (float)((2.0 * kk / L) * 3.14159265358979323846 * m / N);
-    // twiddle entry k = k2*A + n1 of the forward table, n1*B + k2 of the inverse
-    const int k2 = k / A, n1 = k % A;
     double sn, cs;
-    sincospi(-2.0 * (double)((long)n1 * k2 % N) / N, &sn, &cs);
-    twf[k2 * A + n1] = make_float2((float)cs, (float)sn);
-    twi[n1 * B + k2] = make_float2((float)cs, (float)-sn);
+    if (k < base) {  // entry k = k2*A + n1 of the forward table, n1*B + k2 of the inverse
+      const int k2 = k / A, n1 = k % A;
+      sincospi(-2.0 * (double)((long)n1 * k2 % base) / base, &sn, &cs);
+      twf[k2 * A + n1] = make_float2((float)cs, (float)sn);
+      twi[n1 * B + k2] = make_float2((float)cs, (float)-sn);
+    } else {  // group twiddles, k = 256 g + j
+      const int g = k / 256, j = k % 256;
+      sincospi(-2.0 * (double)((long)g * j % N) / N, &sn, &cs);
+      twf[k] = make_float2((float)cs, (float)sn);
+      twi[k] = make_float2((float)cs, (float)-sn);
+    }
   }
-}
-
-int threads_per_pencil(int N) {
-  return (N == 8) ? 2 : (N == 16 || N == 32) ? 4 : (N == 64 || N == 128) ? 8 : (N == 256 || N == 512) ? 16 : 32;
 }
 
 }  // namespace
@@ -138,7 +148,7 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
     float* d = tab + kMaxN;
     float2* twf = reinterpret_cast<float2*>(tab + 2 * kMaxN);
     float2* twi = reinterpret_cast<float2*>(tab + 4 * kMaxN);
-    k_static_axis<<<(N + 127) / 128, 128, 0, s>>>(N, threads_per_pencil(N), desc->length[a], desc->dealias,
+    k_static_axis<<<(N + 127) / 128, 128, 0, s>>>(N, desc->length[a], desc->dealias,
                                                   desc->filter_enabled, desc->filter_p, desc->filter_alpha, P, d,
                                                   twf, twi);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "table kernel");
