@@ -35,6 +35,11 @@ extern "C" {
 /* equation sets */
 #define PS_EQ_EULER 0
 
+/* arithmetic of the LGL differentiation-matrix contractions */
+#define PS_GEMM_FP32 0   /* float32 operands, float32 accumulate                 */
+#define PS_GEMM_FP64 1   /* float64 operands and accumulate (flux in float64)     */
+#define PS_GEMM_BF16X3 2 /* split bf16: hi*hi + hi*lo + lo*hi, float32 accumulate */
+
 typedef struct ps_plan_s* ps_plan;
 
 /*
@@ -57,10 +62,12 @@ typedef struct {
   int filter_interval;   /* cadence of the end-of-step filter (1D/2D)         */
   double gravity[3];     /* constant gravity (solver.py:82-91); 0 = off       */
   double cfl;            /* CFL number for ps_compute_dt                      */
+  int gemm_precision;    /* PS_GEMM_* (LGL grids; ignored for Fourier)        */
 } ps_plan_desc;
 
 /* Fill a descriptor with the reference defaults for `ndim` (dealias on,
- * filter off with p=8, alpha=36, interval 1, gamma 1.4, cfl 0.4/0.3/0.25). */
+ * filter off with p=8, alpha=36, interval 1, gamma 1.4, cfl 0.4/0.3/0.25,
+ * float32 LGL contractions). */
 int ps_plan_desc_init(ps_plan_desc* desc, int ndim);
 
 /* Device scratch a plan allocates at creation (bytes), for HBM admission. */
@@ -69,7 +76,13 @@ int ps_batch_scratch_bytes(const ps_plan_desc* desc, int nsolve, size_t* bytes);
 
 /* Build spectral tables and allocate scratch on the current device.
  * Replaces Grid*.__post_init__ + _setup_fourier_backend (grid.py:183-383,
- * 806-992, 1378-1495) and solver construction (solver.py:156-232). */
+ * 806-992, 1378-1495) and solver construction (solver.py:156-232).
+ * A 2D descriptor with PS_BASIS_LEGENDRE on both axes makes an LGL x LGL
+ * plan (Grid2D with basis_x = basis_y = "legendre", grid.py:806-840, and
+ * LegendreLobattoBasis2D, basis/legendre.py:894-934): n >= 3 nodes per axis,
+ * solid walls (bc "dirichlet", grid.py:994-1154) applied in place to every
+ * stage input and after every step, the 2D positivity clamp after every RK
+ * stage, the nodal filter (legendre.py:825-859) when enabled. */
 int ps_plan_create(const ps_plan_desc* desc, ps_plan* out);
 int ps_plan_destroy(ps_plan plan);
 
@@ -131,6 +144,22 @@ int ps_max_wave_speed(ps_plan plan, const float* U, float* d_out, void* stream);
  * solvers' record() (solver.py:372-377, 741-767, 1439-1468). */
 int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);
 
+/* LGL nodes, quadrature weights and differentiation matrix of one axis,
+ * built on the device in float64: nodes ascending on [0, length], weights
+ * of the reference interval [-1, 1], D[i][j] = d l_j / dx at x_i ([n][n],
+ * row-major).  Replaces _legendre_gauss_lobatto_nodes_weights and
+ * _stable_legendre_diff_matrix with the axis scaling of
+ * LegendreLobattoBasis1D (basis/legendre.py:523-624, 694-729).  Any of the
+ * three outputs may be NULL. */
+int ps_lgl_build(int n, double length, double* d_nodes, double* d_weights, double* d_D, void* stream);
+
+/* Apply the plan's boundary conditions to U in place: the solid walls of an
+ * LGL x LGL plan (grid.py:1072-1154: left, right, top, bottom; density,
+ * tangential momentum and energy copy the neighbouring line, the normal
+ * momentum is zeroed).  A no-op for periodic Fourier plans, like
+ * Grid*.apply_boundary_conditions there (grid.py:631-632, 1087-1089). */
+int ps_apply_boundary_conditions(ps_plan plan, float* U, void* stream);
+
 /* Device status word of a plan, read synchronously: 0 = healthy; bit
  * PS_STATUS_TMA_TIMEOUT = a kernel gave up waiting for a tile load (bounded
  * wait) and its results are invalid.  No reference counterpart: the
@@ -150,7 +179,9 @@ int ps_plan_status(ps_plan plan, int* status);
 #define PS_KIND_LAST 2   /* last pass: rhs + RK4 stage (+ filter)  */
 #define PS_KIND_OP 3     /* one-axis operator / filter pass        */
 #define PS_KIND_STEP1D 4 /* 1D whole-step kernel                   */
-#define PS_NKINDS 5
+#define PS_KIND_LGL_X 5  /* LGL: x flux + contraction with D_x     */
+#define PS_KIND_LGL_Y 6  /* LGL: y flux + D_y contraction + stage  */
+#define PS_NKINDS 7
 int ps_profile_enable(ps_plan plan, int enable);
 int ps_profile_collect(ps_plan plan, int nkinds, int* launches, double* ms, double* bytes);
 

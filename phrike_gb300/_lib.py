@@ -18,7 +18,11 @@ PS_OK = 0
 PS_BASIS_FOURIER = 0
 PS_BASIS_LEGENDRE = 1
 PS_EQ_EULER = 0
-KIND_NAMES = ["x_pass", "y_pass", "last_pass", "op_pass", "step1d"]
+PS_GEMM_FP32 = 0
+PS_GEMM_FP64 = 1
+PS_GEMM_BF16X3 = 2
+GEMM_PRECISIONS = {"fp32": PS_GEMM_FP32, "fp64": PS_GEMM_FP64, "bf16x3": PS_GEMM_BF16X3}
+KIND_NAMES = ["x_pass", "y_pass", "last_pass", "op_pass", "step1d", "lgl_x", "lgl_y"]
 
 
 class PlanDesc(C.Structure):
@@ -36,6 +40,7 @@ class PlanDesc(C.Structure):
         ("filter_interval", C.c_int),
         ("gravity", C.c_double * 3),
         ("cfl", C.c_double),
+        ("gemm_precision", C.c_int),
     ]
 
 
@@ -63,6 +68,8 @@ _SIGNATURES = [
     ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
     ("ps_rhs_static", C.c_int, [C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_lgl_build", C.c_int, [C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_apply_boundary_conditions", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_last_error", C.c_char_p, []),
     ("ps_version", C.c_char_p, []),
 ]

@@ -1,0 +1,288 @@
+// LGL x LGL plans: validation, device tables, the RK4 step loop (fixed dt or
+// CFL), bare right-hand side, derivative and filter operators.
+//
+// One RK stage is three launches: the walls on the stage input (in place, as
+// _compute_rhs_2d does, solver.py:428-466 with grid.py:1072-1154), the x
+// kernel (x flux contracted with D_x) and the y kernel (y flux contracted
+// with D_y, fused with the RK4 stage update and the 2D clamp).  After each
+// step, at the filter cadence, the nodal filter (if enabled) and the walls
+// are applied to the new state (solver.py:623-648).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "lgl.cuh"
+#include "plan.cuh"
+#include "reduce.cuh"
+
+namespace ps {
+namespace {
+
+int cfail(cudaError_t e, const char* what) { return errorf(PS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e)); }
+
+#define LGL_CU(expr, what)                     \
+  do {                                         \
+    cudaError_t _e = (expr);                   \
+    if (_e != cudaSuccess) return cfail(_e, what); \
+  } while (0)
+
+int mode_of(const ps_plan_s* p) { return (p->gemm == PS_GEMM_FP64) ? 1 : (p->gemm == PS_GEMM_BF16X3) ? 2 : 0; }
+
+// axis index of the LGL tables: 0 = x (n[0]), 1 = y (n[1])
+const void* dmat(const ps_plan_s* p, int a) {
+  return (p->gemm == PS_GEMM_FP64) ? static_cast<const void*>(p->D64[a]) : static_cast<const void*>(p->D32[a]);
+}
+const void* fmat(const ps_plan_s* p, int a) {
+  return (p->gemm == PS_GEMM_FP64) ? static_cast<const void*>(p->F64[a]) : static_cast<const void*>(p->F32[a]);
+}
+
+LglStageArgs stage_args(ps_plan p, const float* in, int stage, const float* Un, float* out, double dt,
+                        const double* d_dt, const int* active) {
+  LglStageArgs a{};
+  a.U = in;
+  a.Gx = p->G;
+  a.Dx = dmat(p, 0);
+  a.Dy = dmat(p, 1);
+  a.nx = p->n[0];
+  a.ny = p->n[1];
+  a.ss = p->ss(4);
+  a.gamma = (float)p->desc.gamma;
+  a.eref = p->eref;
+  a.active = active;
+  a.stage = stage;
+  a.Un = Un;
+  a.acc = p->acc;
+  a.out = out;
+  a.dt_dev = d_dt;
+  a.dt = dt;
+  a.rho_min = 1e-8f;  // 2D clamp floors (solver.py:489-490)
+  a.p_min = 1e-10f;
+  a.nsolve = p->nsolve;
+  return a;
+}
+
+// bytes of one float32 field over all solves; the x kernel moves 8 fields
+// (reads U, writes Gx), the y kernel 12..24 (reads U and Gx, plus U^n and the
+// accumulator and their writes as the stage needs them)
+double field_bytes(const ps_plan_s* p) { return 4.0 * p->cells * p->nsolve; }
+
+int stage(ps_plan p, float* in, int st, float* Un, float* out, double dt, const double* d_dt, const int* act,
+          cudaStream_t s) {
+  LGL_CU(launch_lgl_bc(in, p->n[0], p->n[1], p->ss(4), p->nsolve, act, s), "LGL walls");
+  const LglStageArgs a = stage_args(p, in, st, Un, out, dt, d_dt, act);
+  {
+    ProfScope prof(p, s, PS_KIND_LGL_X, 8.0 * field_bytes(p));
+    LGL_CU(launch_lgl_x(a, mode_of(p), s), "LGL x contraction");
+  }
+  {
+    const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
+    ProfScope prof(p, s, PS_KIND_LGL_Y, words * field_bytes(p));
+    LGL_CU(launch_lgl_y(a, mode_of(p), s), "LGL y contraction + stage update");
+  }
+  return PS_OK;
+}
+
+// out[z] = f[z] . M^T along x (M = D_x or F_x) or M . f[z] along y, for Z
+// consecutive fields of `cells` each.  f and out must not alias.
+int contract(ps_plan p, int axis, bool filter, const float* f, float* out, long Z, const int* act, int zper,
+             cudaStream_t s) {
+  const int nx = p->n[0], ny = p->n[1];
+  const long cells = p->cells;
+  GemmArgs g{};
+  g.c = out;
+  g.batch = (int)Z;
+  g.alpha = 1.0f;
+  g.active = act;
+  g.zper = zper;
+  const void* M = filter ? fmat(p, axis) : dmat(p, axis);
+  GemmKind kind = kGemmF32;
+  bool ak, bk;
+  if (axis == 0) {
+    g.a = f;
+    g.b = M;
+    g.M = ny;
+    g.N = nx;
+    g.K = nx;
+    g.am = nx, g.ak = 1, g.az = cells;
+    g.bn = nx, g.bk = 1, g.bz = 0;
+    ak = true;
+    bk = true;
+    if (p->gemm == PS_GEMM_FP64) kind = kGemmF32F64;
+  } else {
+    g.a = M;
+    g.b = f;
+    g.M = ny;
+    g.N = nx;
+    g.K = ny;
+    g.am = ny, g.ak = 1, g.az = 0;
+    g.bn = 1, g.bk = nx, g.bz = cells;
+    ak = true;
+    bk = false;
+    if (p->gemm == PS_GEMM_FP64) kind = kGemmF64F32;
+  }
+  g.cm = nx, g.cn = 1, g.cz = cells;
+  if (p->gemm == PS_GEMM_BF16X3) kind = kGemmSplitAB;
+  for (long z0 = 0; z0 < Z; z0 += 65535) {  // grid.z limit
+    GemmArgs gz = g;
+    gz.batch = (int)((Z - z0 < 65535) ? Z - z0 : 65535);
+    gz.a = (axis == 0) ? static_cast<const void*>(f + z0 * cells) : M;
+    gz.b = (axis == 0) ? M : static_cast<const void*>(f + z0 * cells);
+    gz.c = out + z0 * cells;
+    if (act != nullptr && z0 != 0) return errorf(PS_ERR_INVALID, "internal: masked contraction over 65535 fields");
+    LGL_CU(launch_gemm(gz, kind, ak, bk, s), "LGL contraction");
+  }
+  return PS_OK;
+}
+
+// nodal filter of the state, both axes, through the scratch G (4 nsolve fields)
+int filter_state(ps_plan p, float* U, const int* act, cudaStream_t s) {
+  int rc;
+  const long Z = 4L * p->nsolve;
+  ProfScope prof(p, s, PS_KIND_OP, 16.0 * 4.0 * p->cells * p->nsolve);
+  if ((rc = contract(p, 0, true, U, p->G, Z, act, 4, s)) != PS_OK) return rc;
+  return contract(p, 1, true, p->G, U, Z, act, 4, s);
+}
+
+}  // namespace
+
+int lgl_validate(const ps_plan_desc* d) {
+  if (d->ndim != 2) return errorf(PS_ERR_UNSUPPORTED, "the Legendre basis is supported on 2D grids only");
+  if (d->basis[0] != PS_BASIS_LEGENDRE || d->basis[1] != PS_BASIS_LEGENDRE)
+    return errorf(PS_ERR_UNSUPPORTED, "mixed Fourier x Legendre grids are not supported (LGL on both axes only)");
+  if (d->equations != PS_EQ_EULER) return errorf(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
+  for (int a = 0; a < 2; ++a) {
+    if (d->n[a] < 3 || d->n[a] > 4096)
+      return errorf(PS_ERR_UNSUPPORTED, "axis %d: LGL grids need 3..4096 nodes (got %d)", a, d->n[a]);
+    if (!(d->length[a] > 0.0)) return errorf(PS_ERR_INVALID, "axis %d: length must be positive", a);
+  }
+  if (!(d->gamma > 1.0)) return errorf(PS_ERR_INVALID, "gamma must exceed 1");
+  if (d->filter_interval < 1) return errorf(PS_ERR_INVALID, "filter_interval must be >= 1");
+  if (d->gemm_precision < PS_GEMM_FP32 || d->gemm_precision > PS_GEMM_BF16X3)
+    return errorf(PS_ERR_INVALID, "gemm_precision must be PS_GEMM_FP32, PS_GEMM_FP64 or PS_GEMM_BF16X3");
+  return PS_OK;
+}
+
+size_t lgl_scratch_bytes(const ps_plan_desc* d) {
+  size_t b = 0;
+  for (int a = 0; a < 2; ++a) {
+    const size_t n = (size_t)d->n[a];
+    b += 16 * n + 12 * n * n;                 // nodes, weights, D in float64 and float32
+    if (d->filter_enabled) b += 12 * n * n;  // filter matrices
+  }
+  return b;
+}
+
+int lgl_setup(ps_plan p) {
+  int rc;
+  p->lgl = true;
+  p->gemm = p->desc.gemm_precision;
+  double hmin = 1e300;
+  for (int a = 0; a < 2; ++a) {
+    const int n = p->n[a];
+    if ((rc = plan_alloc(p, &p->lgl_x[a], n)) != PS_OK) return rc;
+    if ((rc = plan_alloc(p, &p->lgl_w[a], n)) != PS_OK) return rc;
+    if ((rc = plan_alloc(p, &p->D64[a], (size_t)n * n)) != PS_OK) return rc;
+    if ((rc = plan_alloc(p, &p->D32[a], (size_t)n * n)) != PS_OK) return rc;
+    LGL_CU(launch_lgl_build(n, p->desc.length[a], p->lgl_x[a], p->lgl_w[a], p->D64[a], p->D32[a], 0),
+           "LGL construction");
+    if (p->desc.filter_enabled) {
+      if ((rc = plan_alloc(p, &p->F64[a], (size_t)n * n)) != PS_OK) return rc;
+      if ((rc = plan_alloc(p, &p->F32[a], (size_t)n * n)) != PS_OK) return rc;
+      LGL_CU(launch_lgl_filter_matrix(n, p->desc.length[a], p->lgl_x[a], p->lgl_w[a], p->desc.filter_p,
+                                      p->desc.filter_alpha, p->F64[a], p->F32[a], 0),
+             "LGL filter matrix");
+    }
+    std::vector<double> x(n);
+    LGL_CU(cudaMemcpy(x.data(), p->lgl_x[a], sizeof(double) * n, cudaMemcpyDeviceToHost), "LGL nodes read");
+    for (int j = 0; j + 1 < n; ++j) hmin = fmin(hmin, x[j + 1] - x[j]);  // grid.py:826-832
+  }
+  p->lgl_hmin = hmin;
+  return PS_OK;
+}
+
+int lgl_rhs(ps_plan p, const float* U, float* rhs, cudaStream_t s) {
+  // the reference applies the walls to U in place before the fluxes; here to
+  // a copy, so U is left as given
+  const size_t bytes = sizeof(float) * p->ss(4) * p->nsolve;
+  LGL_CU(cudaMemcpyAsync(p->Us, U, bytes, cudaMemcpyDeviceToDevice, s), "state copy");
+  float* E = p->Us + 3 * p->cells;
+  LGL_CU(launch_eref_set(E, p->ss(4), p->nsolve, p->eref, s), "energy reference");
+  LGL_CU(launch_energy_shift(E, p->cells, p->ss(4), p->nsolve, p->eref, -1.0f, s), "energy shift");
+  return stage(p, p->Us, -1, nullptr, rhs, 0.0, nullptr, nullptr, s);
+}
+
+int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+              cudaStream_t s) {
+  int rc;
+  const bool cfl = d_t != nullptr;
+  const int* act = cfl ? p->active : nullptr;
+  const double* dtp = cfl ? p->dt : d_dt;
+  const long ssU = p->ss(4);
+  float* E = U + 3 * p->cells;
+  LGL_CU(launch_eref_set(E, ssU, p->nsolve, p->eref, s), "energy reference");
+  LGL_CU(launch_energy_shift(E, p->cells, ssU, p->nsolve, p->eref, -1.0f, s), "energy shift");
+  if (cfl) LGL_CU(launch_fill_int(p->active, p->nsolve, 1, s), "active reset");
+  for (int it = 0; it < nsteps; ++it) {
+    const bool due = (p->step_counter % p->desc.filter_interval) == 0;
+    if (cfl) {
+      // dt from the state as given, before the walls of the first stage
+      // (solver.py:386-389 compute_dt, then step)
+      LGL_CU(launch_speed(2, U, p->cells, ssU, p->nsolve, (float)p->desc.gamma, p->speed, s, p->eref),
+             "wave speed");
+      LGL_CU(launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
+             "step control");
+    }
+    for (int st = 0; st < 4; ++st) {
+      float* in = (st == 0) ? U : p->Us;
+      float* out = (st < 3) ? p->Us : U;
+      if ((rc = stage(p, in, st, U, out, dt, dtp, act, s)) != PS_OK) return rc;
+    }
+    if (due) {
+      if (p->desc.filter_enabled && (rc = filter_state(p, U, act, s)) != PS_OK) return rc;
+      LGL_CU(launch_lgl_bc(U, p->n[0], p->n[1], ssU, p->nsolve, act, s), "LGL walls");
+    }
+    if (cfl) LGL_CU(launch_step_advance(d_t, p->dt, p->speed, p->active, p->steps_done, p->nsolve, s), "advance");
+    p->step_counter += 1;
+  }
+  LGL_CU(launch_energy_shift(E, p->cells, ssU, p->nsolve, p->eref, 1.0f, s), "energy shift");
+  return PS_OK;
+}
+
+int lgl_derivative(ps_plan p, int axis, const float* f, float* out, int nf, cudaStream_t s) {
+  const long Z = (long)nf * p->nsolve;
+  if (f != out) return contract(p, axis, false, f, out, Z, nullptr, 1, s);
+  // in place: through the scratch G (8 nsolve fields) in chunks
+  const long cap = 8L * p->nsolve;
+  int rc;
+  for (long z0 = 0; z0 < Z; z0 += cap) {
+    const long zc = (Z - z0 < cap) ? Z - z0 : cap;
+    if ((rc = contract(p, axis, false, f + z0 * p->cells, p->G, zc, nullptr, 1, s)) != PS_OK) return rc;
+    LGL_CU(cudaMemcpyAsync(out + z0 * p->cells, p->G, sizeof(float) * zc * p->cells, cudaMemcpyDeviceToDevice, s),
+           "derivative copy");
+  }
+  return PS_OK;
+}
+
+int lgl_filter(ps_plan p, const float* f, float* out, int nf, cudaStream_t s) {
+  if (!p->desc.filter_enabled) {
+    // the reference returns the input unchanged when the filter is off
+    // (grid.py:1260-1267)
+    if (f != out)
+      LGL_CU(cudaMemcpyAsync(out, f, sizeof(float) * p->cells * nf * p->nsolve, cudaMemcpyDeviceToDevice, s),
+             "filter copy");
+    return PS_OK;
+  }
+  const long Z = (long)nf * p->nsolve;
+  const long cap = 8L * p->nsolve;
+  int rc;
+  for (long z0 = 0; z0 < Z; z0 += cap) {
+    const long zc = (Z - z0 < cap) ? Z - z0 : cap;
+    if ((rc = contract(p, 0, true, f + z0 * p->cells, p->G, zc, nullptr, 1, s)) != PS_OK) return rc;
+    if ((rc = contract(p, 1, true, p->G, out + z0 * p->cells, zc, nullptr, 1, s)) != PS_OK) return rc;
+  }
+  return PS_OK;
+}
+
+}  // namespace ps

@@ -14,6 +14,8 @@
 
 #include "../../include/phrike_gb300.h"
 #include "launch.cuh"
+#include "lgl.cuh"
+#include "plan.cuh"
 #include "reduce.cuh"
 
 namespace {
@@ -49,100 +51,32 @@ int record_error(int code, const char* msg) {
   g_err = msg;
   return code;
 }
+
+int errorf(int code, const char* fmt, ...) {
+  char msg[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  g_err = msg;
+  return code;
+}
 }  // namespace ps
-
-struct ps_plan_s {
-  ps_plan_desc desc;
-  int nd = 0;
-  int nsolve = 1;  // independent solves of the same grid (a batch)
-  int n[3] = {1, 1, 1};
-  long cells = 0;  // cells of one solve
-  int nc = 0;
-  // per-axis spectral tables (device): P, d, twf, twi
-  float* P[3] = {nullptr, nullptr, nullptr};
-  float* d[3] = {nullptr, nullptr, nullptr};
-  float2* twf[3] = {nullptr, nullptr, nullptr};
-  float2* twi[3] = {nullptr, nullptr, nullptr};
-  // scratch, [nsolve][nfields][cells] each
-  float* G = nullptr;    // x-pass outputs (2D: 8 fields, 3D: 15)
-  float* AB = nullptr;   // 3D y-pass outputs (10 fields)
-  float* acc = nullptr;  // RK accumulator (nc fields)
-  float* Us = nullptr;   // stage input (nc fields)
-  float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
-  // per-solve device scalars
-  float* speed = nullptr;  // CFL wave speed maxima
-  float* eref = nullptr;   // E_ref of the energy-perturbation form
-  double* dt = nullptr;    // step sizes (CFL runs)
-  int* active = nullptr;   // 1 while a solve advances (CFL runs)
-  int* steps_done = nullptr;
-  int* status = nullptr;   // device status word (PS_STATUS_* bits set by kernels)
-  // TMA tensor maps of the plan buffers and of the last state pointer seen
-  CUtensorMap map_G_y{};    // G, y pencils
-  CUtensorMap map_AB_z{};   // AB, z pencils (3D)
-  CUtensorMap map_acc{};    // acc, last-pass pencils
-  const float* map_U_ptr = nullptr;
-  CUtensorMap map_U_last{};  // state, last-pass pencils
-  long step_counter = 0;
-  std::vector<void*> allocations;
-  // launch profiling: CUDA events around every pass launch
-  struct LaunchRec {
-    int kind;
-    double bytes;
-    cudaEvent_t start, stop;
-  };
-  bool profiling = false;
-  std::vector<LaunchRec> launches;
-  std::vector<cudaEvent_t> event_pool;
-
-  ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
-  long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
-  int rows() const { return (int)(cells / n[0]); }     // x-pencil rows of one solve
-  double hmin() const {                                 // smallest grid spacing (CFL)
-    double h = desc.length[0] / n[0];
-    for (int a = 1; a < nd; ++a) h = fmin(h, desc.length[a] / n[a]);
-    return h;
-  }
-};
 
 namespace {
 
-// Launch profiling.  begin() records a start event before a pass launch;
-// end() records the stop event and the algorithmic bytes the pass moves.
-cudaEvent_t take_event(ps_plan p) {
-  if (!p->event_pool.empty()) {
-    cudaEvent_t e = p->event_pool.back();
-    p->event_pool.pop_back();
-    return e;
-  }
-  cudaEvent_t e = nullptr;
-  cudaEventCreate(&e);
-  return e;
-}
+using ps::ProfScope;
 
-struct ProfScope {
-  ps_plan p;
-  cudaStream_t s;
-  int kind;
-  double bytes;
-  cudaEvent_t start = nullptr;
-  ProfScope(ps_plan p_, cudaStream_t s_, int kind_, double bytes_) : p(p_), s(s_), kind(kind_), bytes(bytes_) {
-    if (p->profiling) {
-      start = take_event(p);
-      cudaEventRecord(start, s);
-    }
-  }
-  ~ProfScope() {
-    if (p->profiling && start) {
-      cudaEvent_t stop = take_event(p);
-      cudaEventRecord(stop, s);
-      p->launches.push_back({kind, bytes, start, stop});
-    }
-  }
-};
+bool is_lgl(const ps_plan_desc* d) {
+  for (int a = 0; a < d->ndim && a < 3; ++a)
+    if (d->basis[a] == PS_BASIS_LEGENDRE) return true;
+  return false;
+}
 
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
   if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
+  if (is_lgl(d)) return ps::lgl_validate(d);
   if (d->equations != PS_EQ_EULER) return fail(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
   for (int a = 0; a < d->ndim; ++a) {
     if (d->basis[a] != PS_BASIS_FOURIER)
@@ -202,15 +136,7 @@ void build_axis(int N, double L, int dealias, int fon, int fp, double falpha, st
 
 template <typename Tp>
 int dalloc(ps_plan p, Tp** ptr, size_t count) {
-  void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, count * sizeof(Tp));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return fail(PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(Tp), cudaGetErrorString(e));
-  }
-  p->allocations.push_back(q);
-  *ptr = static_cast<Tp*>(q);
-  return PS_OK;
+  return ps::plan_alloc(p, ptr, count);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no
@@ -531,7 +457,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     ps_plan_destroy(p);
     return code;
   };
-  for (int a = 0; a < p->nd; ++a) {
+  const bool lgl = is_lgl(d);
+  for (int a = 0; a < p->nd && !lgl; ++a) {
     std::vector<float> P, dd;
     std::vector<float2> twf, twi;
     build_axis(p->n[a], d->length[a], d->dealias, d->filter_enabled, d->filter_p, d->filter_alpha, P, dd, twf, twi);
@@ -568,7 +495,9 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
       cudaMemset(p->steps_done, 0, sizeof(int) * nsolve) != cudaSuccess ||
       cudaMemset(p->status, 0, sizeof(int)) != cudaSuccess)
     return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
-  if (p->nd >= 2) {
+  if (lgl) {
+    if ((rc = ps::lgl_setup(p)) != PS_OK) return cleanup(rc);
+  } else if (p->nd >= 2) {
     if ((rc = make_map(&p->map_G_y, p->G, p, (p->nd == 3) ? 15 : 8, 1)) != PS_OK) return cleanup(rc);
     if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
     if ((rc = make_map(&p->map_acc, p->acc, p, p->nc, (p->nd == 3) ? 2 : 1)) != PS_OK) return cleanup(rc);
@@ -614,6 +543,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   for (int a = 0; a < d->ndim; ++a) cells *= d->n[a];
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
+  if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d);
   *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
@@ -688,6 +618,7 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
   if (!p || !U || !rhs) return fail(PS_ERR_INVALID, "null argument");
   cudaStream_t s = (cudaStream_t)stream;
   int rc;
+  if (p->lgl) return ps::lgl_rhs(p, U, rhs, s);
   if (p->nd == 1) {
     PS_CU(ps::launch_flux1d(U, p->cells, p->ss(3), p->nsolve, (float)p->desc.gamma, p->F1, s), "1D flux");
     return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
@@ -708,6 +639,7 @@ int ps_run_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt,
   if (nsteps < 0) return fail(PS_ERR_INVALID, "nsteps must be >= 0");
   if (nsteps == 0) return PS_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  if (p->lgl) return ps::lgl_steps(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
   if (p->nd == 1) return step_1d(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
   return steps_nd(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
 }
@@ -717,6 +649,7 @@ int ps_run_cfl(ps_plan p, float* U, int nsteps, double* d_t, const double* d_ten
   if (nsteps < 0) return fail(PS_ERR_INVALID, "nsteps must be >= 0");
   if (nsteps == 0) return PS_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  if (p->lgl) return ps::lgl_steps(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   if (p->nd == 1) return step_1d(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   return steps_nd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
 }
@@ -726,6 +659,7 @@ int ps_derivative(ps_plan p, int axis, const float* f, float* out, int nf, void*
   if (axis < 0 || axis >= p->nd) return fail(PS_ERR_INVALID, "axis %d out of range", axis);
   if (nf < 1) return fail(PS_ERR_INVALID, "nfields must be >= 1");
   cudaStream_t s = (cudaStream_t)stream;
+  if (p->lgl) return ps::lgl_derivative(p, axis, f, out, nf, s);
   const float* src = f;
   int rc;
   for (int a = 0; a < p->nd; ++a) {
@@ -739,12 +673,30 @@ int ps_filter(ps_plan p, const float* f, float* out, int nf, void* stream) {
   if (!p || !f || !out) return fail(PS_ERR_INVALID, "null argument");
   if (nf < 1) return fail(PS_ERR_INVALID, "nfields must be >= 1");
   cudaStream_t s = (cudaStream_t)stream;
+  if (p->lgl) return ps::lgl_filter(p, f, out, nf, s);
   const float* src = f;
   int rc;
   for (int a = 0; a < p->nd; ++a) {
     if ((rc = apply_op(p, a, src, out, nf, 0, 1.0f, s, true)) != PS_OK) return rc;
     src = out;
   }
+  return PS_OK;
+}
+
+int ps_lgl_build(int n, double length, double* d_nodes, double* d_weights, double* d_D, void* stream) {
+  if (n < 2) return fail(PS_ERR_INVALID, "LGL grids need at least 2 nodes (got %d)", n);
+  if (!(length > 0.0)) return fail(PS_ERR_INVALID, "length must be positive");
+  if (d_D != nullptr && (d_nodes == nullptr || d_weights == nullptr))
+    return fail(PS_ERR_INVALID, "the differentiation matrix needs the node and weight arrays");
+  if (d_nodes == nullptr && d_weights == nullptr) return PS_OK;
+  PS_CU(ps::launch_lgl_build(n, length, d_nodes, d_weights, d_D, nullptr, (cudaStream_t)stream), "LGL build");
+  return PS_OK;
+}
+
+int ps_apply_boundary_conditions(ps_plan p, float* U, void* stream) {
+  if (!p || !U) return fail(PS_ERR_INVALID, "null argument");
+  if (!p->lgl) return PS_OK;  // periodic Fourier grids have none
+  PS_CU(ps::launch_lgl_bc(U, p->n[0], p->n[1], p->ss(4), p->nsolve, nullptr, (cudaStream_t)stream), "LGL walls");
   return PS_OK;
 }
 

@@ -9,9 +9,13 @@ namespace ps {
 
 // Max wave speed with the reference's per-dimension rule
 // (equations.py:89-98 1D |u|+a, 137-147 2D |u_x|+a, 199-211 3D max|u_i|+a).
+// eshift (nullable): per-solve constant added to the stored energy (states in
+// energy-perturbation form store E - E_ref).
 template <int ND>
-__global__ void k_speed(const float* __restrict__ U, long cells, long ss, float gamma, float* out) {
+__global__ void k_speed(const float* __restrict__ U, long cells, long ss, float gamma, const float* eshift,
+                        float* out) {
   __shared__ float red[32];
+  const float es = (eshift != nullptr) ? eshift[blockIdx.y] : 0.0f;
   U += (long)blockIdx.y * ss;
   out += blockIdx.y;
   float m = 0.0f;
@@ -25,7 +29,7 @@ __global__ void k_speed(const float* __restrict__ U, long cells, long ss, float 
       kin = fmaf(v, v, kin);
       if (d == 0 || ND == 3) um = fmaxf(um, fabsf(v));
     }
-    const float p = (gamma - 1.0f) * (U[(ND + 1) * cells + i] - 0.5f * rho * kin);
+    const float p = (gamma - 1.0f) * ((U[(ND + 1) * cells + i] + es) - 0.5f * rho * kin);
     m = fmaxf(m, um + sqrtf(gamma * p / rho));
   }
   m = block_max(m, red);
@@ -170,13 +174,13 @@ static int reduce_blocks(long cells, int nsolve) {
 }
 
 cudaError_t launch_speed(int nd, const float* U, long cells, long ss, int nsolve, float gamma, float* out,
-                         cudaStream_t s) {
+                         cudaStream_t s, const float* eshift) {
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * nsolve, s);
   if (e != cudaSuccess) return e;
   const dim3 grid(reduce_blocks(cells, nsolve), nsolve);
-  if (nd == 1) k_speed<1><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
-  else if (nd == 2) k_speed<2><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
-  else k_speed<3><<<grid, 256, 0, s>>>(U, cells, ss, gamma, out);
+  if (nd == 1) k_speed<1><<<grid, 256, 0, s>>>(U, cells, ss, gamma, eshift, out);
+  else if (nd == 2) k_speed<2><<<grid, 256, 0, s>>>(U, cells, ss, gamma, eshift, out);
+  else k_speed<3><<<grid, 256, 0, s>>>(U, cells, ss, gamma, eshift, out);
   return cudaGetLastError();
 }
 

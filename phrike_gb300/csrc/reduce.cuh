@@ -12,8 +12,9 @@ cudaError_t launch_step_control(const float* speed, double cfl, double hmin, con
                                 int nsolve, double* dt, int* active, cudaStream_t s);
 cudaError_t launch_step_advance(double* t, const double* dt, float* speed, const int* active, int* steps,
                                 int nsolve, cudaStream_t s);
+// eshift (nullable): per-solve energy offset of states stored as E - E_ref
 cudaError_t launch_speed(int nd, const float* U, long cells, long ss, int nsolve, float gamma, float* out,
-                         cudaStream_t s);
+                         cudaStream_t s, const float* eshift = nullptr);
 cudaError_t launch_conserved(int nd, const float* U, long cells, long ss, int nsolve, double gamma, double* out,
                              cudaStream_t s);
 cudaError_t launch_flux1d(const float* U, long n, long ss, int nsolve, float gamma, float* F, cudaStream_t s);

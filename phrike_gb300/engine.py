@@ -22,19 +22,37 @@ def _ptr(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(t.data_ptr())
 
 
+def lgl_build(n: int, length: float, device: Optional[torch.device] = None):
+    """LGL nodes (ascending on [0, length]), weights on [-1, 1] and the
+    differentiation matrix of one axis, built on the device in float64
+    (ps_lgl_build).  Returns three float64 device tensors."""
+    lib = _lib.load()
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    x = torch.empty(n, dtype=torch.float64, device=dev)
+    w = torch.empty(n, dtype=torch.float64, device=dev)
+    D = torch.empty((n, n), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _lib.check(lib.ps_lgl_build(int(n), float(length), _ptr(x), _ptr(w), _ptr(D), _stream(dev)))
+    return x, w, D
+
+
 class Plan:
-    """A batch of ``nsolve`` Fourier pseudo-spectral Euler solves of one grid
+    """A batch of ``nsolve`` pseudo-spectral Euler solves of one grid
     (1-3 dimensions); ``nsolve=1`` is a single solve.
 
     ``shape`` is the spatial shape in array order ((N,), (Ny, Nx) or
     (Nz, Ny, Nx)); ``lengths`` follows the same order.  State tensors have
     shape (ncomp, *shape) for one solve and (nsolve, ncomp, *shape) for a batch.
+    ``basis="legendre"`` makes a 2D LGL x LGL plan with solid walls;
+    ``gemm_precision`` ("fp32", "fp64" or "bf16x3") sets the arithmetic of its
+    differentiation-matrix contractions.
     """
 
     def __init__(self, shape: Sequence[int], lengths: Sequence[float], gamma: float = 1.4,
                  dealias: bool = True, filter_params: Optional[Dict] = None,
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
-                 device: Optional[torch.device] = None, nsolve: int = 1):
+                 device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
+                 gemm_precision: str = "fp32"):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -49,6 +67,16 @@ class Plan:
         for a in range(self.ndim):
             desc.n[a] = xyz[a]
             desc.length[a] = lxyz[a]
+        basis = str(basis).lower()
+        if basis not in ("fourier", "legendre"):
+            raise ValueError(f"unknown basis {basis!r}")
+        self.basis = basis
+        for a in range(self.ndim):
+            desc.basis[a] = _lib.PS_BASIS_LEGENDRE if basis == "legendre" else _lib.PS_BASIS_FOURIER
+        if str(gemm_precision).lower() not in _lib.GEMM_PRECISIONS:
+            raise ValueError(f"gemm_precision must be one of {sorted(_lib.GEMM_PRECISIONS)}")
+        self.gemm_precision = str(gemm_precision).lower()
+        desc.gemm_precision = _lib.GEMM_PRECISIONS[self.gemm_precision]
         desc.gamma = float(gamma)
         desc.dealias = 1 if dealias else 0
         fp = filter_params or {}
@@ -154,6 +182,12 @@ class Plan:
         out = torch.empty_like(f) if out is None else out
         _lib.check(self._lib.ps_filter(self._handle, _ptr(f), _ptr(out), nf, _stream(self.device)))
         return out
+
+    def apply_boundary_conditions_(self, U: torch.Tensor) -> torch.Tensor:
+        """Walls of an LGL plan in place (no-op for Fourier plans)."""
+        self._check_state(U)
+        _lib.check(self._lib.ps_apply_boundary_conditions(self._handle, _ptr(U), _stream(self.device)))
+        return U
 
     def max_wave_speed(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)

@@ -1,5 +1,6 @@
-"""Fourier grids with the reference's constructor signatures and operators,
-backed by the CUDA engine (backend "gb300").
+"""Grids with the reference's constructor signatures and operators, backed
+by the CUDA engine (backend "gb300"): periodic Fourier grids in 1-3D and the
+2D LGL x LGL (Legendre-Gauss-Lobatto) grid with solid walls.
 
 Mirrors phrike/grid.py: Grid1D (lines 144-735), Grid2D (775-1354) and
 Grid3D (1357-1744).  Arrays are float32 torch tensors on the grid's CUDA
@@ -14,7 +15,7 @@ from typing import Any, Dict, Optional, Tuple
 import numpy as np
 import torch
 
-from .engine import Plan
+from .engine import Plan, lgl_build
 
 
 def _fftfreq_k(n: int, length: float) -> np.ndarray:
@@ -45,11 +46,24 @@ def _check_backend(backend: str, basis: str = "fourier") -> None:
         raise ValueError(f"Unknown or unsupported basis for the gb300 Fourier grids: {basis!r}")
 
 
+def _is_lgl2d(basis_x: str, basis_y: str) -> bool:
+    bx, by = str(basis_x).lower(), str(basis_y).lower()
+    if bx == "legendre" and by == "legendre":
+        return True
+    if "legendre" in (bx, by):
+        raise ValueError("backend 'gb300' supports Legendre on both axes (LGL x LGL) or Fourier on both, "
+                         f"not a hybrid (got basis_x={basis_x!r}, basis_y={basis_y!r})")
+    return False
+
+
 class _FourierGridBase:
     """Shared device plumbing: the plan, tensor conversion, operators."""
 
     _shape: Tuple[int, ...]
     _lengths: Tuple[float, ...]
+
+    _basis = "fourier"
+    gemm_precision = "fp32"
 
     def _init_plan(self, dealias: bool, filter_params: Optional[Dict], torch_device: Optional[str],
                    precision: str, gamma: float = 1.4) -> None:
@@ -74,7 +88,8 @@ class _FourierGridBase:
         g = float(gamma)
         if g not in self._plans:
             self._plans[g] = Plan(self._shape, self._lengths, gamma=g, dealias=self.dealias,
-                                  filter_params=self.filter_params, device=self.device)
+                                  filter_params=self.filter_params, device=self.device, basis=self._basis,
+                                  gemm_precision=self.gemm_precision)
         return self._plans[g]
 
     def to_device(self, f: Any) -> torch.Tensor:
@@ -97,8 +112,18 @@ class _FourierGridBase:
         return self.plan.filter(t.reshape((-1,) + self._shape)).reshape(shape)
 
     def apply_boundary_conditions(self, U: Any, equations: Any = None) -> Any:
-        """Periodic Fourier grids have no boundary conditions (grid.py:631-632, 1087-1089)."""
-        return U
+        """Periodic Fourier grids have no boundary conditions (grid.py:631-632,
+        1087-1089); an LGL x LGL grid applies its solid walls in place to a
+        float32 device tensor (grid.py:1072-1154) and returns it."""
+        if self._basis != "legendre":
+            return U
+        t = self.to_device(U)
+        shape = t.shape
+        self.plan.apply_boundary_conditions_(t.reshape((-1,) + self._shape))
+        if isinstance(U, torch.Tensor) and t.data_ptr() != U.data_ptr():
+            U.copy_(t.reshape(U.shape).to(U.dtype))
+            return U
+        return t.reshape(shape)
 
 
 class Grid1D(_FourierGridBase):
@@ -132,9 +157,10 @@ class Grid2D(_FourierGridBase):
                  filter_params: Optional[Dict[str, float]] = None, fft_workers: int = 1,
                  backend: str = "gb300", torch_device: Optional[str] = None, precision: str = "single",
                  debug: bool = False, basis_x: str = "fourier", basis_y: str = "fourier",
-                 bc: str = "dirichlet", bc_config: Optional[Dict[str, Any]] = None):
-        _check_backend(backend, basis_x)
-        _check_backend(backend, basis_y)
+                 bc: str = "dirichlet", bc_config: Optional[Dict[str, Any]] = None,
+                 gemm_precision: str = "fp32"):
+        lgl = _is_lgl2d(basis_x, basis_y)
+        _check_backend(backend, "fourier")
         self.Nx, self.Ny, self.Lx, self.Ly = int(Nx), int(Ny), float(Lx), float(Ly)
         self.basis_x, self.basis_y, self.bc, self.bc_config = basis_x, basis_y, bc, bc_config
         self.fft_workers, self.backend, self.debug = fft_workers, backend, debug
@@ -143,6 +169,9 @@ class Grid2D(_FourierGridBase):
         self.dx, self.dy = self.Lx / self.Nx, self.Ly / self.Ny
         self.dx_min = None
         self.dy_min = None
+        if lgl:
+            self._init_lgl(dealias, filter_params, torch_device, precision, gemm_precision)
+            return
         self._init_plan(dealias, filter_params, torch_device, precision)
         self.x = torch.as_tensor(np.linspace(0.0, self.Lx, self.Nx, endpoint=False), device=self.device)
         self.y = torch.as_tensor(np.linspace(0.0, self.Ly, self.Ny, endpoint=False), device=self.device)
@@ -154,6 +183,27 @@ class Grid2D(_FourierGridBase):
         sx, sy = _sigma_1d(self.Nx, filter_params), _sigma_1d(self.Ny, filter_params)
         self.dealias_mask = torch.as_tensor(my[:, None] * mx[None, :], device=self.device)
         self.filter_sigma = torch.as_tensor(sy[:, None] * sx[None, :], device=self.device)
+
+    def _init_lgl(self, dealias: bool, filter_params: Optional[Dict], torch_device: Optional[str],
+                  precision: str, gemm_precision: str) -> None:
+        """LGL x LGL grid (grid.py:806-840 with LegendreLobattoBasis2D,
+        basis/legendre.py:894-934): nodes ascending on [0, L] per axis, solid
+        walls for bc "dirichlet" (grid.py:994-1154)."""
+        if self.bc_config:
+            raise NotImplementedError("backend 'gb300': per-boundary bc_config maps are not implemented "
+                                      "(LGL grids use solid walls)")
+        if str(self.bc).lower() != "dirichlet":
+            raise NotImplementedError(f"backend 'gb300': LGL grids support bc='dirichlet' (walls), got {self.bc!r}")
+        self._basis = "legendre"
+        self.gemm_precision = str(gemm_precision).lower()
+        self._init_plan(dealias, filter_params, torch_device, precision)
+        self.x, self.w_x, self.Dx = lgl_build(self.Nx, self.Lx, self.device)
+        self.y, self.w_y, self.Dy = lgl_build(self.Ny, self.Ly, self.device)
+        self.dx_min = float(torch.min(torch.diff(self.x)).item())
+        self.dy_min = float(torch.min(torch.diff(self.y)).item())
+        self.kx = self.ky = self.ikx = self.iky = None
+        self.dealias_mask = None
+        self.filter_sigma = None
 
     def dx1(self, f: Any) -> torch.Tensor:
         return self._op(f, 0)

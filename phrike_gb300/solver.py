@@ -49,7 +49,9 @@ class _SpectralSolverBase:
         self.filter_interval = max(1, int(interval)) if interval is not None else 1
         fp["interval"] = self.filter_interval
         self.plan = Plan(grid._shape, grid._lengths, gamma=float(equations.gamma), dealias=grid.dealias,
-                         filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device)
+                         filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device,
+                         basis=getattr(grid, "_basis", "fourier"),
+                         gemm_precision=getattr(grid, "gemm_precision", "fp32"))
 
     # -- reference interface -----------------------------------------------
     def _spacing(self) -> float:

@@ -121,6 +121,29 @@ def main(ref_path: str) -> None:
         np.savez_compressed(os.path.join(HERE, f"khi2d_{Nx}x{Ny}.npz"), U0=U0, rhs0=rhs0, U=U,
                             dts=np.array(dts), t=t, U0_param=1.2, A=0.015)
 
+    # --- 2D LGL x LGL acoustic pulse, walls, torch-CPU float64 backend -----
+    # (the NumPy fallback of LegendreLobattoBasis2D.dy returns transposed
+    # axes when numba is absent, so the torch path is the correct reference)
+    import torch
+    for (nx, ny), nsteps, dt in (((17, 17), 3, 1e-4), ((33, 17), 2, 1e-4)):
+        g = grid.Grid2D(Nx=nx, Ny=ny, Lx=2.0, Ly=2.0, basis_x="legendre", basis_y="legendre",
+                        bc="dirichlet", backend="torch", torch_device="cpu", precision="double")
+        eq = equations.EulerEquations2D(gamma=1.4)
+        s = solver.SpectralSolver2D(g, eq, scheme="rk4", cfl=0.3)
+        x = np.asarray(g.x.cpu().numpy() if hasattr(g.x, "cpu") else g.x)
+        y = np.asarray(g.y.cpu().numpy() if hasattr(g.y, "cpu") else g.y)
+        U0 = problems.acoustic_pulse_lgl_2d(x - 1.0, y - 1.0, gamma=1.4, amp=0.2, width2=0.05)
+        Ut = torch.from_numpy(U0.copy())
+        rhs0 = solver._compute_rhs_2d(g, eq, Ut.clone()).numpy()
+        U = Ut.clone()
+        for _ in range(nsteps):
+            U = s.step(U, dt)
+        Dx = g._legendre_basis._Dx
+        Dy = g._legendre_basis._Dy
+        np.savez_compressed(os.path.join(HERE, f"lgl2d_{nx}x{ny}.npz"), U0=U0, rhs0=rhs0, U=U.numpy(), dt=dt,
+                            nsteps=nsteps, x=x, y=y, Dx=Dx, Dy=Dy, dt_cfl0=s.compute_dt(torch.from_numpy(U0)),
+                            amp=0.2, width2=0.05)
+
     print("golden fixtures written to", HERE)
 
 

@@ -43,3 +43,33 @@ def test_error_paths_without_device(built_lib):
     desc.n[0] = desc.n[1] = desc.n[2] = 256
     assert built_lib.ps_plan_scratch_bytes(C.byref(desc), C.byref(size)) == 0
     assert size.value >= 35 * 256 ** 3 * 4
+
+
+def test_lgl_descriptor_validation_without_device(built_lib):
+    """LGL x LGL descriptors are validated before any device work."""
+    import ctypes as C
+    from phrike_gb300 import _lib
+    desc = _lib.PlanDesc()
+    h = C.c_void_p()
+    size = C.c_size_t()
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 2) == 0
+    assert desc.gemm_precision == _lib.PS_GEMM_FP32
+    desc.n[0], desc.n[1] = 257, 257
+    desc.length[0] = desc.length[1] = 2.0
+    desc.basis[0] = _lib.PS_BASIS_LEGENDRE
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2  # hybrid basis
+    assert b"mixed" in built_lib.ps_last_error()
+    desc.basis[1] = _lib.PS_BASIS_LEGENDRE
+    assert built_lib.ps_batch_scratch_bytes(C.byref(desc), 3, C.byref(size)) == 0
+    assert size.value >= 3 * 16 * 257 * 257 * 4 + 2 * 12 * 257 * 257
+    desc.gemm_precision = 7
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 1
+    desc.gemm_precision = _lib.PS_GEMM_BF16X3
+    desc.n[1] = 2
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 3) == 0
+    for a in range(3):
+        desc.n[a] = 17
+        desc.basis[a] = _lib.PS_BASIS_LEGENDRE
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2  # 3D Legendre
+    assert built_lib.ps_lgl_build(1, 2.0, None, None, None, None) == 1

@@ -1,0 +1,213 @@
+"""LGL x LGL (2D Legendre-Gauss-Lobatto) path on the GPU against the oracle
+and the reference's golden vectors: device construction of nodes, weights
+and differentiation matrices (float64), walls, derivatives, filter, the
+right-hand side and RK4 steps in the three contraction precisions, CFL runs
+and batches.
+
+Tolerances: the state is float32, so a right-hand side carries the float32
+rounding of the flux amplified by the O(N^2) norm of D at the walls; states
+after steps are compared with relative L2 per conserved field.  The split
+bf16 contraction keeps about 16 significand bits of each operand, so its
+rhs tolerance is wider.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_l2
+from oracle import lgl as L
+from phrike_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+GAMMA = 1.4
+RHS_TOL = {"fp64": 2e-6, "fp32": 3e-4, "bf16x3": 3e-3}
+STEP_TOL = {"fp64": 2e-7, "fp32": 2e-6, "bf16x3": 2e-5}
+
+
+def _plan(nx, ny, prec="fp32", nsolve=1, filt=None, cfl=0.3):
+    from phrike_gb300.engine import Plan
+    return Plan((ny, nx), (2.0, 2.0), gamma=GAMMA, filter_params=filt, cfl=cfl, nsolve=nsolve,
+                basis="legendre", gemm_precision=prec)
+
+
+def _dev(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device="cuda")
+
+
+def _pulse(nx, ny, amp=0.01, width2=0.01):
+    ax, ay = L.LGLAxis(nx, 2.0), L.LGLAxis(ny, 2.0)
+    return problems.acoustic_pulse_lgl_2d(ax.x - 1.0, ay.x - 1.0, gamma=GAMMA, amp=amp, width2=width2)
+
+
+def _field_errors(U, R):
+    return [rel_l2(U[c], R[c]) for c in range(4)]
+
+
+@pytest.mark.parametrize("n", [3, 4, 17, 64, 257, 513])
+def test_lgl_build_matches_oracle(cuda_device, n):
+    from phrike_gb300.engine import lgl_build
+    x, w, D = lgl_build(n, 2.0)
+    ax = L.LGLAxis(n, 2.0)
+    np.testing.assert_allclose(x.cpu().numpy(), ax.x, rtol=0, atol=4e-16 * n)
+    np.testing.assert_allclose(w.cpu().numpy(), ax.w_ref, rtol=1e-13, atol=0)
+    Dg = D.cpu().numpy()
+    assert np.abs(Dg - ax.D).max() <= 1e-10 * np.abs(ax.D).max()
+    # derivative of a cubic is exact on n >= 4 nodes
+    if n >= 4:
+        xx = ax.x - 1.0
+        np.testing.assert_allclose(Dg @ xx ** 3, 3 * xx ** 2, atol=1e-9 * n * n)
+
+
+def test_lgl_walls_match_oracle(cuda_device):
+    rng = np.random.default_rng(7)
+    U = rng.uniform(0.5, 1.5, size=(4, 19, 23))
+    p = _plan(23, 19)
+    t = _dev(U)
+    p.apply_boundary_conditions_(t)
+    np.testing.assert_array_equal(t.cpu().numpy(), L.apply_wall_bc(U.astype(np.float32).copy()))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+def test_lgl_derivatives_and_filter(cuda_device, prec):
+    nx, ny = 65, 33
+    rng = np.random.default_rng(3)
+    ax, ay = L.LGLAxis(nx, 2.0), L.LGLAxis(ny, 2.0)
+    X, Y = np.meshgrid(ax.x - 1.0, ay.x - 1.0, indexing="xy")
+    f = np.stack([np.sin(2 * X) * np.cos(3 * Y), np.exp(X * Y), X ** 5 - Y ** 3, rng.standard_normal(X.shape)])
+    p = _plan(nx, ny, prec, filt={"enabled": True, "p": 8, "alpha": 36.0})
+    tol = {"fp64": 1e-7, "fp32": 2e-6, "bf16x3": 5e-5}[prec]
+    dx = p.derivative(_dev(f), 0).cpu().numpy()
+    dy = p.derivative(_dev(f), 1).cpu().numpy()
+    ref_dx = f @ ax.D.T
+    ref_dy = np.einsum("jk,cki->cji", ay.D, f)
+    for c in range(4):
+        assert rel_l2(dx[c], ref_dx[c]) < tol * 30, (c, rel_l2(dx[c], ref_dx[c]))
+        assert rel_l2(dy[c], ref_dy[c]) < tol * 30, (c, rel_l2(dy[c], ref_dy[c]))
+    Fx, Fy = ax.nodal_filter(8, 36.0), ay.nodal_filter(8, 36.0)
+    ff = p.filter(_dev(f)).cpu().numpy()
+    ref = np.einsum("jk,cki->cji", Fy, f @ Fx.T)
+    for c in range(4):
+        assert rel_l2(ff[c], ref[c]) < tol, (c, rel_l2(ff[c], ref[c]))
+    # in-place derivative
+    g = _dev(f)
+    p.derivative(g, 1, out=g)
+    assert rel_l2(g.cpu().numpy(), dy) < 1e-7
+
+
+@pytest.mark.parametrize("nx,ny", [(17, 17), (33, 17)])
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+def test_lgl_rhs_and_steps_match_reference(cuda_device, nx, ny, prec):
+    z = golden(f"lgl2d_{nx}x{ny}.npz")
+    p = _plan(nx, ny, prec)
+    U0 = _dev(z["U0"])
+    rhs = p.rhs(U0).cpu().numpy()
+    errs = _field_errors(rhs, z["rhs0"])
+    # momentum rhs compared as a vector field
+    mom = rel_l2(rhs[1:3], z["rhs0"][1:3])
+    assert max(errs[0], mom, errs[3]) < RHS_TOL[prec], errs
+    np.testing.assert_array_equal(U0.cpu().numpy(), z["U0"].astype(np.float32))  # rhs leaves U alone
+    U = _dev(z["U0"])
+    p.run_(U, int(z["nsteps"]), float(z["dt"]))
+    errs = _field_errors(U.cpu().numpy(), z["U"])
+    mom = rel_l2(U.cpu().numpy()[1:3], z["U"][1:3])
+    assert max(errs[0], mom, errs[3]) < STEP_TOL[prec], errs
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+def test_lgl_acoustic_pulse_vs_oracle(cuda_device, prec):
+    """The acoustic Gaussian pulse (amplitude 0.01, width^2 0.01) on 65 x 65
+    LGL nodes, 200 steps of dt = 1e-5, against the float64 oracle."""
+    n, nsteps, dt = 65, 200, 1e-5
+    U0 = _pulse(n, n)
+    s = L.LGLSolver2D(n, n, gamma=GAMMA)
+    R = U0.copy()
+    for _ in range(nsteps):
+        R = s.step(R, dt)
+    p = _plan(n, n, prec)
+    U = _dev(U0)
+    p.run_(U, nsteps, dt)
+    G = U.cpu().numpy()
+    assert rel_l2(G[0], R[0]) < 1e-6
+    assert rel_l2(G[3], R[3]) < 1e-6
+    tol = {"fp64": 1e-4, "fp32": 1e-3, "bf16x3": 2e-2}[prec]
+    assert rel_l2(G[1:3], R[1:3]) < tol, rel_l2(G[1:3], R[1:3])
+    assert p.status() == 0
+
+
+def test_lgl_filter_in_step(cuda_device):
+    n, nsteps, dt = 33, 20, 1e-4
+    fp = {"enabled": True, "p": 8, "alpha": 36.0, "interval": 3}
+    U0 = _pulse(n, n, amp=0.2, width2=0.05)
+    s = L.LGLSolver2D(n, n, gamma=GAMMA, filter_params=fp)
+    R = U0.copy()
+    for _ in range(nsteps):
+        R = s.step(R, dt)
+    p = _plan(n, n, "fp32", filt=fp)
+    U = _dev(U0)
+    for _ in range(nsteps):
+        p.step_(U, dt)
+    G = U.cpu().numpy()
+    assert max(rel_l2(G[0], R[0]), rel_l2(G[3], R[3])) < 2e-6
+    assert rel_l2(G[1:3], R[1:3]) < 1e-4
+
+
+def test_lgl_cfl_run_vs_oracle(cuda_device):
+    import torch
+    n, t_end = 33, 0.02
+    U0 = _pulse(n, n, amp=0.2, width2=0.05)
+    s = L.LGLSolver2D(n, n, gamma=GAMMA, cfl=0.3)
+    R, t, steps = U0.copy(), 0.0, 0
+    while t < t_end - 1e-12:
+        dt = min(s.compute_dt(R), t_end - t)
+        R = s.step(R, dt)
+        t += dt
+        steps += 1
+    p = _plan(n, n, "fp32", cfl=0.3)
+    U = _dev(U0)
+    tt = torch.zeros(1, dtype=torch.float64, device="cuda")
+    te = torch.full((1,), t_end, dtype=torch.float64, device="cuda")
+    p.run_cfl_(U, steps + 3, tt, te)
+    assert abs(float(tt.item()) - t_end) < 1e-12
+    assert p.steps_done() == [steps]
+    G = U.cpu().numpy()
+    assert max(rel_l2(G[0], R[0]), rel_l2(G[3], R[3])) < 2e-6
+    assert rel_l2(G[1:3], R[1:3]) < 1e-4
+
+
+def test_lgl_batch_matches_alone(cuda_device):
+    import torch
+    n, nsteps, dt = 41, 10, 2e-5
+    states = [_pulse(n, n, amp=a, width2=w) for a, w in ((0.01, 0.01), (0.1, 0.02), (0.05, 0.05))]
+    pb = _plan(n, n, "fp32", nsolve=3)
+    Ub = _dev(np.stack(states))
+    pb.run_(Ub, nsteps, dt)
+    for i, st in enumerate(states):
+        p1 = _plan(n, n, "fp32")
+        U1 = _dev(st)
+        p1.run_(U1, nsteps, dt)
+        assert torch.equal(U1, Ub[i]), i
+
+
+def test_lgl_properties_257(cuda_device):
+    """Config-size grid (257 x 257, 50 steps of dt = 1e-5): mass is conserved
+    to the quadrature accuracy, the pulse stays symmetric under x <-> y, the
+    walls hold and nothing becomes non-finite."""
+    import torch
+    n = 257
+    p = _plan(n, n, "bf16x3")
+    U0 = _pulse(n, n)
+    U = _dev(U0)
+    p.run_(U, 50, 1e-5)
+    G = U.cpu().numpy()
+    assert np.isfinite(G).all()
+    w = L.LGLAxis(n, 2.0).w_ref
+    W = np.outer(w, w)
+    m0, m1 = (W * U0[0]).sum(), (W * G[0].astype(np.float64)).sum()
+    assert abs(m1 - m0) / m0 < 1e-6
+    assert np.abs(G[0] - G[0].T).max() < 1e-5
+    assert np.abs(G[1] - G[2].T).max() < 1e-5
+    np.testing.assert_array_equal(G[1][:, 0], 0.0)
+    np.testing.assert_array_equal(G[2][0, :], 0.0)
+    assert p.status() == 0
+    del torch

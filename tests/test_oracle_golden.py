@@ -94,3 +94,39 @@ def test_separable_rewrite_is_exact():
                     y = one.deriv(y, 0) if a == b else one.filt(y)
                     y = np.moveaxis(y, -1, b)
                 assert rel_l2(y, box.deriv(x, a)) < 1e-12
+
+
+@pytest.mark.parametrize("nx,ny", [(17, 17), (33, 17)])
+def test_lgl_oracle_matches_reference(nx, ny):
+    """LGL x LGL acoustic pulse with walls: nodes, D matrices, the rhs (with
+    walls applied first), steps and the CFL dt against the reference's torch
+    float64 backend."""
+    from oracle import lgl as L
+    z = golden(f"lgl2d_{nx}x{ny}.npz")
+    s = L.LGLSolver2D(nx, ny, 2.0, 2.0, gamma=1.4)
+    np.testing.assert_allclose(s.ax.x, z["x"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(s.ay.x, z["y"], rtol=0, atol=1e-14)
+    assert np.abs(s.ax.D - z["Dx"]).max() <= 1e-12 * np.abs(z["Dx"]).max()
+    assert np.abs(s.ay.D - z["Dy"]).max() <= 1e-12 * np.abs(z["Dy"]).max()
+    U0 = problems.acoustic_pulse_lgl_2d(z["x"] - 1.0, z["y"] - 1.0, gamma=1.4, amp=float(z["amp"]),
+                                        width2=float(z["width2"]))
+    np.testing.assert_allclose(U0, z["U0"], rtol=0, atol=1e-15)
+    assert rel_l2(s.rhs(U0.copy()), z["rhs0"]) < 1e-12
+    U = U0.copy()
+    for _ in range(int(z["nsteps"])):
+        U = s.step(U, float(z["dt"]))
+    for c in range(4):
+        assert rel_l2(U[c], z["U"][c]) < 1e-13, c
+    assert abs(s.compute_dt(U0) - float(z["dt_cfl0"])) <= 1e-14 * float(z["dt_cfl0"])
+
+
+def test_lgl_filter_preserves_low_modes():
+    """The nodal filter keeps constants and linear functions (sigma_0 = 1,
+    sigma_1 = exp(-alpha/(n-1)^p) ~ 1) and damps the top mode by e^-alpha."""
+    from oracle import lgl as L
+    ax = L.LGLAxis(33, 2.0)
+    F = ax.nodal_filter(8, 36.0)
+    one = np.ones(33)
+    np.testing.assert_allclose(F @ one, one, atol=1e-13)
+    top = ax.V[:, -1]
+    assert np.linalg.norm(F @ top) < 1e-14 * np.linalg.norm(top) + np.exp(-36.0) * np.linalg.norm(top) * 2
