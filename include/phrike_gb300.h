@@ -38,7 +38,9 @@ extern "C" {
 /* arithmetic of the LGL differentiation-matrix contractions */
 #define PS_GEMM_FP32 0   /* float32 operands, float32 accumulate                 */
 #define PS_GEMM_FP64 1   /* float64 operands and accumulate (flux in float64)     */
-#define PS_GEMM_BF16X3 2 /* split bf16: hi*hi + hi*lo + lo*hi, float32 accumulate */
+#define PS_GEMM_BF16X3 2 /* split bf16: hi*hi + hi*lo + lo*hi, float32 accumulate,
+                            on tcgen05 tensor cores                              */
+#define PS_GEMM_BF16X3_SIMT 3 /* the same split arithmetic on CUDA cores (for checks) */
 
 typedef struct ps_plan_s* ps_plan;
 

@@ -21,7 +21,9 @@ PS_EQ_EULER = 0
 PS_GEMM_FP32 = 0
 PS_GEMM_FP64 = 1
 PS_GEMM_BF16X3 = 2
-GEMM_PRECISIONS = {"fp32": PS_GEMM_FP32, "fp64": PS_GEMM_FP64, "bf16x3": PS_GEMM_BF16X3}
+PS_GEMM_BF16X3_SIMT = 3
+GEMM_PRECISIONS = {"fp32": PS_GEMM_FP32, "fp64": PS_GEMM_FP64, "bf16x3": PS_GEMM_BF16X3,
+                   "bf16x3_simt": PS_GEMM_BF16X3_SIMT}
 KIND_NAMES = ["x_pass", "y_pass", "last_pass", "op_pass", "step1d", "lgl_x", "lgl_y"]
 
 

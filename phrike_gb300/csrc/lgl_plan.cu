@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "lgl.cuh"
+#include "lgl_tc.cuh"
 #include "plan.cuh"
 #include "reduce.cuh"
 
@@ -28,7 +29,11 @@ int cfail(cudaError_t e, const char* what) { return errorf(PS_ERR_CUDA, "%s: %s"
     if (_e != cudaSuccess) return cfail(_e, what); \
   } while (0)
 
-int mode_of(const ps_plan_s* p) { return (p->gemm == PS_GEMM_FP64) ? 1 : (p->gemm == PS_GEMM_BF16X3) ? 2 : 0; }
+// arithmetic of the CUDA-core kernels (split bf16 for both bf16x3 modes)
+int mode_of(const ps_plan_s* p) {
+  return (p->gemm == PS_GEMM_FP64) ? 1 : (p->gemm == PS_GEMM_BF16X3 || p->gemm == PS_GEMM_BF16X3_SIMT) ? 2 : 0;
+}
+bool tensor_cores(const ps_plan_s* p) { return p->gemm == PS_GEMM_BF16X3; }
 
 // axis index of the LGL tables: 0 = x (n[0]), 1 = y (n[1])
 const void* dmat(const ps_plan_s* p, int a) {
@@ -68,9 +73,88 @@ LglStageArgs stage_args(ps_plan p, const float* in, int stage, const float* Un, 
 // accumulator and their writes as the stage needs them)
 double field_bytes(const ps_plan_s* p) { return 4.0 * p->cells * p->nsolve; }
 
+// One stage on the tensor cores: split flux planes, the two split-bf16 x3
+// contractions (x: all solves and components stacked as rows; y: one batch
+// entry per solve and component), then the elementwise update.
+int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, double dt, const double* d_dt,
+             const int* act, cudaStream_t s) {
+  const int nx = p->n[0], ny = p->n[1];
+  float* Gx = p->G;
+  float* Gy = p->G + 4 * p->cells * p->nsolve;
+  {
+    FluxSplitArgs f{};
+    f.U = in;
+    f.fx = p->FX;
+    f.fyt = p->FYT;
+    f.nx = nx;
+    f.ny = ny;
+    f.px = p->pitch[0];
+    f.py = p->pitch[1];
+    f.nsolve = p->nsolve;
+    f.gamma = (float)p->desc.gamma;
+    f.eref = p->eref;
+    f.active = act;
+    ProfScope prof(p, s, PS_KIND_OP, (4.0 + 8.0) * field_bytes(p));
+    LGL_CU(launch_flux_split(f, s), "LGL split fluxes");
+  }
+  {
+    UmmaArgs g{};
+    g.C = Gx;
+    g.ldc = nx;
+    g.cz = 0;
+    g.M = p->nsolve * 4 * ny;
+    g.N = nx;
+    g.K = nx;
+    g.batch = 1;
+    g.alpha = 1.0f;
+    g.zper = 1;
+    g.status = p->status;
+    ProfScope prof(p, s, PS_KIND_LGL_X, 8.0 * field_bytes(p));
+    LGL_CU(launch_umma_x3(p->map_FX, p->map_Dx, g, p->nt_x, s), "LGL x contraction (tensor cores)");
+  }
+  {
+    UmmaArgs g{};
+    g.C = Gy;
+    g.ldc = nx;
+    g.cz = p->cells;
+    g.M = ny;
+    g.N = nx;
+    g.K = ny;
+    g.batch = p->nsolve * 4;
+    g.b_batched = 1;
+    g.active = act;
+    g.zper = 4;
+    g.alpha = 1.0f;
+    g.status = p->status;
+    ProfScope prof(p, s, PS_KIND_LGL_Y, 8.0 * field_bytes(p));
+    LGL_CU(launch_umma_x3(p->map_Dy, p->map_FYT, g, p->nt_y, s), "LGL y contraction (tensor cores)");
+  }
+  LglUpdateArgs u{};
+  u.Gx = Gx;
+  u.Gy = Gy;
+  u.Un = Un;
+  u.acc = p->acc;
+  u.out = out;
+  u.cells = p->cells;
+  u.nsolve = p->nsolve;
+  u.stage = st;
+  u.dt_dev = d_dt;
+  u.dt = dt;
+  u.gamma = (float)p->desc.gamma;
+  u.rho_min = 1e-8f;
+  u.p_min = 1e-10f;
+  u.eref = p->eref;
+  u.active = act;
+  const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
+  ProfScope prof(p, s, PS_KIND_LAST, words * field_bytes(p));
+  LGL_CU(launch_lgl_update(u, s), "LGL stage update");
+  return PS_OK;
+}
+
 int stage(ps_plan p, float* in, int st, float* Un, float* out, double dt, const double* d_dt, const int* act,
           cudaStream_t s) {
   LGL_CU(launch_lgl_bc(in, p->n[0], p->n[1], p->ss(4), p->nsolve, act, s), "LGL walls");
+  if (tensor_cores(p)) return stage_tc(p, in, st, Un, out, dt, d_dt, act, s);
   const LglStageArgs a = stage_args(p, in, st, Un, out, dt, d_dt, act);
   {
     ProfScope prof(p, s, PS_KIND_LGL_X, 8.0 * field_bytes(p));
@@ -159,17 +243,23 @@ int lgl_validate(const ps_plan_desc* d) {
   }
   if (!(d->gamma > 1.0)) return errorf(PS_ERR_INVALID, "gamma must exceed 1");
   if (d->filter_interval < 1) return errorf(PS_ERR_INVALID, "filter_interval must be >= 1");
-  if (d->gemm_precision < PS_GEMM_FP32 || d->gemm_precision > PS_GEMM_BF16X3)
-    return errorf(PS_ERR_INVALID, "gemm_precision must be PS_GEMM_FP32, PS_GEMM_FP64 or PS_GEMM_BF16X3");
+  if (d->gemm_precision < PS_GEMM_FP32 || d->gemm_precision > PS_GEMM_BF16X3_SIMT)
+    return errorf(PS_ERR_INVALID,
+                  "gemm_precision must be PS_GEMM_FP32, PS_GEMM_FP64, PS_GEMM_BF16X3 or PS_GEMM_BF16X3_SIMT");
   return PS_OK;
 }
 
-size_t lgl_scratch_bytes(const ps_plan_desc* d) {
+size_t lgl_scratch_bytes(const ps_plan_desc* d, int nsolve) {
   size_t b = 0;
   for (int a = 0; a < 2; ++a) {
     const size_t n = (size_t)d->n[a];
     b += 16 * n + 12 * n * n;                 // nodes, weights, D in float64 and float32
     if (d->filter_enabled) b += 12 * n * n;  // filter matrices
+  }
+  if (d->gemm_precision == PS_GEMM_BF16X3) {
+    const size_t nx = d->n[0], ny = d->n[1], px = (nx + 7) / 8 * 8, py = (ny + 7) / 8 * 8;
+    b += 4 * (nx * px + ny * py);                             // split D planes
+    b += 4 * 4 * (size_t)nsolve * (ny * px + nx * py);       // split flux planes
   }
   return b;
 }
@@ -199,6 +289,38 @@ int lgl_setup(ps_plan p) {
     for (int j = 0; j + 1 < n; ++j) hmin = fmin(hmin, x[j + 1] - x[j]);  // grid.py:826-832
   }
   p->lgl_hmin = hmin;
+  if (p->gemm == PS_GEMM_BF16X3) {
+    const int nx = p->n[0], ny = p->n[1];
+    p->pitch[0] = (nx + 7) / 8 * 8;
+    p->pitch[1] = (ny + 7) / 8 * 8;
+    for (int a = 0; a < 2; ++a) {
+      const int n = p->n[a];
+      unsigned short* q = nullptr;  // bf16 storage
+      if ((rc = plan_alloc(p, &q, 2 * (size_t)n * p->pitch[a])) != PS_OK) return rc;
+      LGL_CU(cudaMemset(q, 0, sizeof(unsigned short) * 2 * (size_t)n * p->pitch[a]), "split D clear");
+      LGL_CU(launch_split_matrix(p->D32[a], n, n, p->pitch[a], q, 0), "split D");
+      p->Dsplit[a] = q;
+    }
+    unsigned short* fx = nullptr;
+    unsigned short* fyt = nullptr;
+    const size_t nfx = 2 * (size_t)p->nsolve * 4 * ny * p->pitch[0];
+    const size_t nfy = 2 * (size_t)p->nsolve * 4 * nx * p->pitch[1];
+    if ((rc = plan_alloc(p, &fx, nfx)) != PS_OK) return rc;
+    if ((rc = plan_alloc(p, &fyt, nfy)) != PS_OK) return rc;
+    LGL_CU(cudaMemset(fx, 0, sizeof(unsigned short) * nfx), "flux planes clear");
+    LGL_CU(cudaMemset(fyt, 0, sizeof(unsigned short) * nfy), "flux planes clear");
+    p->FX = fx;
+    p->FYT = fyt;
+    p->nt_x = umma_n_tile(nx);
+    p->nt_y = umma_n_tile(nx);
+    int e = 0;
+    if ((e = encode_split_map(&p->map_FX, p->FX, nx, p->nsolve * 4 * ny, 1, p->pitch[0], 128)) != 0 ||
+        (e = encode_split_map(&p->map_Dx, p->Dsplit[0], nx, nx, 1, p->pitch[0], p->nt_x)) != 0 ||
+        (e = encode_split_map(&p->map_Dy, p->Dsplit[1], ny, ny, 1, p->pitch[1], 128)) != 0 ||
+        (e = encode_split_map(&p->map_FYT, p->FYT, ny, nx, p->nsolve * 4, p->pitch[1], p->nt_y)) != 0)
+      return errorf(PS_ERR_CUDA, "tensor map encoding for the split contractions failed (%d)", e);
+    LGL_CU(cudaDeviceSynchronize(), "split tables");
+  }
   return PS_OK;
 }
 

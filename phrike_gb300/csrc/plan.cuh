@@ -64,9 +64,14 @@ struct ps_plan_s {
   float* D32[2] = {nullptr, nullptr};
   double* F64[2] = {nullptr, nullptr};    // nodal filter matrices (filter on)
   float* F32[2] = {nullptr, nullptr};
-  void* Dsplit[2] = {nullptr, nullptr};   // split-bf16 hi/lo pairs of D (bf16x3)
-  void* Fsplit[2] = {nullptr, nullptr};
   double lgl_hmin = 0.0;                  // smallest node spacing (CFL)
+  // tensor-core split-bf16 contractions: hi/lo planes and their TMA maps
+  int pitch[2] = {0, 0};                  // bf16 row pitch along x / y (multiple of 8)
+  void* Dsplit[2] = {nullptr, nullptr};   // [2][n][pitch] of D_x, D_y
+  void* FX = nullptr;                     // [2][nsolve*4*ny][pitch_x] x flux
+  void* FYT = nullptr;                    // [2][nsolve*4][nx][pitch_y] transposed y flux
+  CUtensorMap map_FX{}, map_Dx{}, map_Dy{}, map_FYT{};
+  int nt_x = 0, nt_y = 0;                 // N tiles of the two contractions
 
   ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
   long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
@@ -138,7 +143,7 @@ int plan_alloc(ps_plan p, Tp** ptr, size_t count) {
 
 // LGL x LGL plans (lgl_plan.cu)
 int lgl_validate(const ps_plan_desc* d);
-size_t lgl_scratch_bytes(const ps_plan_desc* d);
+size_t lgl_scratch_bytes(const ps_plan_desc* d, int nsolve);
 int lgl_setup(ps_plan p);
 int lgl_rhs(ps_plan p, const float* U, float* rhs, cudaStream_t s);
 int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,

@@ -543,7 +543,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   for (int a = 0; a < d->ndim; ++a) cells *= d->n[a];
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
-  if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d);
+  if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
   *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }

@@ -50,7 +50,7 @@ def test_lgl_build_matches_oracle(cuda_device, n):
     x, w, D = lgl_build(n, 2.0)
     ax = L.LGLAxis(n, 2.0)
     np.testing.assert_allclose(x.cpu().numpy(), ax.x, rtol=0, atol=4e-16 * n)
-    np.testing.assert_allclose(w.cpu().numpy(), ax.w_ref, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(w.cpu().numpy(), ax.w_ref, rtol=2e-12, atol=0)
     Dg = D.cpu().numpy()
     assert np.abs(Dg - ax.D).max() <= 1e-10 * np.abs(ax.D).max()
     # derivative of a cubic is exact on n >= 4 nodes
