@@ -366,9 +366,107 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_lgl(args):
+    """Precision on dense collocation: the LGL x LGL acoustic pulse (rho = 1 +
+    0.01 exp(-r^2/0.01), p = rho^gamma/gamma, u = v = 0 on [-1, 1]^2, walls),
+    RK4 with dt = 1e-5 for --lgl-steps steps, per contraction precision: time
+    per step and the relative L2 error per conserved field against the
+    float64 oracle, which runs here on the host cores (its time is the CPU
+    baseline).  The error is given from the float64 initial state (what a
+    float32-state run can reach) and from the float32-rounded one (the
+    contraction precision alone)."""
+    import torch
+    from oracle import lgl as L
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.engine import Plan
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    nsteps, dt = args.lgl_steps, 1e-5
+    precs = ["fp64", "fp32", "bf16x3"]
+    peaks = {}
+    try:
+        with open(PEAKS_FILE) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    table = []
+    headline = None
+    threads = os.cpu_count() or 1
+    for n in [int(x) for x in args.lgl_sizes.split(",")]:
+        ax = L.LGLAxis(n, 2.0)
+        U0 = problems.acoustic_pulse_lgl_2d(ax.x - 1.0, ax.x - 1.0, gamma=1.4)
+        s = L.LGLSolver2D(n, n, gamma=1.4)
+        R = U0.copy()
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            R = s.step(R, dt)
+        cpu_s = time.perf_counter() - t0
+        s32 = L.LGLSolver2D(n, n, gamma=1.4)
+        R32 = U0.astype(np.float32).astype(np.float64)
+        for _ in range(nsteps):
+            R32 = s32.step(R32, dt)
+        row = {"n": n, "cells": n * n, "steps": nsteps, "cpu_oracle_s_per_step": cpu_s / nsteps,
+               "cpu_oracle_cell_updates_per_s": n * n * nsteps / cpu_s, "cpu_threads": threads}
+        for prec in precs:
+            plan = Plan((n, n), (2.0, 2.0), gamma=1.4, basis="legendre", gemm_precision=prec, device=device)
+            Uw = torch.as_tensor(U0, dtype=torch.float32, device=device).contiguous()
+            plan.run_(Uw, 3, dt)  # warm-up
+            U = torch.as_tensor(U0, dtype=torch.float32, device=device).contiguous()
+            torch.cuda.synchronize()
+            st = torch.cuda.current_stream(device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            plan.run_(U, nsteps, dt)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / nsteps
+            G = U.cpu().numpy().astype(np.float64)
+
+            def rl(a, b):
+                return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+            ent = {"ms_per_step": ms, "cell_updates_per_s": n * n / (ms * 1e-3),
+                   "rel_l2_vs_f64_ic": {"rho": rl(G[0], R[0]), "mom": rl(G[1:3], R[1:3]), "E": rl(G[3], R[3])},
+                   "rel_l2_vs_f32_ic": {"rho": rl(G[0], R32[0]), "mom": rl(G[1:3], R32[1:3]),
+                                        "E": rl(G[3], R32[3])},
+                   "status": plan.status()}
+            if prec == "bf16x3":
+                # contraction kernels alone: issued split-bf16 flops per launch / event time
+                plan.profile(True)
+                Up = torch.as_tensor(U0, dtype=torch.float32, device=device).contiguous()
+                plan.run_(Up, 5, dt)
+                prof = plan.collect_profile()
+                plan.profile(False)
+                fl_x = 3 * 2.0 * (4 * n) * n * n
+                fl_y = 3 * 2.0 * 4 * n * n * n
+                for kind, fl in (("lgl_x", fl_x), ("lgl_y", fl_y)):
+                    if kind in prof:
+                        per = prof[kind]["ms"] / prof[kind]["launches"]
+                        ent[f"{kind}_us"] = per * 1e3
+                        ent[f"{kind}_tflops_issued"] = fl / (per * 1e-3) / 1e12
+                        ent[f"{kind}_tensor_frac_of_measured_bf16"] = fl / (per * 1e-3) / 1e12 / tc_peak
+                headline = ent["cell_updates_per_s"]
+            row[prec] = ent
+            plan.close()
+        table.append(row)
+    line = {
+        "metric": "LGL 2D acoustic pulse: cell-updates/s and rel-L2 vs float64 oracle per contraction precision",
+        "value": headline, "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (analytic acoustic pulse initial condition)",
+        "config": {"workload": f"LGL x LGL acoustic pulse, walls, RK4 dt=1e-5, {nsteps} steps, "
+                               f"sizes {args.lgl_sizes}; value = bf16x3 at the last size"},
+        "table": table,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["tgv", "ensemble"], default="tgv")
+    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl"], default="tgv")
+    ap.add_argument("--lgl-sizes", default="257,513")
+    ap.add_argument("--lgl-steps", type=int, default=500)
     ap.add_argument("--nsolve", type=int, default=512)
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--chunk", type=int, default=50)
@@ -392,6 +490,9 @@ def main():
         if args.workload == "ensemble":
             if rank == 0:
                 run_ensemble(args)
+        elif args.workload == "lgl":
+            if rank == 0:
+                run_lgl(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:

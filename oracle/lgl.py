@@ -113,7 +113,7 @@ class LGLSolver2D:
         return f @ self.ax.D.T
 
     def dy(self, f):
-        return np.einsum("jk,...ki->...ji", self.ay.D, f)
+        return np.matmul(self.ay.D, f)  # D_y applied along the second-to-last axis
 
     def rhs(self, U: np.ndarray) -> np.ndarray:
         """Applies the BCs to U in place first, like _compute_rhs_2d."""
@@ -141,7 +141,7 @@ class LGLSolver2D:
         Un = self.clamp(U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4))
         if self.step_counter % self.interval == 0:
             if self.filter:
-                Un = np.einsum("jk,...ki->...ji", self.Fy, Un @ self.Fx.T)
+                Un = np.matmul(self.Fy, Un @ self.Fx.T)
             apply_wall_bc(Un)
         self.step_counter += 1
         return Un

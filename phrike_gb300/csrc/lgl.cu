@@ -508,7 +508,11 @@ __global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
         r = idx % BMg;
       }
       const int m = m0 + r, k = k0 + c;
-      const TC va = (m < g.M && k < g.K) ? (TC)A[m * g.am + k * g.ak] : TC(0);
+      TC va = TC(0);
+      if (m < g.M && k < g.K) {
+        va = (TC)A[m * g.am + k * g.ak];
+        if (g.offset == 1) va -= (TC)A[m * g.am];
+      }
       split_store<MODE, TC>(&As[0][c][r], &As[NS - 1][c][r], va);
       if (BK) {
         r = idx / BKg;
@@ -518,7 +522,11 @@ __global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
         r = idx % BNg;
       }
       const int n = n0 + r, k2 = k0 + c;
-      const TC vb = (n < g.N && k2 < g.K) ? (TC)Bm[n * g.bn + k2 * g.bk] : TC(0);
+      TC vb = TC(0);
+      if (n < g.N && k2 < g.K) {
+        vb = (TC)Bm[n * g.bn + k2 * g.bk];
+        if (g.offset == 2) vb -= (TC)Bm[n * g.bn];
+      }
       split_store<MODE, TC>(&Bs[0][c][r], &Bs[NS - 1][c][r], vb);
     }
     __syncthreads();
@@ -543,10 +551,13 @@ __global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
   for (int i = 0; i < 4; ++i) {
     const int m = m0 + ty + 16 * i;
     if (m >= g.M) continue;
+    const TC base_a = (g.add_back && g.offset == 1) ? (TC)A[m * g.am] : TC(0);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int n = n0 + tx + 16 * j;
-      if (n < g.N) C[m * g.cm + n * g.cn] = (float)((TC)g.alpha * acc[i][j]);
+      if (n >= g.N) continue;
+      const TC base = (g.add_back && g.offset == 2) ? (TC)Bm[n * g.bn] : base_a;
+      C[m * g.cm + n * g.cn] = (float)((TC)g.alpha * acc[i][j] + base);
     }
   }
 }

@@ -19,6 +19,14 @@ struct GemmArgs {
   float alpha;
   const int* active;  // nullable: batch entry z is skipped when active[z / zper] == 0
   int zper;
+  // Pencil offset: 1 subtracts A[m][0] from row m of A, 2 subtracts B[n][0]
+  // from row n of B, before the product (exact for a matrix that annihilates
+  // constants, such as a differentiation matrix, and it keeps the rounding of
+  // the operand relative to its variation, not its size); add_back adds the
+  // subtracted value to the output (for a matrix that preserves constants,
+  // such as the nodal filter).
+  int offset;
+  int add_back;
 };
 
 // Operand storage / arithmetic of the generic contraction

@@ -207,7 +207,11 @@ int contract(ps_plan p, int axis, bool filter, const float* f, float* out, long 
     if (p->gemm == PS_GEMM_FP64) kind = kGemmF64F32;
   }
   g.cm = nx, g.cn = 1, g.cz = cells;
-  if (p->gemm == PS_GEMM_BF16X3) kind = kGemmSplitAB;
+  // subtract each pencil's first value from the field operand (x pencils are
+  // rows of A, y pencils rows of B); D annihilates it, the filter keeps it
+  g.offset = (axis == 0) ? 1 : 2;
+  g.add_back = filter ? 1 : 0;
+  if (p->gemm == PS_GEMM_BF16X3 || p->gemm == PS_GEMM_BF16X3_SIMT) kind = kGemmSplitAB;
   for (long z0 = 0; z0 < Z; z0 += 65535) {  // grid.z limit
     GemmArgs gz = g;
     gz.batch = (int)((Z - z0 < 65535) ? Z - z0 : 65535);

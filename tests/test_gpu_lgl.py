@@ -1,14 +1,17 @@
 """LGL x LGL (2D Legendre-Gauss-Lobatto) path on the GPU against the oracle
 and the reference's golden vectors: device construction of nodes, weights
 and differentiation matrices (float64), walls, derivatives, filter, the
-right-hand side and RK4 steps in the three contraction precisions, CFL runs
-and batches.
+right-hand side and RK4 steps in every contraction precision, CFL runs and
+batches.
 
-Tolerances: the state is float32, so a right-hand side carries the float32
-rounding of the flux amplified by the O(N^2) norm of D at the walls; states
-after steps are compared with relative L2 per conserved field.  The split
-bf16 contraction keeps about 16 significand bits of each operand, so its
-rhs tolerance is wider.
+Tolerances.  The state is float32, so even float64 contractions see the
+float32 rounding of the input state (notably of E ~ 1.8 for the acoustic
+pulse), amplified at the walls by the O(N^2) norm of D: that floor is about
+3e-6 relative on the momentum right-hand side of the 17- and 33-point
+fixtures.  Split bf16 x3 keeps about 16 significand bits of each operand, so
+its momentum right-hand side sits near 2e-5.  The tensor-core and CUDA-core
+forms of the split arithmetic differ only in float32 accumulation order
+(about 2e-6 relative at 513 points).
 """
 import numpy as np
 import pytest
@@ -20,8 +23,8 @@ from phrike_gb300 import problems
 pytestmark = pytest.mark.gpu
 
 GAMMA = 1.4
-RHS_TOL = {"fp64": 2e-6, "fp32": 3e-4, "bf16x3": 3e-3}
-STEP_TOL = {"fp64": 2e-7, "fp32": 2e-6, "bf16x3": 2e-5}
+PRECS = ["fp32", "fp64", "bf16x3", "bf16x3_simt"]
+RHS_TOL = {"fp64": 1e-5, "fp32": 1e-5, "bf16x3": 6e-5, "bf16x3_simt": 6e-5}
 
 
 def _plan(nx, ny, prec="fp32", nsolve=1, filt=None, cfl=0.3):
@@ -68,27 +71,32 @@ def test_lgl_walls_match_oracle(cuda_device):
     np.testing.assert_array_equal(t.cpu().numpy(), L.apply_wall_bc(U.astype(np.float32).copy()))
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_lgl_derivatives_and_filter(cuda_device, prec):
+    """dx1/dy1 and the nodal filter against the oracle applied to the same
+    float32 inputs; one field carries a large constant offset (the pencil
+    offset keeps its derivative accurate in the split modes)."""
     nx, ny = 65, 33
-    rng = np.random.default_rng(3)
     ax, ay = L.LGLAxis(nx, 2.0), L.LGLAxis(ny, 2.0)
     X, Y = np.meshgrid(ax.x - 1.0, ay.x - 1.0, indexing="xy")
-    f = np.stack([np.sin(2 * X) * np.cos(3 * Y), np.exp(X * Y), X ** 5 - Y ** 3, rng.standard_normal(X.shape)])
+    f = np.stack([np.sin(2 * X) * np.cos(3 * Y), np.exp(X * Y), X ** 5 - Y ** 3,
+                  1.0 + 0.01 * np.exp(-(X ** 2 + Y ** 2) / 0.05)]).astype(np.float32)
+    f64 = f.astype(np.float64)
     p = _plan(nx, ny, prec, filt={"enabled": True, "p": 8, "alpha": 36.0})
-    tol = {"fp64": 1e-7, "fp32": 2e-6, "bf16x3": 5e-5}[prec]
+    tol = {"fp64": 1e-7, "fp32": 3e-5, "bf16x3": 3e-3, "bf16x3_simt": 3e-3}[prec]
     dx = p.derivative(_dev(f), 0).cpu().numpy()
     dy = p.derivative(_dev(f), 1).cpu().numpy()
-    ref_dx = f @ ax.D.T
-    ref_dy = np.einsum("jk,cki->cji", ay.D, f)
+    ref_dx = f64 @ ax.D.T
+    ref_dy = np.einsum("jk,cki->cji", ay.D, f64)
     for c in range(4):
-        assert rel_l2(dx[c], ref_dx[c]) < tol * 30, (c, rel_l2(dx[c], ref_dx[c]))
-        assert rel_l2(dy[c], ref_dy[c]) < tol * 30, (c, rel_l2(dy[c], ref_dy[c]))
+        assert rel_l2(dx[c], ref_dx[c]) < tol, (c, rel_l2(dx[c], ref_dx[c]))
+        assert rel_l2(dy[c], ref_dy[c]) < tol, (c, rel_l2(dy[c], ref_dy[c]))
     Fx, Fy = ax.nodal_filter(8, 36.0), ay.nodal_filter(8, 36.0)
     ff = p.filter(_dev(f)).cpu().numpy()
-    ref = np.einsum("jk,cki->cji", Fy, f @ Fx.T)
+    ref = np.einsum("jk,cki->cji", Fy, f64 @ Fx.T)
+    ftol = {"fp64": 1e-7, "fp32": 1e-6, "bf16x3": 3e-5, "bf16x3_simt": 3e-5}[prec]
     for c in range(4):
-        assert rel_l2(ff[c], ref[c]) < tol, (c, rel_l2(ff[c], ref[c]))
+        assert rel_l2(ff[c], ref[c]) < ftol, (c, rel_l2(ff[c], ref[c]))
     # in-place derivative
     g = _dev(f)
     p.derivative(g, 1, out=g)
@@ -96,28 +104,55 @@ def test_lgl_derivatives_and_filter(cuda_device, prec):
 
 
 @pytest.mark.parametrize("nx,ny", [(17, 17), (33, 17)])
-@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_lgl_rhs_and_steps_match_reference(cuda_device, nx, ny, prec):
     z = golden(f"lgl2d_{nx}x{ny}.npz")
     p = _plan(nx, ny, prec)
     U0 = _dev(z["U0"])
     rhs = p.rhs(U0).cpu().numpy()
-    errs = _field_errors(rhs, z["rhs0"])
-    # momentum rhs compared as a vector field
-    mom = rel_l2(rhs[1:3], z["rhs0"][1:3])
-    assert max(errs[0], mom, errs[3]) < RHS_TOL[prec], errs
+    # momentum compared as a vector field; density and energy per field
+    errs = [rel_l2(rhs[0], z["rhs0"][0]), rel_l2(rhs[1:3], z["rhs0"][1:3]), rel_l2(rhs[3], z["rhs0"][3])]
+    assert max(errs) < RHS_TOL[prec], errs
     np.testing.assert_array_equal(U0.cpu().numpy(), z["U0"].astype(np.float32))  # rhs leaves U alone
     U = _dev(z["U0"])
     p.run_(U, int(z["nsteps"]), float(z["dt"]))
-    errs = _field_errors(U.cpu().numpy(), z["U"])
-    mom = rel_l2(U.cpu().numpy()[1:3], z["U"][1:3])
-    assert max(errs[0], mom, errs[3]) < STEP_TOL[prec], errs
+    G = U.cpu().numpy()
+    assert max(rel_l2(G[0], z["U"][0]), rel_l2(G[3], z["U"][3])) < 2e-7
+    assert rel_l2(G[1:3], z["U"][1:3]) < RHS_TOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64", "bf16x3"])
+@pytest.mark.parametrize("n", [17, 65, 257, 513])
+def test_lgl_tensor_cores_match_cuda_core_split(cuda_device, n):
+    """The tcgen05 split-bf16 x3 contractions against the same split
+    arithmetic on CUDA cores, on a state with a velocity field that vanishes
+    at the walls: they differ only in float32 accumulation order."""
+    ax = L.LGLAxis(n, 2.0)
+    x = ax.x - 1.0
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    rho = 1.0 + 0.2 * np.exp(-(X ** 2 + Y ** 2) / 0.05)
+    u = 0.3 * np.sin(np.pi * X) * np.cos(0.5 * np.pi * Y)
+    v = -0.2 * np.cos(0.5 * np.pi * X) * np.sin(np.pi * Y)
+    pr = rho ** GAMMA / GAMMA
+    U0 = np.stack([rho, rho * u, rho * v, pr / (GAMMA - 1) + 0.5 * rho * (u * u + v * v)])
+    r_tc = _plan(n, n, "bf16x3").rhs(_dev(U0)).cpu().numpy()
+    r_cc = _plan(n, n, "bf16x3_simt").rhs(_dev(U0)).cpu().numpy()
+    for c in range(4):
+        assert rel_l2(r_tc[c], r_cc[c]) < 1e-5, (c, rel_l2(r_tc[c], r_cc[c]))
+    Ua, Ub = _dev(U0), _dev(U0)
+    pa, pb = _plan(n, n, "bf16x3"), _plan(n, n, "bf16x3_simt")
+    pa.run_(Ua, 5, 1e-5)
+    pb.run_(Ub, 5, 1e-5)
+    Ga, Gb = Ua.cpu().numpy(), Ub.cpu().numpy()
+    for c in range(4):
+        assert rel_l2(Ga[c], Gb[c]) < 1e-6, (c, rel_l2(Ga[c], Gb[c]))
+    assert pa.status() == 0
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_lgl_acoustic_pulse_vs_oracle(cuda_device, prec):
     """The acoustic Gaussian pulse (amplitude 0.01, width^2 0.01) on 65 x 65
-    LGL nodes, 200 steps of dt = 1e-5, against the float64 oracle."""
+    LGL nodes, 200 steps of dt = 1e-5, against the float64 oracle (measured:
+    momentum 2.5e-5 for every precision, the float32-state floor)."""
     n, nsteps, dt = 65, 200, 1e-5
     U0 = _pulse(n, n)
     s = L.LGLSolver2D(n, n, gamma=GAMMA)
@@ -129,9 +164,8 @@ def test_lgl_acoustic_pulse_vs_oracle(cuda_device, prec):
     p.run_(U, nsteps, dt)
     G = U.cpu().numpy()
     assert rel_l2(G[0], R[0]) < 1e-6
-    assert rel_l2(G[3], R[3]) < 1e-6
-    tol = {"fp64": 1e-4, "fp32": 1e-3, "bf16x3": 2e-2}[prec]
-    assert rel_l2(G[1:3], R[1:3]) < tol, rel_l2(G[1:3], R[1:3])
+    assert rel_l2(G[3], R[3]) < 1e-7
+    assert rel_l2(G[1:3], R[1:3]) < 1e-4, rel_l2(G[1:3], R[1:3])
     assert p.status() == 0
 
 
