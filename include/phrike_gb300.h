@@ -34,6 +34,9 @@ extern "C" {
 
 /* equation sets */
 #define PS_EQ_EULER 0
+#define PS_EQ_MHD 1 /* 2D (2.5D) ideal MHD, 8 components [rho, rho u (3), E, B (3)],
+                       periodic Fourier grids (equations.py:770-907,
+                       SpectralSolverMHD, solver.py:840-1049)            */
 
 /* arithmetic of the LGL differentiation-matrix contractions */
 #define PS_GEMM_FP32 0   /* float32 operands, float32 accumulate                 */
@@ -65,6 +68,13 @@ typedef struct {
   double gravity[3];     /* constant gravity (solver.py:82-91); 0 = off       */
   double cfl;            /* CFL number for ps_compute_dt                      */
   int gemm_precision;    /* PS_GEMM_* (LGL grids; ignored for Fourier)        */
+  /* PS_EQ_MHD options (grid.mhd_config of the reference, solver.py:871-880) */
+  double mhd_rho_min;          /* clamp floors (default 1e-10, 1e-12)          */
+  double mhd_p_min;
+  int mhd_project_substages;   /* project B after every RK stage (default 1)   */
+  int mhd_divergence_clean;    /* 1: Helmholtz projection, 0: none (default 1) */
+  double mhd_resistivity;      /* eta; must be 0 (explicit diffusion not built) */
+  double mhd_viscosity;        /* nu;  must be 0                                */
 } ps_plan_desc;
 
 /* Fill a descriptor with the reference defaults for `ndim` (dealias on,
@@ -143,7 +153,10 @@ int ps_max_wave_speed(ps_plan plan, const float* U, float* d_out, void* stream);
 
 /* d_out (device doubles, ncomp values per solve: mass, momenta..., energy) = plain
  * sums of the conserved quantities, accumulated in float64.  Replaces the
- * solvers' record() (solver.py:372-377, 741-767, 1439-1468). */
+ * solvers' record() (solver.py:372-377, 741-767, 1439-1468).  For PS_EQ_MHD
+ * the 8 values per solve are mass, momentum x/y/z, energy, magnetic energy,
+ * cross helicity and 0 (MHDEquations2D.conserved_quantities,
+ * equations.py:889-907). */
 int ps_conserved(ps_plan plan, const float* U, double* d_out, void* stream);
 
 /* LGL nodes, quadrature weights and differentiation matrix of one axis,
@@ -161,6 +174,18 @@ int ps_lgl_build(int n, double length, double* d_nodes, double* d_weights, doubl
  * momentum is zeroed).  A no-op for periodic Fourier plans, like
  * Grid*.apply_boundary_conditions there (grid.py:631-632, 1087-1089). */
 int ps_apply_boundary_conditions(ps_plan plan, float* U, void* stream);
+
+/* Helmholtz (Leray) projection of the in-plane field (Bx, By) in place,
+ * div B = 0 to rounding: the Nyquist row and column are zeroed and
+ * B_hat -= k (k . B_hat)/|k|^2.  Bx and By each hold nsolve fields of the
+ * plan's 2D Fourier grid.  Replaces Grid2D.project_solenoidal
+ * (grid.py:1297-1327). */
+int ps_project_solenoidal(ps_plan plan, float* Bx, float* By, void* stream);
+
+/* The MHD state projection of SpectralSolverMHD._project_B
+ * (solver.py:966-986) in place on U (PS_EQ_MHD plans): B projected, E
+ * recomputed with the thermal pressure held fixed. */
+int ps_project_state(ps_plan plan, float* U, void* stream);
 
 /* Device status word of a plan, read synchronously: 0 = healthy; bit
  * PS_STATUS_TMA_TIMEOUT = a kernel gave up waiting for a tile load (bounded

@@ -1,0 +1,155 @@
+"""CPU oracle for 2D (2.5D) ideal MHD on a periodic Fourier grid.
+
+TEST INFRASTRUCTURE ONLY (see oracle/spectral.py).  Restates, in NumPy
+float64, the reference's MHDEquations2D (phrike/equations.py:770-907), the
+2D Helmholtz (Leray) projection of Grid2D (grid.py:1297-1327) and the RK4
+step of SpectralSolverMHD (solver.py:840-1049) for the ideal case
+(resistivity = viscosity = 0).  Pinned against golden vectors produced by
+running the reference's NumPy path (tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+from typing import Dict, Optional, Tuple
+
+import numpy as np
+
+from .spectral import FourierBox, fftn, ifftn
+
+
+def primitive(U: np.ndarray, gamma: float):
+    """rho, ux, uy, uz, p, Bx, By, Bz; p = (gamma-1)(E - rho|u|^2/2 - |B|^2/2)
+    (equations.py:783-795)."""
+    rho = U[0]
+    ux, uy, uz = U[1] / rho, U[2] / rho, U[3] / rho
+    Bx, By, Bz = U[5], U[6], U[7]
+    kin = 0.5 * rho * (ux * ux + uy * uy + uz * uz)
+    mag = 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    p = (gamma - 1.0) * (U[4] - kin - mag)
+    return rho, ux, uy, uz, p, Bx, By, Bz
+
+
+def conservative(rho, ux, uy, uz, p, Bx, By, Bz, gamma: float) -> np.ndarray:
+    """equations.py:797-810"""
+    E = p / (gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    return np.array([rho, rho * ux, rho * uy, rho * uz, E, Bx, By, Bz])
+
+
+def fluxes(U: np.ndarray, gamma: float) -> Tuple[np.ndarray, np.ndarray]:
+    """Fx, Fy of equations.py:812-872 (E taken from the state)."""
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    E = U[4]
+    uB = ux * Bx + uy * By + uz * Bz
+    ps = p + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    mx, my = rho * ux, rho * uy
+    z = np.zeros_like(rho)
+    Fx = np.array([mx, mx * ux + ps - Bx * Bx, mx * uy - Bx * By, mx * uz - Bx * Bz,
+                   (E + ps) * ux - Bx * uB, z, ux * By - uy * Bx, ux * Bz - uz * Bx])
+    Fy = np.array([my, my * ux - By * Bx, my * uy + ps - By * By, my * uz - By * Bz,
+                   (E + ps) * uy - By * uB, uy * Bx - ux * By, z, uy * Bz - uz * By])
+    return Fx, Fy
+
+
+def max_wave_speed(U: np.ndarray, gamma: float) -> float:
+    """max(|ux|, |uy|) + sqrt(a^2 + b^2) (equations.py:874-887)."""
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    a2 = gamma * p / rho
+    b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+    return float(np.max(np.maximum(np.abs(ux), np.abs(uy)) + np.sqrt(np.maximum(a2 + b2, 0.0))))
+
+
+def conserved_quantities(U: np.ndarray, gamma: float) -> Dict[str, float]:
+    """equations.py:889-907"""
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    b2 = Bx * Bx + By * By + Bz * Bz
+    E = p / (gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * b2
+    return {"mass": float(rho.sum()), "momentum_x": float((rho * ux).sum()),
+            "momentum_y": float((rho * uy).sum()), "momentum_z": float((rho * uz).sum()),
+            "energy": float(E.sum()), "magnetic_energy": float((0.5 * b2).sum()),
+            "cross_helicity": float((ux * Bx + uy * By + uz * Bz).sum())}
+
+
+def project_solenoidal(box: FourierBox, Bx: np.ndarray, By: np.ndarray):
+    """Grid2D.project_solenoidal (grid.py:1297-1327): Nyquist row/column
+    zeroed, then B_hat -= k (k . B_hat) / k^2 (k = 0 kept)."""
+    ny, nx = box.shape
+    Fx = fftn(Bx, (-2, -1))
+    Fy = fftn(By, (-2, -1))
+    for F in (Fx, Fy):
+        if nx % 2 == 0:
+            F[..., :, nx // 2] = 0
+        if ny % 2 == 0:
+            F[..., ny // 2, :] = 0
+    kx = box.k[1][None, :]
+    ky = box.k[0][:, None]
+    k2 = kx * kx + ky * ky
+    k2s = np.where(k2 == 0.0, 1.0, k2)
+    coef = (kx * Fx + ky * Fy) / k2s
+    return ifftn(Fx - kx * coef, (-2, -1)).real, ifftn(Fy - ky * coef, (-2, -1)).real
+
+
+class MHDSolver2D:
+    """SpectralSolverMHD in 2D, ideal, RK4 (solver.py:942-1049): rhs =
+    -(dx1 Fx + dy1 Fy); every stage clamp then project; after the step, at the
+    filter cadence, the spectral filter then the projection."""
+
+    def __init__(self, nx: int, ny: int, lx: float = 2 * np.pi, ly: float = 2 * np.pi, gamma: float = 5.0 / 3.0,
+                 dealias: bool = True, filter_params: Optional[dict] = None, cfl: float = 0.3,
+                 rho_min: float = 1e-10, p_min: float = 1e-12, project_each_substage: bool = True,
+                 divergence_clean: str = "projection"):
+        fp = filter_params or {}
+        self.box = FourierBox((ny, nx), (ly, lx), dealias=dealias, filter_enabled=bool(fp.get("enabled", False)),
+                              filter_p=int(fp.get("p", 8)), filter_alpha=float(fp.get("alpha", 36.0)))
+        self.gamma = gamma
+        self.cfl = cfl
+        self.rho_min, self.p_min = rho_min, p_min
+        self.project_each_substage = project_each_substage
+        self.divergence_clean = divergence_clean
+        self.interval = max(1, int(fp.get("interval", 1) or 1))
+        self.step_counter = 0
+
+    def rhs(self, U: np.ndarray) -> np.ndarray:
+        Fx, Fy = fluxes(U, self.gamma)
+        return -(self.box.deriv(Fx, 1) + self.box.deriv(Fy, 0))
+
+    def clamp(self, U: np.ndarray) -> np.ndarray:
+        """_clamp (solver.py:956-964)"""
+        rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, self.gamma)
+        return conservative(np.maximum(rho, self.rho_min), ux, uy, uz, np.maximum(p, self.p_min), Bx, By, Bz,
+                            self.gamma)
+
+    def project(self, U: np.ndarray) -> np.ndarray:
+        """_project_B (solver.py:966-986): project (Bx, By), recompute E with
+        the thermal pressure held fixed."""
+        if self.divergence_clean == "none":
+            return U
+        rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, self.gamma)
+        Bx, By = project_solenoidal(self.box, U[5], U[6])
+        V = U.copy()
+        V[5], V[6], V[7] = Bx, By, Bz
+        V[4] = p / (self.gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+        return V
+
+    def step(self, U: np.ndarray, dt: float) -> np.ndarray:
+        proj = self.project if self.project_each_substage else (lambda x: x)
+        k1 = self.rhs(U)
+        U2 = proj(self.clamp(U + 0.5 * dt * k1))
+        k2 = self.rhs(U2)
+        U3 = proj(self.clamp(U + 0.5 * dt * k2))
+        k3 = self.rhs(U3)
+        U4 = proj(self.clamp(U + dt * k3))
+        k4 = self.rhs(U4)
+        Un = proj(self.clamp(U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4)))
+        if self.step_counter % self.interval == 0:
+            Un = self.project(self.box.filt(Un))
+        self.step_counter += 1
+        return Un
+
+    def compute_dt(self, U: np.ndarray) -> float:
+        """compute_dt (solver.py:1018-1034), ideal: cfl * min(dx, dy) / max speed."""
+        s = max_wave_speed(U, self.gamma)
+        if s <= 0.0:
+            return 1e-6
+        return self.cfl * min(self.box.spacing) / s
+
+    def max_div_b(self, U: np.ndarray) -> float:
+        return float(np.max(np.abs(self.box.deriv(U[5], 1) + self.box.deriv(U[6], 0))))

@@ -52,7 +52,8 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
     phrike.run_simulation (phrike/__init__.py:14-56).
 
     Problems: "sod" (1D smoothed Sod step), "tgv3d" (3D Taylor-Green vortex),
-    "khi2d" (2D Kelvin-Helmholtz double shear layer).  Config keys follow the
+    "khi2d" (2D Kelvin-Helmholtz double shear layer), "orszag_tang2d" (2D ideal
+    MHD, rho = gamma^2, p = gamma, B0 = 1 on [0, 2 pi)^2 by default).  Config keys follow the
     reference schema: grid.{N|Nx,Ny,Nz, Lx,Ly,Lz, dealias}, physics.gamma,
     integration.{t0, t_end, cfl, scheme, dt, output_interval, spectral_filter},
     initial_conditions.{...}.  integration.dt (fixed step) is an addition.
@@ -99,8 +100,19 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
         eqs = E.EulerEquations2D(gamma=gamma)
         U0 = P.kelvin_helmholtz_2d(Nx, Ny, float(ic.get("U0", 1.0)), float(ic.get("A", 0.01)), gamma)
         solver = S.SpectralSolver2D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.4)))
+    elif name == "orszag_tang2d":
+        N = int(g.get("N", 128))
+        Nx, Ny = int(g.get("Nx", N)), int(g.get("Ny", N))
+        L = float(g.get("Lx", 2.0 * 3.141592653589793))
+        gamma = float(phys.get("gamma", 5.0 / 3.0))
+        grid = G.Grid2D(Nx=Nx, Ny=Ny, Lx=L, Ly=float(g.get("Ly", L)), **kw)
+        grid.mhd_config = (phys.get("mhd", {}) or {})
+        eqs = E.MHDEquations2D(gamma=gamma)
+        U0 = P.orszag_tang_2d(Nx, Ny, gamma, ic.get("rho0"), ic.get("p0"), float(ic.get("B0", 1.0)), L)
+        solver = S.SpectralSolverMHD2D(grid, eqs, scheme=integ.get("scheme", "rk4"),
+                                       cfl=float(integ.get("cfl", 0.3)))
     else:
-        raise ValueError(f"unknown problem {problem_name!r} (available: sod, tgv3d, khi2d)")
+        raise ValueError(f"unknown problem {problem_name!r} (available: sod, tgv3d, khi2d, orszag_tang2d)")
     dt = integ.get("dt", None)
     history = solver.run(U0, float(integ.get("t0", 0.0)), float(integ.get("t_end", 0.01)),
                          output_interval=float(integ.get("output_interval", 0.1)),
@@ -113,10 +125,10 @@ def __getattr__(name: str):
     if name in ("Grid1D", "Grid2D", "Grid3D"):
         from . import grid
         return getattr(grid, name)
-    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D"):
+    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D", "MHDEquations2D"):
         from . import equations
         return getattr(equations, name)
-    if name in ("SpectralSolver1D", "SpectralSolver2D", "SpectralSolver3D"):
+    if name in ("SpectralSolver1D", "SpectralSolver2D", "SpectralSolver3D", "SpectralSolverMHD2D"):
         from . import solver
         return getattr(solver, name)
     raise AttributeError(name)

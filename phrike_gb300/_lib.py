@@ -18,6 +18,7 @@ PS_OK = 0
 PS_BASIS_FOURIER = 0
 PS_BASIS_LEGENDRE = 1
 PS_EQ_EULER = 0
+PS_EQ_MHD = 1
 PS_GEMM_FP32 = 0
 PS_GEMM_FP64 = 1
 PS_GEMM_BF16X3 = 2
@@ -43,6 +44,12 @@ class PlanDesc(C.Structure):
         ("gravity", C.c_double * 3),
         ("cfl", C.c_double),
         ("gemm_precision", C.c_int),
+        ("mhd_rho_min", C.c_double),
+        ("mhd_p_min", C.c_double),
+        ("mhd_project_substages", C.c_int),
+        ("mhd_divergence_clean", C.c_int),
+        ("mhd_resistivity", C.c_double),
+        ("mhd_viscosity", C.c_double),
     ]
 
 
@@ -72,6 +79,8 @@ _SIGNATURES = [
     ("ps_rhs_static", C.c_int, [C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_lgl_build", C.c_int, [C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_apply_boundary_conditions", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_project_solenoidal", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_project_state", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_last_error", C.c_char_p, []),
     ("ps_version", C.c_char_p, []),
 ]

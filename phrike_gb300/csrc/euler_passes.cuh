@@ -327,6 +327,7 @@ struct OpArgs {
   int deriv;         // 0: P, 1: D
   float scale;       // multiplies the symbol (e.g. -1 for a right-hand side)
   int complement;    // P only: out = in - IFFT((1/N - P) FFT in)  (exact, see AxisOps)
+  const int* active; // contiguous only, nullable: rows of inactive solves are left as they are
 };
 
 template <int N, int T, bool STRIDED>
@@ -351,6 +352,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
     const int row = blockIdx.x * T + p;
     valid = row < a.rows;
     const int r = valid ? row : 0;
+    if (a.active != nullptr && a.active[r / a.rps] == 0) valid = false;
     base = (long)(r / a.rps) * a.ss + (long)(r % a.rps) * N + t;
     step = A;
   }

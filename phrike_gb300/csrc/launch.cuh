@@ -26,6 +26,11 @@ template <int N>
 cudaError_t launch_last_t(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, const CUtensorMap& mAcc,
                           const LastTArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_op_t(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s);
+// 2D ideal MHD: x pass and the three Helmholtz projection passes
+template <int N> cudaError_t launch_xfirst_mhd(const MhdXArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_proj_xf(const ProjArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_proj_y(const ProjArgs& a, cudaStream_t s);
+template <int N> cudaError_t launch_proj_xi(const ProjArgs& a, cudaStream_t s);
 
 inline bool supported_n(int n) {
   return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
@@ -114,6 +119,9 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
     if (nd == 3) {                                                                                    \
       if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;                  \
       k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);              \
+    } else if (a.mhd) {                                                                               \
+      if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;                \
+      k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);            \
     } else {                                                                                          \
       if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;                   \
       k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);               \
@@ -128,6 +136,42 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_op_t<NN, T, R>, sm)) != cudaSuccess) return e;                                \
     k_op_t<NN, T, R><<<grid, Shape<NN>::A * T, sm, s>>>(mIn, a);                                      \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_xfirst_mhd<NN>(const MhdXArgs& a, cudaStream_t s) {                              \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_xfirst_mhd<NN, T>, sm)) != cudaSuccess) return e;                             \
+    k_xfirst_mhd<NN, T><<<(a.rows + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                         \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_proj_xf<NN>(const ProjArgs& a, cudaStream_t s) {                                 \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_proj_xf<NN, T>, sm)) != cudaSuccess) return e;                                \
+    k_proj_xf<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                   \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_proj_y<NN>(const ProjArgs& a, cudaStream_t s) {                                  \
+    constexpr int T = (NN >= 512) ? 8 : 16;                                                           \
+    const size_t sm = sizeof(ProjYSmem<NN, T>);                                                       \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_proj_y<NN, T>, sm)) != cudaSuccess) return e;                                 \
+    k_proj_y<NN, T><<<dim3((a.hx + T - 1) / T, a.nsolve), Shape<NN>::A * T, sm, s>>>(a);               \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_proj_xi<NN>(const ProjArgs& a, cudaStream_t s) {                                 \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_proj_xi<NN, T>, sm)) != cudaSuccess) return e;                                \
+    k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                   \
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \

@@ -15,6 +15,7 @@
 // pencils; either lands in shared memory as rows of T floats.
 #pragma once
 #include "euler_passes.cuh"
+#include "mhd_passes.cuh"
 #include "tma.cuh"
 
 namespace ps {
@@ -275,13 +276,16 @@ struct LastTArgs {
   const float* eref;     // per-solve E_ref
   int filter_last;
   int* status;
+  int mhd;             // 1: 2D ideal MHD (8 components, the PHYS = 1 kernel)
 };
 
-template <int N, int T, int ND, bool CLAMP, int R>
-__global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
+// PHYS 0: Euler (ND + 2 components, energy-perturbation clamp); PHYS 1: 2D
+// ideal MHD (8 components, MHD clamp, mhd_passes.cuh).
+template <int N, int T, int ND, bool CLAMP, int R, int PHYS = 0>
+__global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_blocks<N, T>())
     k_last_t(const __grid_constant__ CUtensorMap mAB, const __grid_constant__ CUtensorMap mU,
              const __grid_constant__ CUtensorMap mAcc, LastTArgs a) {
-  constexpr int NC = ND + 2;
+  constexpr int NC = (PHYS == 1) ? 8 : ND + 2;
   constexpr int A = Shape<N>::A, B = Shape<N>::B;
   using PF = Pencil<N, T, true>;
   extern __shared__ __align__(1024) unsigned char smem_tma[];
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
           }
       }
     } else {
-      constexpr int CH = 4;  // positions per batch of epilogue loads
+      constexpr int CH = (NC > 5) ? 2 : 4;  // positions per batch of epilogue loads
 #pragma unroll
       for (int n0 = 0; n0 < B; n0 += CH) {
         float un[CH][NC], ac[CH][NC];
@@ -454,7 +458,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
             }
             u[c] = valid ? res : ((c == 0) ? 1.0f : 0.0f);
           }
-          clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
+          if constexpr (PHYS == 1) clamp_mhd(u, a.gamma, a.rho_min, a.p_min);
+          else clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             if (c & 1) kk[c / 2][n2].y = u[c];

@@ -65,6 +65,9 @@ struct ps_plan_s {
   double* F64[2] = {nullptr, nullptr};    // nodal filter matrices (filter on)
   float* F32[2] = {nullptr, nullptr};
   double lgl_hmin = 0.0;                  // smallest node spacing (CFL)
+  // 2D ideal MHD (PS_EQ_MHD): half spectra of the Helmholtz projection
+  bool mhd = false;
+  float2* H = nullptr;                    // [nsolve][2][ny][nx/2+1]
   // tensor-core split-bf16 contractions: hi/lo planes and their TMA maps
   int pitch[2] = {0, 0};                  // bf16 row pitch along x / y (multiple of 8)
   void* Dsplit[2] = {nullptr, nullptr};   // [2][n][pitch] of D_x, D_y

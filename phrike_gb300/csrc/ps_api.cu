@@ -77,7 +77,15 @@ int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
   if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
   if (is_lgl(d)) return ps::lgl_validate(d);
-  if (d->equations != PS_EQ_EULER) return fail(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
+  if (d->equations == PS_EQ_MHD) {
+    if (d->ndim != 2) return fail(PS_ERR_UNSUPPORTED, "MHD plans are 2D (got ndim %d)", d->ndim);
+    if (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0)
+      return fail(PS_ERR_UNSUPPORTED, "explicit resistivity / viscosity are not implemented (ideal MHD only)");
+    if (!(d->mhd_rho_min >= 0.0) || !(d->mhd_p_min >= 0.0))
+      return fail(PS_ERR_INVALID, "MHD clamp floors must be non-negative");
+  } else if (d->equations != PS_EQ_EULER) {
+    return fail(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
+  }
   for (int a = 0; a < d->ndim; ++a) {
     if (d->basis[a] != PS_BASIS_FOURIER)
       return fail(PS_ERR_UNSUPPORTED, "axis %d: only the Fourier basis is supported by this plan type", a);
@@ -90,8 +98,9 @@ int validate(const ps_plan_desc* d) {
   return PS_OK;
 }
 
-size_t scratch_fields(int nd) {
-  // G + AB + acc + Us (+ 1D flux)
+size_t scratch_fields(int nd, bool mhd = false) {
+  // G + AB + acc + Us (+ 1D flux); MHD: G (16) + acc + Us + half spectra (~2)
+  if (mhd) return 16 + 8 + 8 + 3;
   if (nd == 1) return 3;
   if (nd == 2) return 8 + 4 + 4;
   return 15 + 10 + 5 + 5;
@@ -212,8 +221,8 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
   ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells * p->nsolve);
   cudaError_t e;
   if (axis == 0) {
-    if (active != nullptr) return fail(PS_ERR_INVALID, "internal: masked x operator");
     ps::OpArgs a{};
+    a.active = active;
     a.in = in;
     a.out = out;
     a.nf = nf;
@@ -335,6 +344,11 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   // the 2D kernel clamps (solver.py:467-513); the 3D solver has none (1220-1230)
   a.rho_min = 1e-8f;  // _positivity_clamp_2d floors (solver.py:467)
   a.p_min = 1e-10f;
+  if (p->mhd) {  // SpectralSolverMHD._clamp floors from mhd_config (solver.py:876-877)
+    a.rho_min = (float)p->desc.mhd_rho_min;
+    a.p_min = (float)p->desc.mhd_p_min;
+    a.mhd = 1;
+  }
   a.eref = p->eref;
   a.filter_last = filter_last ? 1 : 0;
   a.status = p->status;
@@ -437,6 +451,100 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
   return PS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// 2D ideal MHD (SpectralSolverMHD, solver.py:840-1049)
+// ---------------------------------------------------------------------------
+int xfirst_mhd(ps_plan p, const float* U, float* speed, cudaStream_t s, const int* active) {
+  ps::MhdXArgs a{};
+  a.U = U;
+  a.out = p->G;
+  a.fs = p->cells;
+  a.ssU = p->ss(8);
+  a.ssOut = p->ss(16);
+  a.rows = p->rows() * p->nsolve;
+  a.rps = p->rows();
+  a.ax = p->ax(0);
+  a.gamma = (float)p->desc.gamma;
+  a.speed = speed;
+  a.active = active;
+  ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * p->nsolve * (8 + 16));
+  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_xfirst_mhd<decltype(nc)::value>(a, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "MHD x pass");
+  return PS_OK;
+}
+
+// Helmholtz projection of (Bx, By) in place (solve stride ss); E (nullable)
+// updated with the thermal pressure held fixed.
+int project(ps_plan p, float* Bx, float* By, float* E, long ss, const int* active, cudaStream_t s) {
+  ps::ProjArgs a{};
+  a.Bx = Bx;
+  a.By = By;
+  a.E = E;
+  a.ss = ss;
+  a.H = p->H;
+  a.nx = p->n[0];
+  a.ny = p->n[1];
+  a.hx = p->n[0] / 2 + 1;
+  a.nsolve = p->nsolve;
+  a.kx0 = (float)(2.0 * M_PI / p->desc.length[0]);
+  a.ky0 = (float)(2.0 * M_PI / p->desc.length[1]);
+  a.active = active;
+  // bytes: read B (2), write 2 half spectra; read/write them; read B (+E), write B (+E)
+  ProfScope prof(p, s, PS_KIND_OP, 4.0 * p->cells * p->nsolve * (2 + 2 + 4 + 2 + (E ? 4 : 2)));
+  a.ax = p->ax(0);
+  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_proj_xf<decltype(nc)::value>(a, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "projection x forward");
+  a.ax = p->ax(1);
+  e = ps::dispatch_n(p->n[1], [&](auto nc) { return ps::launch_proj_y<decltype(nc)::value>(a, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "projection y");
+  a.ax = p->ax(0);
+  e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_proj_xi<decltype(nc)::value>(a, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "projection x inverse");
+  return PS_OK;
+}
+
+int project_state(ps_plan p, float* U, const int* active, cudaStream_t s) {
+  if (!p->desc.mhd_divergence_clean) return PS_OK;  // divergence_clean "none"
+  return project(p, U + 5 * p->cells, U + 6 * p->cells, U + 4 * p->cells, p->ss(8), active, s);
+}
+
+// Fixed dt or CFL steps: every stage the x pass, the last pass with the MHD
+// clamp and (project_each_substage) the projection; after a step, at the
+// filter cadence, the spectral filter then the projection (solver.py:988-1049).
+int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+              cudaStream_t s) {
+  int rc;
+  const bool cfl = d_t != nullptr;
+  const int* act = cfl ? p->active : nullptr;
+  const double* dtp = cfl ? p->dt : d_dt;
+  if (cfl) {
+    PS_CU(cudaMemsetAsync(p->speed, 0, sizeof(float) * p->nsolve, s), "speed reset");
+    PS_CU(ps::launch_fill_int(p->active, p->nsolve, 1, s), "active reset");
+  }
+  for (int it = 0; it < nsteps; ++it) {
+    const bool due = (p->step_counter % p->desc.filter_interval) == 0;
+    for (int stage = 0; stage < 4; ++stage) {
+      const float* src = (stage == 0) ? U : p->Us;
+      float* out = (stage < 3) ? p->Us : U;
+      if ((rc = xfirst_mhd(p, src, (cfl && stage == 0) ? p->speed : nullptr, s, act)) != PS_OK) return rc;
+      if (cfl && stage == 0)
+        PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
+              "step control");
+      if ((rc = last(p, stage, U, out, dt, dtp, false, s, act)) != PS_OK) return rc;
+      if (p->desc.mhd_project_substages && (rc = project_state(p, out, act, s)) != PS_OK) return rc;
+    }
+    if (due) {
+      if ((rc = apply_op(p, 0, U, U, 8, 0, 1.0f, s, true, act)) != PS_OK) return rc;
+      if ((rc = apply_op(p, 1, U, U, 8, 0, 1.0f, s, true, act)) != PS_OK) return rc;
+      if ((rc = project_state(p, U, act, s)) != PS_OK) return rc;
+    }
+    if (cfl)
+      PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->active, p->steps_done, p->nsolve, s), "step advance");
+    p->step_counter += 1;
+  }
+  return PS_OK;
+}
+
 int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   int rc = validate(d);
   if (rc != PS_OK) return rc;
@@ -445,7 +553,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   ps_plan p = new ps_plan_s();
   p->desc = *d;
   p->nd = d->ndim;
-  p->nc = d->ndim + 2;
+  p->mhd = d->equations == PS_EQ_MHD;
+  p->nc = p->mhd ? 8 : d->ndim + 2;
   p->nsolve = nsolve;
   p->cells = 1;
   for (int a = 0; a < p->nd; ++a) {
@@ -478,8 +587,10 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   if (p->nd == 1) {
     if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
   } else {
-    const int ng = (p->nd == 3) ? 15 : 8;
+    const int ng = p->mhd ? 16 : (p->nd == 3) ? 15 : 8;
     if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
+    if (p->mhd && (rc = dalloc(p, &p->H, (size_t)2 * nsolve * p->n[1] * (p->n[0] / 2 + 1))) != PS_OK)
+      return cleanup(rc);
     if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
@@ -498,7 +609,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   if (lgl) {
     if ((rc = ps::lgl_setup(p)) != PS_OK) return cleanup(rc);
   } else if (p->nd >= 2) {
-    if ((rc = make_map(&p->map_G_y, p->G, p, (p->nd == 3) ? 15 : 8, 1)) != PS_OK) return cleanup(rc);
+    if ((rc = make_map(&p->map_G_y, p->G, p, p->mhd ? 16 : (p->nd == 3) ? 15 : 8, 1)) != PS_OK)
+      return cleanup(rc);
     if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
     if ((rc = make_map(&p->map_acc, p->acc, p, p->nc, (p->nd == 3) ? 2 : 1)) != PS_OK) return cleanup(rc);
   }
@@ -531,6 +643,10 @@ int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   d->filter_alpha = 36.0;
   d->filter_interval = 1;
   d->cfl = (ndim == 1) ? 0.4 : (ndim == 2) ? 0.3 : 0.25;
+  d->mhd_rho_min = 1e-10;
+  d->mhd_p_min = 1e-12;
+  d->mhd_project_substages = 1;
+  d->mhd_divergence_clean = 1;
   return PS_OK;
 }
 
@@ -544,7 +660,8 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
   if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
-  *bytes = scratch_fields(d->ndim) * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
+  *bytes = scratch_fields(d->ndim, d->equations == PS_EQ_MHD) * (size_t)cells * sizeof(float) * nsolve + tables +
+           64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
 
@@ -619,6 +736,10 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   int rc;
   if (p->lgl) return ps::lgl_rhs(p, U, rhs, s);
+  if (p->mhd) {
+    if ((rc = xfirst_mhd(p, U, nullptr, s, nullptr)) != PS_OK) return rc;
+    return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
+  }
   if (p->nd == 1) {
     PS_CU(ps::launch_flux1d(U, p->cells, p->ss(3), p->nsolve, (float)p->desc.gamma, p->F1, s), "1D flux");
     return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
@@ -640,6 +761,7 @@ int ps_run_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt,
   if (nsteps == 0) return PS_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (p->lgl) return ps::lgl_steps(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
+  if (p->mhd) return steps_mhd(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
   if (p->nd == 1) return step_1d(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
   return steps_nd(p, U, nsteps, dt, d_dt, nullptr, nullptr, s);
 }
@@ -650,6 +772,7 @@ int ps_run_cfl(ps_plan p, float* U, int nsteps, double* d_t, const double* d_ten
   if (nsteps == 0) return PS_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (p->lgl) return ps::lgl_steps(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
+  if (p->mhd) return steps_mhd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   if (p->nd == 1) return step_1d(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   return steps_nd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
 }
@@ -700,8 +823,26 @@ int ps_apply_boundary_conditions(ps_plan p, float* U, void* stream) {
   return PS_OK;
 }
 
+int ps_project_solenoidal(ps_plan p, float* Bx, float* By, void* stream) {
+  if (!p || !Bx || !By) return fail(PS_ERR_INVALID, "null argument");
+  if (p->lgl || p->nd != 2 || p->H == nullptr)
+    return fail(PS_ERR_UNSUPPORTED, "the Helmholtz projection needs a 2D Fourier MHD plan");
+  return project(p, Bx, By, nullptr, p->cells, nullptr, (cudaStream_t)stream);
+}
+
+int ps_project_state(ps_plan p, float* U, void* stream) {
+  if (!p || !U) return fail(PS_ERR_INVALID, "null argument");
+  if (!p->mhd) return fail(PS_ERR_UNSUPPORTED, "ps_project_state needs a PS_EQ_MHD plan");
+  return project_state(p, U, nullptr, (cudaStream_t)stream);
+}
+
 int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
   if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
+  if (p->mhd) {
+    PS_CU(ps::launch_speed_mhd(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out, (cudaStream_t)stream),
+          "max wave speed");
+    return PS_OK;
+  }
   PS_CU(ps::launch_speed(p->nd, U, p->cells, p->ss(p->nc), p->nsolve, (float)p->desc.gamma, d_out,
                          (cudaStream_t)stream),
         "max wave speed");
@@ -710,6 +851,11 @@ int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
 
 int ps_conserved(ps_plan p, const float* U, double* d_out, void* stream) {
   if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
+  if (p->mhd) {
+    PS_CU(ps::launch_conserved_mhd(U, p->cells, p->ss(8), p->nsolve, p->desc.gamma, d_out, (cudaStream_t)stream),
+          "conserved sums");
+    return PS_OK;
+  }
   PS_CU(ps::launch_conserved(p->nd, U, p->cells, p->ss(p->nc), p->nsolve, p->desc.gamma, d_out,
                              (cudaStream_t)stream),
         "conserved sums");

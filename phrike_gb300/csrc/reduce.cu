@@ -81,6 +81,65 @@ __global__ void k_conserved(const float* __restrict__ U, long cells, long ss, do
   }
 }
 
+// 2D ideal MHD: max(|ux|, |uy|) + sqrt(a^2 + b^2) (equations.py:874-887)
+__global__ void k_speed_mhd(const float* __restrict__ U, long cells, long ss, float gamma, float* out) {
+  __shared__ float red[32];
+  U += (long)blockIdx.y * ss;
+  out += blockIdx.y;
+  float m = 0.0f;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
+    const float rho = U[i];
+    const float ux = U[cells + i] / rho, uy = U[2 * cells + i] / rho, uz = U[3 * cells + i] / rho;
+    const float bx = U[5 * cells + i], by = U[6 * cells + i], bz = U[7 * cells + i];
+    const float b2 = bx * bx + by * by + bz * bz;
+    const float p = (gamma - 1.0f) * (U[4 * cells + i] - 0.5f * rho * (ux * ux + uy * uy + uz * uz) - 0.5f * b2);
+    m = fmaxf(m, fmaxf(fabsf(ux), fabsf(uy)) + sqrtf(fmaxf(gamma * p / rho + b2 / rho, 0.0f)));
+  }
+  m = block_max(m, red);
+  if (threadIdx.x == 0) atomic_max_nonneg(out, m);
+}
+
+// 2D ideal MHD conserved sums in float64 (equations.py:889-907): mass,
+// momentum x/y/z, energy rebuilt from primitives, magnetic energy, cross
+// helicity (and a zero pad to 8 values)
+__global__ void k_conserved_mhd(const float* __restrict__ U, long cells, long ss, double gamma, double* out) {
+  __shared__ double red[7][32];
+  U += (long)blockIdx.y * ss;
+  out += (long)blockIdx.y * 8;
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
+    const double rho = U[i];
+    const double ux = U[cells + i] / rho, uy = U[2 * cells + i] / rho, uz = U[3 * cells + i] / rho;
+    const double bx = U[5 * cells + i], by = U[6 * cells + i], bz = U[7 * cells + i];
+    const double v2 = ux * ux + uy * uy + uz * uz, b2 = bx * bx + by * by + bz * bz;
+    const double p = (gamma - 1.0) * ((double)U[4 * cells + i] - 0.5 * rho * v2 - 0.5 * b2);
+    s[0] += rho;
+    s[1] += rho * ux;
+    s[2] += rho * uy;
+    s[3] += rho * uz;
+    s[4] += p / (gamma - 1.0) + 0.5 * rho * v2 + 0.5 * b2;
+    s[5] += 0.5 * b2;
+    s[6] += ux * bx + uy * by + uz * bz;
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < 7; ++c) {
+    double v = s[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) red[c][w] = v;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 7; ++c) {
+      double v = (l < nw) ? red[c][l] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (l == 0) atomicAdd(out + c, v);
+    }
+  }
+}
+
 // 1D flux F = [rho u, rho u^2 + p, (E + p) u] (equations.py:67-86)
 __global__ void k_flux1d(const float* __restrict__ U, long n, float gamma, float* __restrict__ F) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
@@ -200,6 +259,26 @@ cudaError_t launch_flux1d(const float* U, long n, long ss, int nsolve, float gam
   for (int q = 0; q < nsolve; ++q) {
     k_flux1d<<<blocks, 256, 0, s>>>(U + (long)q * ss, n, gamma, F + (long)q * 3 * n);
   }
+  return cudaGetLastError();
+}
+
+}  // namespace ps
+
+namespace ps {
+
+cudaError_t launch_speed_mhd(const float* U, long cells, long ss, int nsolve, float gamma, float* out,
+                             cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * nsolve, s);
+  if (e != cudaSuccess) return e;
+  k_speed_mhd<<<dim3(reduce_blocks(cells, nsolve), nsolve), 256, 0, s>>>(U, cells, ss, gamma, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conserved_mhd(const float* U, long cells, long ss, int nsolve, double gamma, double* out,
+                                 cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * 8 * nsolve, s);
+  if (e != cudaSuccess) return e;
+  k_conserved_mhd<<<dim3(reduce_blocks(cells, nsolve), nsolve), 256, 0, s>>>(U, cells, ss, gamma, out);
   return cudaGetLastError();
 }
 

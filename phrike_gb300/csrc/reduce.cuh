@@ -17,5 +17,9 @@ cudaError_t launch_speed(int nd, const float* U, long cells, long ss, int nsolve
                          cudaStream_t s, const float* eshift = nullptr);
 cudaError_t launch_conserved(int nd, const float* U, long cells, long ss, int nsolve, double gamma, double* out,
                              cudaStream_t s);
+cudaError_t launch_speed_mhd(const float* U, long cells, long ss, int nsolve, float gamma, float* out,
+                             cudaStream_t s);
+cudaError_t launch_conserved_mhd(const float* U, long cells, long ss, int nsolve, double gamma, double* out,
+                                 cudaStream_t s);
 cudaError_t launch_flux1d(const float* U, long n, long ss, int nsolve, float gamma, float* F, cudaStream_t s);
 }  // namespace ps

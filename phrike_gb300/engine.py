@@ -52,14 +52,17 @@ class Plan:
                  dealias: bool = True, filter_params: Optional[Dict] = None,
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
-                 gemm_precision: str = "fp32"):
+                 gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
             raise RuntimeError("phrike_gb300 plans run on a CUDA device only")
         self.shape = tuple(int(n) for n in shape)
         self.ndim = len(self.shape)
-        self.ncomp = self.ndim + 2
+        self.equations = str(equations).lower()
+        if self.equations not in ("euler", "mhd"):
+            raise ValueError(f"equations must be 'euler' or 'mhd' (got {equations!r})")
+        self.ncomp = 8 if self.equations == "mhd" else self.ndim + 2
         desc = _lib.PlanDesc()
         _lib.check(lib.ps_plan_desc_init(C.byref(desc), self.ndim))
         xyz = list(reversed(self.shape))
@@ -77,6 +80,15 @@ class Plan:
             raise ValueError(f"gemm_precision must be one of {sorted(_lib.GEMM_PRECISIONS)}")
         self.gemm_precision = str(gemm_precision).lower()
         desc.gemm_precision = _lib.GEMM_PRECISIONS[self.gemm_precision]
+        if self.equations == "mhd":
+            desc.equations = _lib.PS_EQ_MHD
+            mc = mhd_config or {}
+            desc.mhd_rho_min = float(mc.get("rho_min", 1e-10))
+            desc.mhd_p_min = float(mc.get("p_min", 1e-12))
+            desc.mhd_project_substages = 1 if bool(mc.get("project_each_substage", True)) else 0
+            desc.mhd_divergence_clean = 0 if str(mc.get("divergence_clean", "projection")) == "none" else 1
+            desc.mhd_resistivity = float(mc.get("resistivity", 0.0))
+            desc.mhd_viscosity = float(mc.get("viscosity", 0.0))
         desc.gamma = float(gamma)
         desc.dealias = 1 if dealias else 0
         fp = filter_params or {}
@@ -189,6 +201,19 @@ class Plan:
         _lib.check(self._lib.ps_apply_boundary_conditions(self._handle, _ptr(U), _stream(self.device)))
         return U
 
+    def project_state_(self, U: torch.Tensor) -> torch.Tensor:
+        """MHD: Helmholtz projection of B and the energy update in place."""
+        self._check_state(U)
+        _lib.check(self._lib.ps_project_state(self._handle, _ptr(U), _stream(self.device)))
+        return U
+
+    def project_solenoidal_(self, Bx: torch.Tensor, By: torch.Tensor):
+        """Helmholtz projection of (Bx, By) in place (one field per solve each)."""
+        self._check_state(Bx, 1)
+        self._check_state(By, 1)
+        _lib.check(self._lib.ps_project_solenoidal(self._handle, _ptr(Bx), _ptr(By), _stream(self.device)))
+        return Bx, By
+
     def max_wave_speed(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)
         out = torch.empty(self.nsolve, dtype=torch.float32, device=self.device) if out is None else out
@@ -198,7 +223,8 @@ class Plan:
     def conserved(self, U: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)
         if out is None:
-            shape = (self.ncomp,) if self.nsolve == 1 else (self.nsolve, self.ncomp)
+            nv = 8 if self.equations == "mhd" else self.ncomp
+            shape = (nv,) if self.nsolve == 1 else (self.nsolve, nv)
             out = torch.empty(shape, dtype=torch.float64, device=self.device)
         _lib.check(self._lib.ps_conserved(self._handle, _ptr(U), _ptr(out), _stream(self.device)))
         return out

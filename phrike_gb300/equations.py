@@ -1,7 +1,8 @@
-"""Compressible Euler equations with the reference's interface (backend "gb300").
+"""Compressible Euler and 2D ideal MHD equations with the reference's
+interface (backend "gb300").
 
-Mirrors EulerEquations1D/2D/3D of phrike/equations.py (lines 217-319,
-322-381, 551-637).  These helpers evaluate element-wise formulas on device
+Mirrors EulerEquations1D/2D/3D and MHDEquations2D of phrike/equations.py
+(lines 217-319, 322-381, 551-637, 770-907).  These helpers evaluate element-wise formulas on device
 tensors for user code (initial conditions, monitoring); the time stepper
 itself runs the fused CUDA kernels of phrike_gb300.engine.  The state layout
 is [rho, m_1..m_d, E] with momenta ordered x, y, z.
@@ -141,3 +142,60 @@ class EulerEquations3D(_Euler):
         return {"mass": float(rho.double().sum()), "momentum_x": float((rho * ux).double().sum()),
                 "momentum_y": float((rho * uy).double().sum()), "momentum_z": float((rho * uz).double().sum()),
                 "energy": float((p / (self.gamma - 1.0) + kin).double().sum())}
+
+
+@dataclass
+class MHDEquations2D:
+    """Ideal compressible MHD in 2D (2.5D: all three vector components, fields
+    depending on x and y), conservative state [rho, rho ux, rho uy, rho uz, E,
+    Bx, By, Bz] (phrike/equations.py:770-907).  Element-wise helpers on
+    device tensors; the stepper runs the CUDA kernels of the engine."""
+
+    gamma: float = 5.0 / 3.0
+
+    def primitive(self, U):
+        U = _t(U)
+        rho = U[0]
+        ux, uy, uz = U[1] / rho, U[2] / rho, U[3] / rho
+        Bx, By, Bz = U[5], U[6], U[7]
+        kin = 0.5 * rho * (ux * ux + uy * uy + uz * uz)
+        mag = 0.5 * (Bx * Bx + By * By + Bz * Bz)
+        p = (self.gamma - 1.0) * (U[4] - kin - mag)
+        return rho, ux, uy, uz, p, Bx, By, Bz
+
+    def conservative(self, rho, ux, uy, uz, p, Bx, By, Bz):
+        rho = _t(rho)
+        ux, uy, uz, p, Bx, By, Bz = (_t(v, rho) for v in (ux, uy, uz, p, Bx, By, Bz))
+        E = (p / (self.gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz)
+             + 0.5 * (Bx * Bx + By * By + Bz * Bz))
+        return torch.stack([rho, rho * ux, rho * uy, rho * uz, E, Bx, By, Bz], dim=0)
+
+    def flux(self, U):
+        U = _t(U)
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        E = U[4]
+        uB = ux * Bx + uy * By + uz * Bz
+        ps = p + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+        mx, my = rho * ux, rho * uy
+        z = torch.zeros_like(rho)
+        Fx = torch.stack([mx, mx * ux + ps - Bx * Bx, mx * uy - Bx * By, mx * uz - Bx * Bz,
+                          (E + ps) * ux - Bx * uB, z, ux * By - uy * Bx, ux * Bz - uz * Bx], dim=0)
+        Fy = torch.stack([my, my * ux - By * Bx, my * uy + ps - By * By, my * uz - By * Bz,
+                          (E + ps) * uy - By * uB, uy * Bx - ux * By, z, uy * Bz - uz * By], dim=0)
+        return Fx, Fy
+
+    def max_wave_speed(self, U) -> float:
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        a2 = self.gamma * p / rho
+        b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+        fast = torch.sqrt(torch.clamp(a2 + b2, min=0.0))
+        return float(torch.max(torch.maximum(torch.abs(ux), torch.abs(uy)) + fast).item())
+
+    def conserved_quantities(self, U) -> Dict[str, float]:
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        b2 = Bx * Bx + By * By + Bz * Bz
+        E = p / (self.gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * b2
+        return {"mass": float(rho.double().sum()), "momentum_x": float((rho * ux).double().sum()),
+                "momentum_y": float((rho * uy).double().sum()), "momentum_z": float((rho * uz).double().sum()),
+                "energy": float(E.double().sum()), "magnetic_energy": float((0.5 * b2).double().sum()),
+                "cross_helicity": float((ux * Bx + uy * By + uz * Bz).double().sum())}

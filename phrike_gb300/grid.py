@@ -169,6 +169,8 @@ class Grid2D(_FourierGridBase):
         self.dx, self.dy = self.Lx / self.Nx, self.Ly / self.Ny
         self.dx_min = None
         self.dy_min = None
+        self.mhd_config: Optional[Dict[str, Any]] = None  # set by MHD problems (grid.mhd_config)
+        self._mhd_plan: Optional[Plan] = None
         if lgl:
             self._init_lgl(dealias, filter_params, torch_device, precision, gemm_precision)
             return
@@ -210,6 +212,23 @@ class Grid2D(_FourierGridBase):
 
     def dy1(self, f: Any) -> torch.Tensor:
         return self._op(f, 1)
+
+    # --- MHD solenoidal helpers (grid.py:1290-1327) ---
+    def divergence(self, Bx: Any, By: Any) -> torch.Tensor:
+        """dx1(Bx) + dy1(By) with the masked derivative operators."""
+        return self.dx1(Bx) + self.dy1(By)
+
+    def project_solenoidal(self, Bx: Any, By: Any) -> Tuple[torch.Tensor, torch.Tensor]:
+        """Helmholtz (Leray) projection of (Bx, By); returns new tensors."""
+        if self._basis != "fourier":
+            raise ValueError("project_solenoidal requires Fourier basis in x and y")
+        if self._mhd_plan is None:
+            self._mhd_plan = Plan(self._shape, self._lengths, dealias=self.dealias, filter_params=self.filter_params,
+                                  device=self.device, equations="mhd")
+        bx = self.to_device(Bx).clone()
+        by = self.to_device(By).clone()
+        self._mhd_plan.project_solenoidal_(bx, by)
+        return bx, by
 
     def xy_mesh(self) -> Tuple[torch.Tensor, torch.Tensor]:
         Y, X = torch.meshgrid(self.y, self.x, indexing="ij")

@@ -71,25 +71,31 @@ def kelvin_helmholtz_2d(Nx: int, Ny: int = None, U0: float = 1.0, A: float = 0.0
     return _euler_conservative(rho, [u, v], p, gamma)
 
 
-def orszag_tang_2d(Nx: int, Ny: int = None, gamma: float = 5.0 / 3.0) -> np.ndarray:
-    """rho = gamma^2, p = gamma, u = -sin y, v = sin x, Bx = -sin y, By = sin 2x
-    on [0, 2 pi)^2.  8 components [rho, mx, my, mz, Bx, By, Bz, E] with
-    E = p/(gamma-1) + rho|u|^2/2 + |B|^2/2."""
+def orszag_tang_2d(Nx: int, Ny: int = None, gamma: float = 5.0 / 3.0, rho0: float = None, p0: float = None,
+                   B0: float = 1.0, L: float = 2.0 * np.pi) -> np.ndarray:
+    """Orszag-Tang vortex on [0, L)^2 with the reference's parametrisation
+    (problems/problem_list/orszag_tang2d.py:33-66): rho = rho0, p = p0,
+    u = -sin(2 pi y/L), v = sin(2 pi x/L), Bx = -B0 sin(2 pi y/L),
+    By = B0 sin(4 pi x/L); defaults rho0 = gamma^2, p0 = gamma, B0 = 1,
+    L = 2 pi.  8 components in the reference order
+    [rho, rho ux, rho uy, rho uz, E, Bx, By, Bz] (equations.py:770-810)."""
     Ny = Nx if Ny is None else Ny
-    L = 2.0 * np.pi
+    rho0 = gamma ** 2 if rho0 is None else rho0
+    p0 = gamma if p0 is None else p0
     x = np.linspace(0.0, L, Nx, endpoint=False)
     y = np.linspace(0.0, L, Ny, endpoint=False)
     X, Y = np.meshgrid(x, y, indexing="xy")
-    rho = gamma ** 2 * np.ones_like(X)
-    p = gamma * np.ones_like(X)
-    u = -np.sin(Y)
-    v = np.sin(X)
+    k = 2.0 * np.pi / L
+    rho = rho0 * np.ones_like(X)
+    p = p0 * np.ones_like(X)
+    u = -np.sin(k * Y)
+    v = np.sin(k * X)
     w = np.zeros_like(X)
-    Bx = -np.sin(Y)
-    By = np.sin(2.0 * X)
+    Bx = -B0 * np.sin(k * Y)
+    By = B0 * np.sin(2.0 * k * X)
     Bz = np.zeros_like(X)
     E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
-    return np.stack([rho, rho * u, rho * v, rho * w, Bx, By, Bz, E])
+    return np.stack([rho, rho * u, rho * v, rho * w, E, Bx, By, Bz])
 
 
 def acoustic_pulse_lgl_2d(x: np.ndarray, y: np.ndarray, gamma: float = 1.4,

@@ -20,6 +20,7 @@ from .engine import Plan
 class _SpectralSolverBase:
     _ndim = 1
     _history_keys: List[str] = []
+    _equations = "euler"
 
     def __init__(self, grid, equations, U0: Optional[Any] = None, scheme: str = "rk4", cfl: float = 0.4,
                  adaptive_config: Optional[Dict] = None, artificial_viscosity_config: Optional[Dict] = None,
@@ -51,7 +52,8 @@ class _SpectralSolverBase:
         self.plan = Plan(grid._shape, grid._lengths, gamma=float(equations.gamma), dealias=grid.dealias,
                          filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device,
                          basis=getattr(grid, "_basis", "fourier"),
-                         gemm_precision=getattr(grid, "gemm_precision", "fp32"))
+                         gemm_precision=getattr(grid, "gemm_precision", "fp32"), equations=self._equations,
+                         mhd_config=getattr(grid, "mhd_config", None))
 
     # -- reference interface -----------------------------------------------
     def _spacing(self) -> float:
@@ -156,3 +158,59 @@ class SpectralSolver3D(_SpectralSolverBase):
 
     def _spacing(self) -> float:
         return min(self.grid.dx, self.grid.dy, self.grid.dz)
+
+
+class SpectralSolverMHD2D(_SpectralSolverBase):
+    """2D (2.5D) ideal MHD, RK4 (phrike/solver.py:840-1049, 1169-1170).
+
+    Options come from ``grid.mhd_config`` like the reference (resistivity,
+    viscosity, project_each_substage, divergence_clean, rho_min, p_min;
+    explicit resistivity/viscosity are not implemented).  Every RK stage is
+    clamped and projected on the device; after a step, at the filter cadence,
+    the spectral filter and the projection.  run() projects U0 first and
+    records magnetic energy, cross helicity and max |div B| as well.
+    CFL dt = cfl * min(dx, dy) / max(max(|ux|, |uy|) + sqrt(a^2 + b^2)).
+    """
+
+    _ndim = 2
+    _equations = "mhd"
+    _history_keys = ["mass", "momentum_x", "momentum_y", "momentum_z", "energy", "magnetic_energy",
+                     "cross_helicity"]
+
+    def __init__(self, grid, equations, U0=None, scheme="rk4", cfl=0.3, adaptive_config=None,
+                 artificial_viscosity_config=None, gravity_config=None):
+        cfg = getattr(grid, "mhd_config", None) or {}
+        self.resistivity = float(cfg.get("resistivity", 0.0))
+        self.viscosity = float(cfg.get("viscosity", 0.0))
+        self.project_each_substage = bool(cfg.get("project_each_substage", True))
+        self.divergence_clean = str(cfg.get("divergence_clean", "projection"))
+        if self.resistivity != 0.0 or self.viscosity != 0.0:
+            raise NotImplementedError("backend 'gb300': explicit resistivity/viscosity are not implemented")
+        if gravity_config and gravity_config.get("enabled", False):
+            raise NotImplementedError("backend 'gb300': gravity is not implemented for MHD")
+        self.dim = 2
+        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, artificial_viscosity_config, None)
+
+    def _spacing(self) -> float:
+        return min(self.grid.dx, self.grid.dy)
+
+    def _project_B(self, U: Any) -> torch.Tensor:
+        V = self.grid.to_device(U).clone()
+        self.plan.project_state_(V)
+        return V
+
+    def max_div_b(self, U: Any) -> float:
+        t = self.grid.to_device(U)
+        return float(torch.max(torch.abs(self.grid.divergence(t[5], t[6]))).item())
+
+    def _record(self, history: Dict[str, List[float]]) -> None:
+        super()._record(history)
+        history.setdefault("div_b_max", []).append(self.max_div_b(self.U))
+
+    def run(self, U0: Any, t0: float, t_end: float, output_interval: float = 0.1, checkpoint_interval: float = 0.0,
+            outdir: Optional[str] = None, on_output: Optional[Callable[[float, Any], None]] = None,
+            on_step: Optional[Callable[[int, float, Any], None]] = None, tracers: Optional[Any] = None,
+            dt: Optional[float] = None) -> Dict[str, List[float]]:
+        """solver.py:1092-1162: the initial state is projected first."""
+        return super().run(self._project_B(U0), t0, t_end, output_interval, checkpoint_interval, outdir,
+                           on_output, on_step, tracers, dt)

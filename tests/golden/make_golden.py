@@ -38,9 +38,11 @@ def import_reference(path: str):
     return grid, equations, solver
 
 
-def main(ref_path: str) -> None:
+def main(ref_path: str, only: str = "") -> None:
     grid, equations, solver = import_reference(ref_path)
     from phrike_gb300 import problems
+    if only == "mhd":
+        return mhd_fixtures(grid, equations, solver, problems)
 
     out = {}
 
@@ -144,8 +146,39 @@ def main(ref_path: str) -> None:
                             nsteps=nsteps, x=x, y=y, Dx=Dx, Dy=Dy, dt_cfl0=s.compute_dt(torch.from_numpy(U0)),
                             amp=0.2, width2=0.05)
 
+    mhd_fixtures(grid, equations, solver, problems)
     print("golden fixtures written to", HERE)
 
 
+def mhd_fixtures(grid, equations, solver, problems) -> None:
+    """2D ideal MHD: Orszag-Tang (rho = gamma^2, p = gamma, B0 = 1 on
+    [0, 2 pi)^2) plus a divergent perturbation of B that the projection
+    removes and an out-of-plane field; NumPy backend."""
+    for (nx, ny), fon, nsteps, dt in (((32, 32), True, 3, 2e-3), ((32, 16), False, 2, 2e-3)):
+        fp = {"enabled": True, "p": 8, "alpha": 36.0} if fon else None
+        L = 2.0 * np.pi
+        g = grid.Grid2D(Nx=nx, Ny=ny, Lx=L, Ly=L, dealias=True, filter_params=fp)
+        g.mhd_config = {"resistivity": 0.0, "viscosity": 0.0, "project_each_substage": True,
+                        "divergence_clean": "projection"}
+        eq = equations.MHDEquations2D(gamma=5.0 / 3.0)
+        s = solver.SpectralSolverMHD2D(g, eq, scheme="rk4", cfl=0.3)
+        U0 = problems.orszag_tang_2d(nx, ny, gamma=5.0 / 3.0)
+        X, Y = np.meshgrid(np.asarray(g.x), np.asarray(g.y), indexing="xy")
+        U0[5] += 0.05 * np.cos(X) * np.cos(2.0 * Y)   # div B != 0
+        U0[6] += 0.03 * np.sin(3.0 * X) * np.sin(Y)
+        U0[7] = 0.1 * np.cos(X + Y)                     # out-of-plane field
+        rhs0 = s._compute_rhs(U0.copy())
+        P0 = s._project_B(U0.copy())
+        U = U0.copy()
+        for _ in range(nsteps):
+            U = s.step(U, dt)
+        cons0 = eq.conserved_quantities(U0)
+        np.savez_compressed(os.path.join(HERE, f"mhd2d_{nx}x{ny}.npz"), U0=U0, rhs0=rhs0, P0=P0, U=U, dt=dt,
+                            nsteps=nsteps, filter=int(fon), dt_cfl0=s.compute_dt(U0),
+                            cons0=np.array([cons0[k] for k in ("mass", "momentum_x", "momentum_y", "momentum_z",
+                                                               "energy", "magnetic_energy", "cross_helicity")]),
+                            divb_P0=s.max_div_b(P0), divb_U0=s.max_div_b(U0))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2] if len(sys.argv) > 2 else "")
