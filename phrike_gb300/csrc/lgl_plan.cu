@@ -98,36 +98,40 @@ int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, do
     LGL_CU(launch_flux_split(f, s), "LGL split fluxes");
   }
   {
+    // Gx^T[i][(solve, c, j)] = sum_k D_x[i][k] F_x[(solve, c, j)][k]
     UmmaArgs g{};
     g.C = Gx;
     g.ldc = nx;
     g.cz = 0;
-    g.M = p->nsolve * 4 * ny;
-    g.N = nx;
+    g.M = nx;
+    g.N = p->nsolve * 4 * ny;
     g.K = nx;
     g.batch = 1;
+    g.c_trans = 1;
     g.alpha = 1.0f;
     g.zper = 1;
     g.status = p->status;
     ProfScope prof(p, s, PS_KIND_LGL_X, 8.0 * field_bytes(p));
-    LGL_CU(launch_umma_x3(p->map_FX, p->map_Dx, g, p->nt_x, s), "LGL x contraction (tensor cores)");
+    LGL_CU(launch_umma_x3(p->map_Dx, p->map_FX, g, p->nt_x, s), "LGL x contraction (tensor cores)");
   }
   {
+    // Gy[solve, c]^T[i][j] = sum_k F_y^T[solve, c][i][k] D_y[j][k]
     UmmaArgs g{};
     g.C = Gy;
     g.ldc = nx;
     g.cz = p->cells;
-    g.M = ny;
-    g.N = nx;
+    g.M = nx;
+    g.N = ny;
     g.K = ny;
     g.batch = p->nsolve * 4;
-    g.b_batched = 1;
+    g.a_batched = 1;
+    g.c_trans = 1;
     g.active = act;
     g.zper = 4;
     g.alpha = 1.0f;
     g.status = p->status;
     ProfScope prof(p, s, PS_KIND_LGL_Y, 8.0 * field_bytes(p));
-    LGL_CU(launch_umma_x3(p->map_Dy, p->map_FYT, g, p->nt_y, s), "LGL y contraction (tensor cores)");
+    LGL_CU(launch_umma_x3(p->map_FYT, p->map_Dy, g, p->nt_y, s), "LGL y contraction (tensor cores)");
   }
   LglUpdateArgs u{};
   u.Gx = Gx;
@@ -315,13 +319,14 @@ int lgl_setup(ps_plan p) {
     LGL_CU(cudaMemset(fyt, 0, sizeof(unsigned short) * nfy), "flux planes clear");
     p->FX = fx;
     p->FYT = fyt;
-    p->nt_x = umma_n_tile(nx);
-    p->nt_y = umma_n_tile(nx);
+    // A operands (128-row boxes): D_x and F_y^T; B operands (N-tile boxes): F_x and D_y
+    p->nt_x = umma_n_tile(nx, p->nsolve * 4 * ny, 1);
+    p->nt_y = umma_n_tile(nx, ny, p->nsolve * 4);
     int e = 0;
-    if ((e = encode_split_map(&p->map_FX, p->FX, nx, p->nsolve * 4 * ny, 1, p->pitch[0], 128)) != 0 ||
-        (e = encode_split_map(&p->map_Dx, p->Dsplit[0], nx, nx, 1, p->pitch[0], p->nt_x)) != 0 ||
-        (e = encode_split_map(&p->map_Dy, p->Dsplit[1], ny, ny, 1, p->pitch[1], 128)) != 0 ||
-        (e = encode_split_map(&p->map_FYT, p->FYT, ny, nx, p->nsolve * 4, p->pitch[1], p->nt_y)) != 0)
+    if ((e = encode_split_map(&p->map_Dx, p->Dsplit[0], nx, nx, 1, p->pitch[0], 128)) != 0 ||
+        (e = encode_split_map(&p->map_FX, p->FX, nx, p->nsolve * 4 * ny, 1, p->pitch[0], p->nt_x)) != 0 ||
+        (e = encode_split_map(&p->map_FYT, p->FYT, ny, nx, p->nsolve * 4, p->pitch[1], 128)) != 0 ||
+        (e = encode_split_map(&p->map_Dy, p->Dsplit[1], ny, ny, 1, p->pitch[1], p->nt_y)) != 0)
       return errorf(PS_ERR_CUDA, "tensor map encoding for the split contractions failed (%d)", e);
     LGL_CU(cudaDeviceSynchronize(), "split tables");
   }

@@ -11,8 +11,10 @@
 // Per RK stage (solver.py:428-466, 623-648):
 //   k_flux_split   walls already applied; x flux F_x[c][j][k] and the
 //                  transposed y flux F_y^T[c][i][k] as hi/lo planes
-//   k_umma_x3      Gx = F_x D_x^T  (rows (solve, c, j) stacked, one batch)
-//                  Gy^T-free form: Gy[c] = D_y F_y[c], as D_y (F_y^T)^T
+//   k_umma_x3      Gx^T = D_x F_x^T (columns (solve, c, j) stacked) and
+//                  Gy[c]^T = F_y[c]^T D_y^T per solve and component: the
+//                  accumulator lanes run along x, the contiguous axis of the
+//                  outputs, so the epilogue stores whole 128-byte lines
 //   k_lgl_update   k = -(Gx + Gy), the RK4 stage update and the 2D clamp
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -266,11 +268,19 @@ __global__ void __launch_bounds__(128, 1) k_umma_x3(const __grid_constant__ CUte
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       if (m < g.M) {
-        float* row = C + (long)m * g.ldc;
+        if (g.c_trans) {  // lanes (m) along contiguous memory: one 128-byte store per column
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int n = n0 + c0 + q;
-          if (n < g.N) row[n] = g.alpha * v[q];
+          for (int q = 0; q < 16; ++q) {
+            const int n = n0 + c0 + q;
+            if (n < g.N) C[(long)n * g.ldc + m] = g.alpha * v[q];
+          }
+        } else {
+          float* row = C + (long)m * g.ldc;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int n = n0 + c0 + q;
+            if (n < g.N) row[n] = g.alpha * v[q];
+          }
         }
       }
     }
@@ -330,20 +340,18 @@ static cudaError_t umma_t(const CUtensorMap& mA, const CUtensorMap& mB, const Um
   return cudaGetLastError();
 }
 
-int umma_n_tile(int N) {
-  // fewest tiles of at most 256 columns, each a multiple of 16 (>= 32)
-  const int tiles = (N + 255) / 256;
-  int nt = (N + tiles - 1) / tiles;
-  nt = (nt + 15) / 16 * 16;
-  if (nt < 32) nt = 32;
-  return nt <= 64 ? 64 : nt <= 128 ? 128 : nt <= 144 ? 144 : nt <= 176 ? 176 : 256;
+int umma_n_tile(int M, int N, int batch) {
+  const long mt = (M + 127) / 128;
+  const int cand[4] = {256, 176, 128, 64};
+  for (int nt : cand)
+    if (mt * ((N + nt - 1) / nt) * batch >= 148 || nt == 64) return nt;
+  return 64;
 }
 
 cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const UmmaArgs& g, int nt, cudaStream_t s) {
   switch (nt) {
     case 64: return umma_t<64, 4>(mA, mB, g, s);
     case 128: return umma_t<128, 3>(mA, mB, g, s);
-    case 144: return umma_t<144, 3>(mA, mB, g, s);
     case 176: return umma_t<176, 2>(mA, mB, g, s);
     case 256: return umma_t<256, 2>(mA, mB, g, s);
     default: return cudaErrorInvalidValue;

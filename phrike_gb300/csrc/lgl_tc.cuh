@@ -30,6 +30,7 @@ struct UmmaArgs {
   long ldc, cz;
   int M, N, K, batch;
   int a_batched, b_batched;
+  int c_trans;        // 1: element (m, n) stored at C[z*cz + n*ldc + m] (lanes along contiguous memory)
   const int* active;  // nullable: batch entry z skipped when active[z / zper] == 0
   int zper;
   float alpha;
@@ -37,8 +38,9 @@ struct UmmaArgs {
 };
 // tensor map over split planes [2][batch][rows][pitch] with a 64 x box_rows box
 int encode_split_map(CUtensorMap* m, const void* base, int nk, int rows, int batch, int pitch, int box_rows);
-// N tile (64, 128, 144, 176 or 256 columns) for N output columns
-int umma_n_tile(int N);
+// N tile (256, 176, 128 or 64 columns): the widest that still gives
+// about one CTA per SM for an M x N x batch problem, else 64
+int umma_n_tile(int M, int N, int batch);
 cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const UmmaArgs& g, int nt, cudaStream_t s);
 
 // k = -(Gx + Gy); stage -1 writes k, stages 0..3 the RK4 update and clamp
