@@ -462,6 +462,68 @@ def run_lgl(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ot(args):
+    """2D ideal MHD: the Orszag-Tang vortex (rho = gamma^2, p = gamma, B0 = 1
+    on [0, 2 pi)^2, gamma = 5/3, filter p = 8, alpha = 36) at --ot-n^2, fixed
+    dt = 1e-3 RK4 steps with per-stage clamp and Helmholtz projection:
+    cell-updates/s, per-pass launch times against the measured HBM peak, and
+    the float64 oracle's step time on the host cores as the CPU baseline."""
+    import torch
+    from oracle import mhd as M
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.engine import Plan
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    n = args.ot_n
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    U0 = problems.orszag_tang_2d(n, n, gamma=5.0 / 3.0)
+    plan = Plan((n, n), (2 * np.pi, 2 * np.pi), gamma=5.0 / 3.0, filter_params=fp, device=device, equations="mhd")
+    U = torch.as_tensor(U0, dtype=torch.float32, device=device).contiguous()
+    plan.project_state_(U)
+    plan.run_(U, args.warmup, 1e-3)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    st = torch.cuda.current_stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    plan.run_(U, args.steps, 1e-3)
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    plan.profile(True)
+    plan.run_(U, 3, 1e-3)
+    prof = plan.collect_profile()
+    plan.profile(False)
+    peak, src = hbm_peak()
+    kinds = {}
+    for k, v in prof.items():
+        per = v["ms"] / v["launches"]
+        kinds[k] = {"launches_per_step": v["launches"] / 3, "us_per_launch": per * 1e3,
+                    "gbs": v["bytes"] / v["launches"] / (per * 1e-3) / 1e9,
+                    "frac_of_peak": v["bytes"] / v["launches"] / (per * 1e-3) / 1e9 / peak}
+    # CPU baseline: the float64 oracle, one step at a bounded size
+    s = M.MHDSolver2D(n, n, filter_params=fp)
+    R = s.project(U0)
+    t0 = time.perf_counter()
+    R = s.step(R, 1e-3)
+    cpu_s = time.perf_counter() - t0
+    G = U.cpu().numpy()
+    line = {
+        "metric": "2D ideal MHD Orszag-Tang: cell-updates/s (RK4, per-stage projection)", "value": n * n / (ms * 1e-3),
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (analytic Orszag-Tang initial condition)",
+        "config": {"workload": f"Orszag-Tang {n}^2, gamma 5/3, filter p=8 alpha=36, RK4 dt=1e-3"},
+        "passes": kinds, "peak_gbs": peak, "peak_source": src,
+        "cpu_baseline": {"value": n * n / cpu_s, "unit": "cell-updates/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"1 RK4 step of the float64 oracle at {n}^2"},
+        "state_finite": bool(np.isfinite(G).all()), "status": plan.status(), "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serving(args):
     """Serving: a seeded Poisson stream (200 requests/s) mixing Sod 1D,
     KHI 2D, Orszag-Tang MHD, TGV 3D and LGL acoustic solves with t_end ~
@@ -520,7 +582,7 @@ def run_serving(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving"], default="tgv")
+    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot"], default="tgv")
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
@@ -533,6 +595,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--ot-n", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -554,6 +617,9 @@ def main():
         elif args.workload == "serving":
             if rank == 0:
                 run_serving(args)
+        elif args.workload == "ot":
+            if rank == 0:
+                run_ot(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
