@@ -340,17 +340,22 @@ static cudaError_t umma_t(const CUtensorMap& mA, const CUtensorMap& mB, const Um
   return cudaGetLastError();
 }
 
+// Resident CTAs per SM of each N tile (shared memory: NT = 64 runs 2 stages in
+// 97 KB, two per SM; the others 150-200 KB, one per SM).  The smallest tile
+// whose grid fits in one wave gives the most parallelism; a grid too large for
+// one wave takes the widest tile (fewest re-reads of the A operand).
 int umma_n_tile(int M, int N, int batch) {
   const long mt = (M + 127) / 128;
-  const int cand[4] = {256, 176, 128, 64};
-  for (int nt : cand)
-    if (mt * ((N + nt - 1) / nt) * batch >= 148 || nt == 64) return nt;
-  return 64;
+  const int cand[4] = {64, 128, 176, 256};
+  const int per_sm[4] = {2, 1, 1, 1};
+  for (int i = 0; i < 4; ++i)
+    if (mt * ((N + cand[i] - 1) / cand[i]) * batch <= 148L * per_sm[i]) return cand[i];
+  return 256;
 }
 
 cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const UmmaArgs& g, int nt, cudaStream_t s) {
   switch (nt) {
-    case 64: return umma_t<64, 4>(mA, mB, g, s);
+    case 64: return umma_t<64, 2>(mA, mB, g, s);
     case 128: return umma_t<128, 3>(mA, mB, g, s);
     case 176: return umma_t<176, 2>(mA, mB, g, s);
     case 256: return umma_t<256, 2>(mA, mB, g, s);

@@ -38,8 +38,8 @@ struct UmmaArgs {
 };
 // tensor map over split planes [2][batch][rows][pitch] with a 64 x box_rows box
 int encode_split_map(CUtensorMap* m, const void* base, int nk, int rows, int batch, int pitch, int box_rows);
-// N tile (256, 176, 128 or 64 columns): the widest that still gives
-// about one CTA per SM for an M x N x batch problem, else 64
+// N tile (64, 128, 176 or 256 columns) for an M x N x batch problem: the
+// smallest whose grid fits in one wave of resident CTAs, else 256
 int umma_n_tile(int M, int N, int batch);
 cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const UmmaArgs& g, int nt, cudaStream_t s);
 
