@@ -75,7 +75,22 @@ typedef struct {
   int mhd_divergence_clean;    /* 1: Helmholtz projection, 0: none (default 1) */
   double mhd_resistivity;      /* eta; must be 0 (explicit diffusion not built) */
   double mhd_viscosity;        /* nu;  must be 0                                */
+  /* Artificial viscosity, 1D/2D Euler (SpectralArtificialViscosity,
+   * artificial_viscosity.py:37-403): rhs_c += div(w_c nu grad U_c) with
+   * nu = av_nu_max ((s > av_s_min ? s : 0) / av_s_ref)^av_p and
+   * s = clip(|grad q| / (|q| + av_epsilon) / av_s_ref, 0, 1), or nu constant. */
+  int av_mode;                 /* PS_AV_OFF, PS_AV_SENSOR, PS_AV_CONSTANT       */
+  int av_sensor;               /* PS_AV_Q_*: the sensor variable q              */
+  double av_nu_max, av_nu_constant, av_s_ref, av_s_min, av_p, av_epsilon;
+  double av_weight[5];         /* w_c per state component                       */
 } ps_plan_desc;
+
+#define PS_AV_OFF 0
+#define PS_AV_SENSOR 1
+#define PS_AV_CONSTANT 2
+#define PS_AV_Q_DENSITY 0
+#define PS_AV_Q_PRESSURE 1 /* 1D: p; 2D: u_y, as the reference's sensor unpacks it */
+#define PS_AV_Q_SPEED 2    /* |u| (1D only)                                     */
 
 /* Fill a descriptor with the reference defaults for `ndim` (dealias on,
  * filter off with p=8, alpha=36, interval 1, gamma 1.4, cfl 0.4/0.3/0.25,

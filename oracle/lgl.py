@@ -97,7 +97,7 @@ class LGLSolver2D:
     then BCs after the step."""
 
     def __init__(self, nx: int, ny: int, lx: float = 2.0, ly: float = 2.0, gamma: float = 1.4,
-                 filter_params: Optional[dict] = None, cfl: float = 0.3):
+                 filter_params: Optional[dict] = None, cfl: float = 0.3, gravity: Optional[Tuple[float, float]] = None):
         self.ax = LGLAxis(nx, lx)
         self.ay = LGLAxis(ny, ly)
         self.gamma = gamma
@@ -108,6 +108,7 @@ class LGLSolver2D:
         self.Fy = self.ay.nodal_filter(int(fp.get("p", 8)), float(fp.get("alpha", 36.0))) if self.filter else None
         self.step_counter = 0
         self.interval = max(1, int(fp.get("interval", 1) or 1))
+        self.gravity = gravity
 
     def dx(self, f):
         return f @ self.ax.D.T
@@ -123,7 +124,13 @@ class LGLSolver2D:
         mx, my = rho * vel[0], rho * vel[1]
         Fx = np.array([mx, mx * vel[0] + p, mx * vel[1], (E + p) * vel[0]])
         Fy = np.array([my, my * vel[0], my * vel[1] + p, (E + p) * vel[1]])
-        return -(self.dx(Fx) + self.dy(Fy))
+        r = -(self.dx(Fx) + self.dy(Fy))
+        if self.gravity is not None:  # solver.py:453-464
+            gx, gy = self.gravity
+            r[1] += rho * gx
+            r[2] += rho * gy
+            r[3] += rho * (gx * vel[0] + gy * vel[1])
+        return r
 
     def clamp(self, U):
         return positivity_clamp(U, self.gamma, 1e-8, 1e-10)

@@ -220,7 +220,9 @@ class EulerSolver:
     the step) and 259-269 (the cadence filter applied again).
     2D: solver.py:428-524 (clamp each stage, filter by cadence) and 637-648.
     3D: solver.py:1177-1237 (no clamp), 1330-1337 (filter every step).
-    Gravity (solver.py:82-91, 453-464, 1193-1206) is supported as constant g.
+    Gravity (solver.py:82-91, 453-464, 1193-1206) is supported as constant g;
+    artificial viscosity in 1D/2D (solver.py:73-78, 446-451; the 3D solver
+    passes none, 1330-1337).
     """
 
     box: FourierBox
@@ -229,6 +231,7 @@ class EulerSolver:
     filter_interval: int = 1
     gravity: Optional[Sequence[float]] = None
     step_counter: int = 0
+    av: Optional[Dict] = None  # artificial-viscosity config (1D/2D), see av_terms
 
     @property
     def ndim(self) -> int:
@@ -238,11 +241,61 @@ class EulerSolver:
         """Direction 0=x,1=y,2=z → spatial axis index in array order."""
         return self.ndim - 1 - direction
 
+    def av_terms(self, U: np.ndarray) -> np.ndarray:
+        """SpectralArtificialViscosity.compute_viscosity_terms
+        (artificial_viscosity.py:270-403, config 37-105, sensor 124-190,
+        coefficient 193-235): sensor s = clip(|grad q| / (|q| + eps) / s_ref,
+        0, 1) on q = density, pressure or |u|; nu = nu_max ((s > s_min ? s : 0)
+        / s_ref)^p (or a constant); term_i = div(w_i nu grad U_i), with the
+        weight looked up by position in the fixed name list."""
+        cfg = self.av
+        d = self.ndim
+        axes = [self.flux_axis_index(a) for a in range(d)]
+        mode = str(cfg.get("mode", "sensor")).lower().strip()
+        if mode == "constant":
+            nu = float(cfg.get("nu_constant", 0.0))
+            if nu == 0.0:
+                nu = float(cfg.get("nu_max", 1e-3))
+            nu = np.full_like(U[0], nu)
+        else:
+            var = cfg.get("sensor_variable", "density")
+            rho, vel, p = primitive(U, self.gamma)
+            if var == "density":
+                q = U[0]
+            elif var == "pressure":
+                # the sensor unpacks `_, _, p, _ = primitive(U)` (artificial_viscosity.py:131):
+                # in 1D that is p, in 2D (rho, ux, uy, p) it is uy
+                q = p if d == 1 else vel[1]
+            elif d == 1:
+                q = np.abs(vel[0])
+            else:
+                raise NotImplementedError("the reference's 2D velocity_magnitude sensor broadcasts rows of ux")
+            grads = [self.box.deriv(q, ax) for ax in axes]
+            gm = np.abs(grads[0]) if d == 1 else np.sqrt(sum(g * g for g in grads))
+            sref = float(cfg.get("s_ref", 1.0))
+            sen = gm / (np.abs(q) + float(cfg.get("epsilon", 1e-12)))
+            if sref > 0:
+                sen = np.clip(sen / sref, 0.0, 1.0)
+            act = np.where(sen > float(cfg.get("s_min", 0.1)), sen, 0.0)
+            if sref > 0:
+                act = act / sref
+            nu = float(cfg.get("nu_max", 1e-3)) * act ** float(cfg.get("p", 2.0))
+        names = ["density", "momentum_x", "momentum_y", "momentum_z", "energy"]
+        weights = cfg.get("variable_weights", None) or {}
+        out = np.zeros_like(U)
+        for i in range(U.shape[0]):
+            w = float(weights.get(names[i], 1.0))
+            for ax in axes:
+                out[i] += self.box.deriv(nu * w * self.box.deriv(U[i], ax), ax)
+        return out
+
     def rhs(self, U: np.ndarray) -> np.ndarray:
         F = fluxes(U, self.gamma)
         r = np.zeros_like(U)
         for a, Fa in enumerate(F):
             r -= self.box.deriv(Fa, self.flux_axis_index(a))
+        if self.av is not None and self.ndim < 3:
+            r += self.av_terms(U)
         if self.gravity is not None:
             d = self.ndim
             rho, vel, p = primitive(U, self.gamma)

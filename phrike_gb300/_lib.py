@@ -19,6 +19,8 @@ PS_BASIS_FOURIER = 0
 PS_BASIS_LEGENDRE = 1
 PS_EQ_EULER = 0
 PS_EQ_MHD = 1
+PS_AV_OFF, PS_AV_SENSOR, PS_AV_CONSTANT = 0, 1, 2
+PS_AV_Q_DENSITY, PS_AV_Q_PRESSURE, PS_AV_Q_SPEED = 0, 1, 2
 PS_GEMM_FP32 = 0
 PS_GEMM_FP64 = 1
 PS_GEMM_BF16X3 = 2
@@ -50,6 +52,15 @@ class PlanDesc(C.Structure):
         ("mhd_divergence_clean", C.c_int),
         ("mhd_resistivity", C.c_double),
         ("mhd_viscosity", C.c_double),
+        ("av_mode", C.c_int),
+        ("av_sensor", C.c_int),
+        ("av_nu_max", C.c_double),
+        ("av_nu_constant", C.c_double),
+        ("av_s_ref", C.c_double),
+        ("av_s_min", C.c_double),
+        ("av_p", C.c_double),
+        ("av_epsilon", C.c_double),
+        ("av_weight", C.c_double * 5),
     ]
 
 

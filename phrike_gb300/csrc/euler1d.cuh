@@ -35,6 +35,7 @@ struct Step1DArgs {
   const double* tend;    // per-solve end time
   float cfl, dx;
   int* steps_done;       // per-solve count of steps taken (CFL mode; may be null)
+  AVParams av;           // artificial viscosity (mode 0: off)
 };
 
 template <int N>
@@ -80,6 +81,16 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
   const float href = a.gamma * er;
   const float pmin_shift = a.p_min - g1 * er;
 
+  // w <- scale * D w for a packed pair (two real pencils)
+  auto deriv_pair = [&](float2 (&w)[B], float scale) {
+    pf.fwd(w);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const float dd = scale * S.ax.d[pf.kidx(r)];
+      w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
+    }
+    pf.inv(w);
+  };
   auto filter_pair = [&](float2 (&w)[B]) {  // complementary form
     float2 w0[B];
 #pragma unroll
@@ -146,6 +157,41 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
         w2[r] = make_float2(w2[r].y * dd, -w2[r].x * dd);
       }
       pf.inv(w2);
+      if (a.av.mode != 0) {
+        // artificial viscosity (artificial_viscosity.py:270-403): gradients of
+        // (q, U_0) and (U_1, U_2) packed in two transforms, nu per point, then
+        // the divergence of the viscous fluxes w_c nu dU_c/dx
+        float2 g0[B], g1v[B];
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          const float rho = S.us[sl(0, n2)], m = S.us[sl(1, n2)], E = S.us[sl(2, n2)];
+          const float u = m / rho;
+          float q = rho;
+          if (a.av.sensor == 1) q = g1 * (E - 0.5f * rho * u * u) + g1 * er;  // true pressure
+          else if (a.av.sensor == 2) q = fabsf(u);
+          g0[n2] = make_float2(q, rho);
+          g1v[n2] = make_float2(m, E);
+        }
+        float qv[B];
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) qv[n2] = g0[n2].x;
+        deriv_pair(g0, 1.0f);
+        deriv_pair(g1v, 1.0f);
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          const float nu = av_nu(a.av, fabsf(g0[n2].x), qv[n2]);
+          g0[n2] = make_float2(a.av.w[0] * nu * g0[n2].y, a.av.w[1] * nu * g1v[n2].x);
+          g1v[n2] = make_float2(a.av.w[2] * nu * g1v[n2].y, 0.0f);
+        }
+        deriv_pair(g0, 1.0f);
+        deriv_pair(g1v, 1.0f);
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          w01[n2].x += g0[n2].x;
+          w01[n2].y += g0[n2].y;
+          w2[n2].x += g1v[n2].x;
+        }
+      }
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
         float k[3] = {w01[n2].x, w01[n2].y, w2[n2].x};

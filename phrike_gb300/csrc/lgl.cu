@@ -366,6 +366,12 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
       float k[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) k[c] = -(Gx[c * cells + o] + (float)acc[c][m][q]);
+      if (a.gravity) {  // rho g on the momenta, g . m on the energy, from the stage input
+        const float rho = U[o], mx = U[cells + o], my = U[2 * cells + o];
+        k[1] = fmaf(rho, a.g[0], k[1]);
+        k[2] = fmaf(rho, a.g[1], k[2]);
+        k[3] += a.g[0] * mx + a.g[1] * my;
+      }
       if (a.stage < 0) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) a.out[so + c * cells + o] = k[c];

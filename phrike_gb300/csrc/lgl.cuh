@@ -58,6 +58,8 @@ struct LglStageArgs {
   double dt;
   float rho_min, p_min;  // 2D clamp floors
   int nsolve;
+  float g[2];            // constant gravity (solver.py:453-464); gravity = 0: off
+  int gravity;
 };
 
 cudaError_t launch_lgl_build(int n, double length, double* x, double* w, double* D, float* D32, cudaStream_t s);

@@ -65,6 +65,9 @@ LglStageArgs stage_args(ps_plan p, const float* in, int stage, const float* Un, 
   a.rho_min = 1e-8f;  // 2D clamp floors (solver.py:489-490)
   a.p_min = 1e-10f;
   a.nsolve = p->nsolve;
+  a.g[0] = (float)p->desc.gravity[0];
+  a.g[1] = (float)p->desc.gravity[1];
+  a.gravity = (p->desc.gravity[0] != 0.0 || p->desc.gravity[1] != 0.0) ? 1 : 0;
   return a;
 }
 
@@ -149,6 +152,10 @@ int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, do
   u.p_min = 1e-10f;
   u.eref = p->eref;
   u.active = act;
+  u.Uin = in;
+  u.g[0] = (float)p->desc.gravity[0];
+  u.g[1] = (float)p->desc.gravity[1];
+  u.gravity = (p->desc.gravity[0] != 0.0 || p->desc.gravity[1] != 0.0) ? 1 : 0;
   const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
   ProfScope prof(p, s, PS_KIND_LAST, words * field_bytes(p));
   LGL_CU(launch_lgl_update(u, s), "LGL stage update");
@@ -251,6 +258,8 @@ int lgl_validate(const ps_plan_desc* d) {
   }
   if (!(d->gamma > 1.0)) return errorf(PS_ERR_INVALID, "gamma must exceed 1");
   if (d->filter_interval < 1) return errorf(PS_ERR_INVALID, "filter_interval must be >= 1");
+  if (d->av_mode != PS_AV_OFF)
+    return errorf(PS_ERR_UNSUPPORTED, "artificial viscosity is not implemented for LGL grids");
   if (d->gemm_precision < PS_GEMM_FP32 || d->gemm_precision > PS_GEMM_BF16X3_SIMT)
     return errorf(PS_ERR_INVALID,
                   "gemm_precision must be PS_GEMM_FP32, PS_GEMM_FP64, PS_GEMM_BF16X3 or PS_GEMM_BF16X3_SIMT");

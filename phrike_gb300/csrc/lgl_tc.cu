@@ -378,6 +378,12 @@ __global__ void k_lgl_update(LglUpdateArgs a) {
     float k[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) k[c] = -(a.Gx[so + c * cells + o] + a.Gy[so + c * cells + o]);
+    if (a.gravity) {  // rho g on the momenta, g . m on the energy (solver.py:453-464)
+      const float rho = a.Uin[so + o], mx = a.Uin[so + cells + o], my = a.Uin[so + 2 * cells + o];
+      k[1] = fmaf(rho, a.g[0], k[1]);
+      k[2] = fmaf(rho, a.g[1], k[2]);
+      k[3] += a.g[0] * mx + a.g[1] * my;
+    }
     if (a.stage < 0) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) a.out[so + c * cells + o] = k[c];

@@ -58,6 +58,9 @@ struct LglUpdateArgs {
   float gamma, rho_min, p_min;
   const float* eref;
   const int* active;
+  const float* Uin;  // stage input (gravity source)
+  float g[2];
+  int gravity;
 };
 cudaError_t launch_lgl_update(const LglUpdateArgs& a, cudaStream_t s);
 

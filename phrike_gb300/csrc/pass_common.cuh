@@ -126,4 +126,24 @@ __device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, flo
   u[ND + 1] = pc / (gamma - 1.0f) + 0.5f * rc * kin;
 }
 
+// Artificial-viscosity parameters (artificial_viscosity.py:37-105, 193-235)
+struct AVParams {
+  int mode;      // 0 off, 1 sensor, 2 constant
+  int sensor;    // 0 density, 1 pressure (2D: u_y), 2 |u|
+  float nu_max, nu_const, s_ref, s_min, p, eps;
+  float w[5];    // per-component weights
+};
+
+// Viscosity coefficient from |grad q| and q: the sensor
+// s = clip(|grad q| / (|q| + eps) / s_ref, 0, 1) (s_ref > 0), then
+// nu = nu_max ((s > s_min ? s : 0) / s_ref)^p; constant mode returns nu_const.
+__device__ __forceinline__ float av_nu(const AVParams& av, float gradmag, float q) {
+  if (av.mode == 2) return av.nu_const;
+  float s = gradmag / (fabsf(q) + av.eps);
+  if (av.s_ref > 0.0f) s = fminf(fmaxf(s / av.s_ref, 0.0f), 1.0f);
+  float act = (s > av.s_min) ? s : 0.0f;
+  if (av.s_ref > 0.0f) act = act / av.s_ref;
+  return av.nu_max * powf(act, av.p);
+}
+
 }  // namespace ps

@@ -277,7 +277,27 @@ struct LastTArgs {
   int filter_last;
   int* status;
   int mhd;             // 1: 2D ideal MHD (8 components, the PHYS = 1 kernel)
+  // constant gravity (solver.py:453-464, 1193-1206): rhs_m += rho g, rhs_E += g . m,
+  // from the stage input Uin (same layout and solve stride as Un)
+  const float* Uin;
+  float grav[3];
+  int gravity;
 };
+
+// Gravity source at one point of solve-local offset o (element index of
+// component 0): adds rho g to the momenta and g . m to the energy of k.
+template <int ND>
+__device__ __forceinline__ void gravity_source(const LastTArgs& a, const float* uin, long o, long fs,
+                                               float (&k)[ND + 2]) {
+  const float rho = uin[o];
+  float gm = 0.0f;
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    k[1 + d] = fmaf(rho, a.grav[d], k[1 + d]);
+    gm = fmaf(a.grav[d], uin[o + (1 + d) * fs], gm);
+  }
+  k[ND + 1] += gm;
+}
 
 // PHYS 0: Euler (ND + 2 components, energy-perturbation clamp); PHYS 1: 2D
 // ideal MHD (8 components, MHD clamp, mhd_passes.cuh).
@@ -367,6 +387,20 @@ __global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_block
       const int m = two ? 2 : 1;
       float2 w[B];
       rhs_pair(c, w);
+      if constexpr (PHYS == 0) {
+        if (a.gravity && valid) {  // components (c, c+1) of rho g / g . m
+          const float* uin = a.Uin + (long)sol * a.ssUn;
+#pragma unroll
+          for (int n2 = 0; n2 < B; ++n2) {
+            float kk[ND + 2];
+#pragma unroll
+            for (int q = 0; q < ND + 2; ++q) kk[q] = 0.0f;
+            gravity_source<ND>(a, uin, addr(0, n2), a.fs, kk);
+            w[n2].x += kk[c];
+            if (two) w[n2].y += kk[c + 1];
+          }
+        }
+      }
       if (a.stage < 0) {
         if (valid) {
 #pragma unroll
@@ -420,6 +454,23 @@ __global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_block
     float2 kk[(NC + 1) / 2][B];
 #pragma unroll
     for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
+    if constexpr (PHYS == 0) {
+      if (a.gravity && valid) {
+        const float* uin = a.Uin + (long)sol * a.ssUn;
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) {
+          float k[NC];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) k[c] = (c & 1) ? kk[c / 2][n2].y : kk[c / 2][n2].x;
+          gravity_source<ND>(a, uin, addr(0, n2), a.fs, k);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            if (c & 1) kk[c / 2][n2].y = k[c];
+            else kk[c / 2][n2].x = k[c];
+          }
+        }
+      }
+    }
     if (a.stage < 0) {
       if (valid) {
 #pragma unroll

@@ -65,6 +65,9 @@ struct ps_plan_s {
   double* F64[2] = {nullptr, nullptr};    // nodal filter matrices (filter on)
   float* F32[2] = {nullptr, nullptr};
   double lgl_hmin = 0.0;                  // smallest node spacing (CFL)
+  // artificial viscosity (1D in the step kernel; 2D through av_buf, 21 fields per solve)
+  ps::AVParams av{};
+  float* av_buf = nullptr;
   // 2D ideal MHD (PS_EQ_MHD): half spectra of the Helmholtz projection
   bool mhd = false;
   float2* H = nullptr;                    // [nsolve][2][ny][nx/2+1]

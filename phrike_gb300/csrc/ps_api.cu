@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/phrike_gb300.h"
+#include "av.cuh"
 #include "launch.cuh"
 #include "lgl.cuh"
 #include "plan.cuh"
@@ -95,7 +96,32 @@ int validate(const ps_plan_desc* d) {
   }
   if (!(d->gamma > 1.0)) return fail(PS_ERR_INVALID, "gamma must exceed 1");
   if (d->filter_interval < 1) return fail(PS_ERR_INVALID, "filter_interval must be >= 1");
+  if (d->av_mode != PS_AV_OFF) {
+    if (d->av_mode != PS_AV_SENSOR && d->av_mode != PS_AV_CONSTANT)
+      return fail(PS_ERR_INVALID, "av_mode must be PS_AV_OFF, PS_AV_SENSOR or PS_AV_CONSTANT");
+    if (d->ndim == 3 || d->equations != PS_EQ_EULER)
+      return fail(PS_ERR_UNSUPPORTED,
+                  "artificial viscosity is defined for 1D/2D Euler (the reference's 3D solver passes none)");
+    if (d->av_sensor < PS_AV_Q_DENSITY || d->av_sensor > PS_AV_Q_SPEED)
+      return fail(PS_ERR_INVALID, "av_sensor out of range");
+    if (d->ndim == 2 && d->av_sensor == PS_AV_Q_SPEED)
+      return fail(PS_ERR_UNSUPPORTED, "the 2D velocity-magnitude sensor is not supported");
+  }
   return PS_OK;
+}
+
+ps::AVParams av_params(const ps_plan_desc* d) {
+  ps::AVParams a{};
+  a.mode = d->av_mode;
+  a.sensor = d->av_sensor;
+  a.nu_max = (float)d->av_nu_max;
+  a.nu_const = (float)d->av_nu_constant;
+  a.s_ref = (float)d->av_s_ref;
+  a.s_min = (float)d->av_s_min;
+  a.p = (float)d->av_p;
+  a.eps = (float)d->av_epsilon;
+  for (int c = 0; c < 5; ++c) a.w[c] = (float)d->av_weight[c];
+  return a;
 }
 
 size_t scratch_fields(int nd, bool mhd = false) {
@@ -352,6 +378,13 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   a.eref = p->eref;
   a.filter_last = filter_last ? 1 : 0;
   a.status = p->status;
+  a.Uin = (stage <= 0) ? Un : p->Us;  // the stage input: U^n at stage 0 and for a bare rhs
+  a.gravity = 0;
+  for (int d = 0; d < p->nd && d < 3; ++d) {
+    a.grav[d] = (float)p->desc.gravity[d];
+    if (p->desc.gravity[d] != 0.0) a.gravity = 1;
+  }
+  if (p->mhd) a.gravity = 0;
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
@@ -389,12 +422,69 @@ int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, doub
   a.cfl = (float)p->desc.cfl;
   a.dx = (float)(p->desc.length[0] / p->n[0]);
   a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
+  a.av = p->av;
   ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3 * p->nsolve);
   cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
     return ps::launch_step1d<decltype(nc)::value>(a, p->nsolve, s);
   });
   if (e != cudaSuccess) return cuda_fail(e, "1D step");
   if (d_t == nullptr) p->step_counter += nsteps;
+  return PS_OK;
+}
+
+// 2D artificial viscosity, before the stage's x pass: gradients of the stage
+// input S (and of the sensor variable), nu and the viscous fluxes, then their
+// x factors into the av_buf fields TA (D_x of the x fluxes) and TB (P_x of the
+// y fluxes), which av_apply subtracts from the Euler x-pass outputs.
+int av_prepass(ps_plan p, const float* S, cudaStream_t s, const int* act) {
+  int rc;
+  const long c = p->cells * p->nsolve;
+  float* TA = p->av_buf;
+  float* TB = TA + 4 * c;
+  float* GX = TB + 4 * c;
+  float* GY = GX + 4 * c;
+  float* Q = GY + 4 * c;
+  float* QA = Q + c;
+  float* QB = QA + c;
+  float* QX = QB + c;
+  float* QY = QX + c;
+  if ((rc = apply_op(p, 0, S, TA, 4, 1, 1.0f, s, false, act)) != PS_OK) return rc;  // D_x U
+  if ((rc = apply_op(p, 0, S, TB, 4, 0, 1.0f, s, false, act)) != PS_OK) return rc;  // P_x U
+  if ((rc = apply_op(p, 1, TA, GX, 4, 0, 1.0f, s, false, act)) != PS_OK) return rc; // dx1 U
+  if ((rc = apply_op(p, 1, TB, GY, 4, 1, 1.0f, s, false, act)) != PS_OK) return rc; // dy1 U
+  ps::AVFluxArgs f{};
+  f.GX = GX;
+  f.GY = GY;
+  f.cells = p->cells;
+  f.ssG = p->ss(4);
+  f.ssS = p->ss(4);
+  f.av = p->av;
+  if (p->av.mode == PS_AV_SENSOR && p->av.sensor == PS_AV_Q_PRESSURE) {
+    PS_CU(ps::launch_av_uy(S, p->cells, p->ss(4), p->nsolve, Q, s), "AV sensor variable");
+    if ((rc = apply_op(p, 0, Q, QA, 1, 1, 1.0f, s, false, act)) != PS_OK) return rc;
+    if ((rc = apply_op(p, 0, Q, QB, 1, 0, 1.0f, s, false, act)) != PS_OK) return rc;
+    if ((rc = apply_op(p, 1, QA, QX, 1, 0, 1.0f, s, false, act)) != PS_OK) return rc;
+    if ((rc = apply_op(p, 1, QB, QY, 1, 1, 1.0f, s, false, act)) != PS_OK) return rc;
+    f.q = Q;
+    f.qx = QX;
+    f.qy = QY;
+    f.ssQ = p->cells;
+  } else {  // density: q = rho, its gradients are the first fields of GX, GY
+    f.q = S;
+    f.qx = GX;
+    f.qy = GY;
+    f.ssQ = p->ss(4);
+  }
+  PS_CU(ps::launch_av_flux(f, p->nsolve, s), "AV fluxes");
+  if ((rc = apply_op(p, 0, GX, TA, 4, 1, 1.0f, s, false, act)) != PS_OK) return rc;  // D_x (w nu dx1 U)
+  if ((rc = apply_op(p, 0, GY, TB, 4, 0, 1.0f, s, false, act)) != PS_OK) return rc;  // P_x (w nu dy1 U)
+  return PS_OK;
+}
+
+int av_apply(ps_plan p, cudaStream_t s) {
+  const long c = p->cells * p->nsolve;
+  PS_CU(ps::launch_av_sub(p->G, p->ss(8), p->av_buf, p->av_buf + 4 * c, p->ss(4), p->cells, p->nsolve, s),
+        "AV terms");
   return PS_OK;
 }
 
@@ -422,7 +512,9 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
     for (int stage = 0; stage < 4; ++stage) {
       const float* src = (stage == 0) ? U : p->Us;
       float* Uw = (stage == 0 && pending_px) ? U : nullptr;
+      if (p->av_buf && (rc = av_prepass(p, src, s, act)) != PS_OK) return rc;
       if ((rc = xfirst(p, src, Uw, (cfl && stage == 0) ? p->speed : nullptr, s, false, act)) != PS_OK) return rc;
+      if (p->av_buf && (rc = av_apply(p, s)) != PS_OK) return rc;
       if (cfl && stage == 0)
         PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
               "step control");
@@ -433,7 +525,13 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
     pending_px = false;
     if (filt) {
       if (p->nd == 3 && (rc = apply_op(p, 1, U, U, p->nc, 0, 1.0f, s, true, act)) != PS_OK) return rc;
-      pending_px = true;
+      if (p->av_buf) {
+        // the viscosity pre-pass of the next step reads the state, so the
+        // filter's x factor is applied now instead of in the next x pass
+        if ((rc = apply_op(p, 0, U, U, p->nc, 0, 1.0f, s, true, act)) != PS_OK) return rc;
+      } else {
+        pending_px = true;
+      }
     }
     if (cfl)
       PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->active, p->steps_done, p->nsolve, s), "step advance");
@@ -595,6 +693,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
   }
+  p->av = av_params(d);
+  if (d->av_mode != PS_AV_OFF && p->nd == 2 && (rc = dalloc(p, &p->av_buf, 21 * c)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->speed, nsolve)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->eref, nsolve)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->dt, nsolve)) != PS_OK) return cleanup(rc);
@@ -643,6 +743,13 @@ int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   d->filter_alpha = 36.0;
   d->filter_interval = 1;
   d->cfl = (ndim == 1) ? 0.4 : (ndim == 2) ? 0.3 : 0.25;
+  d->av_mode = PS_AV_OFF;
+  d->av_nu_max = 1e-3;  // ArtificialViscosityConfig defaults (artificial_viscosity.py:55-63)
+  d->av_s_ref = 1.0;
+  d->av_s_min = 0.1;
+  d->av_p = 2.0;
+  d->av_epsilon = 1e-12;
+  for (int c = 0; c < 5; ++c) d->av_weight[c] = 1.0;
   d->mhd_rho_min = 1e-10;
   d->mhd_p_min = 1e-12;
   d->mhd_project_substages = 1;
@@ -660,8 +767,9 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
   if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
-  *bytes = scratch_fields(d->ndim, d->equations == PS_EQ_MHD) * (size_t)cells * sizeof(float) * nsolve + tables +
-           64 + 32 * (size_t)nsolve;
+  size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
+  if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
+  *bytes = fields * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
 
@@ -741,12 +849,16 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
     return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
   }
   if (p->nd == 1) {
+    if (p->av.mode != PS_AV_OFF || p->desc.gravity[0] != 0.0)
+      return fail(PS_ERR_UNSUPPORTED, "1D ps_rhs covers the flux divergence only (no gravity or viscosity terms)");
     PS_CU(ps::launch_flux1d(U, p->cells, p->ss(3), p->nsolve, (float)p->desc.gamma, p->F1, s), "1D flux");
     return apply_op(p, 0, p->F1, rhs, 3, 1, -1.0f, s);
   }
   PS_CU(ps::launch_eref_set(U + (long)(p->nc - 1) * p->cells, p->ss(p->nc), p->nsolve, p->eref, s),
         "energy reference");
+  if (p->av_buf && (rc = av_prepass(p, U, s, nullptr)) != PS_OK) return rc;
   if ((rc = xfirst(p, U, nullptr, nullptr, s, true)) != PS_OK) return rc;
+  if (p->av_buf && (rc = av_apply(p, s)) != PS_OK) return rc;
   if (p->nd == 3 && (rc = ymid(p, s, nullptr)) != PS_OK) return rc;
   return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
 }

@@ -111,6 +111,8 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   long cells = 1;
   for (int a = 0; a < desc->ndim; ++a) {
     if (desc->basis[a] != PS_BASIS_FOURIER) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: Fourier basis only");
+  if (desc->av_mode != PS_AV_OFF || desc->gravity[0] != 0.0 || desc->gravity[1] != 0.0 || desc->gravity[2] != 0.0)
+    return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: no artificial viscosity or gravity terms");
     if (!ps::supported_n(desc->n[a]))
       return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: axis length must be a power of two in 8..1024");
     if (!(desc->length[a] > 0.0)) return fail(PS_ERR_INVALID, "ps_rhs_static: lengths must be positive");

@@ -52,7 +52,8 @@ class Plan:
                  dealias: bool = True, filter_params: Optional[Dict] = None,
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
-                 gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None):
+                 gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None,
+                 av_config: Optional[Dict] = None):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -89,6 +90,32 @@ class Plan:
             desc.mhd_divergence_clean = 0 if str(mc.get("divergence_clean", "projection")) == "none" else 1
             desc.mhd_resistivity = float(mc.get("resistivity", 0.0))
             desc.mhd_viscosity = float(mc.get("viscosity", 0.0))
+        if av_config and av_config.get("enabled", False):
+            # ArtificialViscosityConfig fields and defaults (artificial_viscosity.py:37-105)
+            mode = str(av_config.get("mode", "sensor")).lower().strip()
+            if mode not in ("sensor", "constant"):
+                raise ValueError(f"Invalid mode '{mode}'. Must be 'sensor' or 'constant'")
+            desc.av_mode = _lib.PS_AV_SENSOR if mode == "sensor" else _lib.PS_AV_CONSTANT
+            sensors = {"density": _lib.PS_AV_Q_DENSITY, "pressure": _lib.PS_AV_Q_PRESSURE,
+                       "velocity_magnitude": _lib.PS_AV_Q_SPEED}
+            var = av_config.get("sensor_variable", "density")
+            if var not in sensors:
+                raise ValueError(f"Unknown sensor variable: {var}")
+            desc.av_sensor = sensors[var]
+            nu_c = float(av_config.get("nu_constant", 0.0))
+            if mode == "constant" and nu_c < 0:
+                raise ValueError("nu_constant must be non-negative")
+            desc.av_nu_max = float(av_config.get("nu_max", 1e-3))
+            desc.av_nu_constant = nu_c if nu_c != 0.0 else desc.av_nu_max
+            desc.av_s_ref = float(av_config.get("s_ref", 1.0))
+            desc.av_s_min = float(av_config.get("s_min", 0.1))
+            desc.av_p = float(av_config.get("p", 2.0))
+            desc.av_epsilon = float(av_config.get("epsilon", 1e-12))
+            # weights by position in the reference's fixed name list
+            names = ["density", "momentum_x", "momentum_y", "momentum_z", "energy"]
+            wts = av_config.get("variable_weights", None) or {}
+            for c in range(5):
+                desc.av_weight[c] = float(wts.get(names[c], 1.0))
         desc.gamma = float(gamma)
         desc.dealias = 1 if dealias else 0
         fp = filter_params or {}

@@ -29,13 +29,16 @@ class _SpectralSolverBase:
             raise NotImplementedError(f"backend 'gb300' implements the fixed-step rk4 scheme (got {scheme!r})")
         if adaptive_config and adaptive_config.get("enabled", False):
             raise NotImplementedError("backend 'gb300': adaptive embedded RK is not implemented")
+        av = None
         if artificial_viscosity_config and artificial_viscosity_config.get("enabled", False):
-            raise NotImplementedError("backend 'gb300': artificial viscosity is not implemented")
+            if self._ndim == 3:
+                artificial_viscosity_config = None  # the reference's 3D solver ignores it (solver.py:1266, 1330-1337)
+            else:
+                av = dict(artificial_viscosity_config)
         gravity = None
         if gravity_config and gravity_config.get("enabled", False):
-            if self._ndim != 1:
-                raise NotImplementedError("backend 'gb300': gravity is implemented for 1D only")
-            gravity = [float(gravity_config.get("gx", 0.0))]
+            # (gx[, gy[, gz]]) along x, y, z (solver.py:82-91, 453-464, 1193-1206)
+            gravity = [float(gravity_config.get(k, 0.0)) for k in ("gx", "gy", "gz")[: self._ndim]]
         self.grid = grid
         self.equations = equations
         self.scheme = "rk4"
@@ -43,17 +46,19 @@ class _SpectralSolverBase:
         self.t = 0.0
         self.U = U0
         self.adaptive_enabled = False
-        self.artificial_viscosity = None
         self.gravity_config = gravity_config
         fp = dict(getattr(grid, "filter_params", None) or {})
         interval = fp.get("interval", None)
-        self.filter_interval = max(1, int(interval)) if interval is not None else 1
+        # 1D: cadence 5 by default when artificial viscosity is on (solver.py:220-232)
+        default_interval = 5 if (av is not None and self._ndim == 1) else 1
+        self.filter_interval = max(1, int(interval)) if interval is not None else default_interval
+        self.artificial_viscosity = av
         fp["interval"] = self.filter_interval
         self.plan = Plan(grid._shape, grid._lengths, gamma=float(equations.gamma), dealias=grid.dealias,
                          filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device,
                          basis=getattr(grid, "_basis", "fourier"),
                          gemm_precision=getattr(grid, "gemm_precision", "fp32"), equations=self._equations,
-                         mhd_config=getattr(grid, "mhd_config", None))
+                         mhd_config=getattr(grid, "mhd_config", None), av_config=av)
 
     # -- reference interface -----------------------------------------------
     def _spacing(self) -> float:
@@ -189,7 +194,9 @@ class SpectralSolverMHD2D(_SpectralSolverBase):
         if gravity_config and gravity_config.get("enabled", False):
             raise NotImplementedError("backend 'gb300': gravity is not implemented for MHD")
         self.dim = 2
-        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, artificial_viscosity_config, None)
+        # the reference's MHD solver takes artificial_viscosity_config for API
+        # compatibility and does not use it
+        super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, None, None)
 
     def _spacing(self) -> float:
         return min(self.grid.dx, self.grid.dy)

@@ -43,6 +43,8 @@ def main(ref_path: str, only: str = "") -> None:
     from phrike_gb300 import problems
     if only == "mhd":
         return mhd_fixtures(grid, equations, solver, problems)
+    if only == "sources":
+        return source_fixtures(grid, equations, solver, problems)
 
     out = {}
 
@@ -147,8 +149,56 @@ def main(ref_path: str, only: str = "") -> None:
                             amp=0.2, width2=0.05)
 
     mhd_fixtures(grid, equations, solver, problems)
+    source_fixtures(grid, equations, solver, problems)
     print("golden fixtures written to", HERE)
 
+
+def source_fixtures(grid, equations, solver, problems) -> None:
+    """Gravity (2D KHI, 3D TGV) and artificial viscosity (1D Sod, 2D KHI,
+    sensor and constant modes) through the reference's NumPy path."""
+    grav2 = {"enabled": True, "gx": 0.3, "gy": -1.0}
+    grav3 = {"enabled": True, "gx": 0.2, "gy": -0.5, "gz": 1.0}
+    out = {}
+    g2 = grid.Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, dealias=True)
+    s2 = solver.SpectralSolver2D(g2, equations.EulerEquations2D(gamma=1.4), cfl=0.4, gravity_config=grav2)
+    U0 = problems.kelvin_helmholtz_2d(32, 32, U0=1.2, A=0.015)
+    U = U0.copy()
+    for _ in range(3):
+        U = s2.step(U, 2e-3)
+    out["grav2d_U0"], out["grav2d_U"] = U0, U
+    out["grav2d_rhs0"] = solver._compute_rhs_2d(g2, s2.equations, U0.copy(), None, grav2)
+    g3 = grid.Grid3D(Nx=16, Ny=16, Nz=16, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, dealias=True)
+    s3 = solver.SpectralSolver3D(g3, equations.EulerEquations3D(gamma=1.4), cfl=0.25, gravity_config=grav3)
+    T0 = problems.taylor_green_3d(16, 16, 16)
+    T = T0.copy()
+    for _ in range(2):
+        T = s3.step(T, 1e-3)
+    out["grav3d_U0"], out["grav3d_U"] = T0, T
+    out["grav3d_rhs0"] = solver._compute_rhs_3d(g3, s3.equations, T0.copy(), None, grav3)
+    # artificial viscosity, 1D (sensor mode, default cadence 5) and 2D (sensor / constant)
+    av_sensor = {"enabled": True, "mode": "sensor", "nu_max": 2e-3, "s_ref": 1.0, "s_min": 0.1, "p": 2.0,
+                 "epsilon": 1e-12, "sensor_variable": "density"}
+    g1 = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params={"enabled": True, "p": 8, "alpha": 36.0})
+    s1 = solver.SpectralSolver1D(g1, equations.EulerEquations1D(gamma=1.4), cfl=0.4,
+                                 artificial_viscosity_config=av_sensor)
+    S0 = problems.sod_smoothed(128)
+    S = S0.copy()
+    for _ in range(7):
+        S = s1.step(S, 2e-5)
+    out["av1d_U0"], out["av1d_U"], out["av1d_interval"] = S0, S, s1.filter_interval
+    out["av1d_rhs0"] = solver._compute_rhs(g1, s1.equations, S0.copy(), s1.artificial_viscosity, None)
+    for mode, cfg in (("sensor", dict(av_sensor, sensor_variable="pressure")),
+                      ("constant", {"enabled": True, "mode": "constant", "nu_constant": 1e-3})):
+        g2b = grid.Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, dealias=True)
+        s2b = solver.SpectralSolver2D(g2b, equations.EulerEquations2D(gamma=1.4), cfl=0.4,
+                                      artificial_viscosity_config=cfg)
+        V = U0.copy()
+        for _ in range(3):
+            V = s2b.step(V, 2e-3)
+        out[f"av2d_{mode}_U"] = V
+        out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
+                                                           None)
+    np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
 
 def mhd_fixtures(grid, equations, solver, problems) -> None:
     """2D ideal MHD: Orszag-Tang (rho = gamma^2, p = gamma, B0 = 1 on
