@@ -36,17 +36,37 @@ struct Step1DArgs {
   float cfl, dx;
   int* steps_done;       // per-solve count of steps taken (CFL mode; may be null)
   AVParams av;           // artificial viscosity (mode 0: off)
+  float* scratch;        // N >= 4096: U^n and accumulator, [nsolve][6][N]
+};
+
+// N = 4096 keeps U^n and the accumulator in global scratch (6 fields per
+// solve, L2-resident) so that the rest fits in one CTA's shared memory.
+template <int N>
+struct Step1DGlobal {
+  static constexpr bool value = N >= 4096;
 };
 
 template <int N>
 struct Step1DSmem {
   AxisSmem<N> ax;
   float2 buf[Pencil<N, 1, false>::BUF];
-  float un[3 * N];
+  float un[Step1DGlobal<N>::value ? 1 : 3 * N];
   float us[3 * N];
-  float acc[3 * N];
+  float acc[Step1DGlobal<N>::value ? 1 : 3 * N];
   float red[32];
 };
+
+// w <- D w for a packed pair of real pencils (D = i k m s)
+template <int N, typename PF>
+__device__ __forceinline__ void deriv_pair(const PF& pf, const AxisSmem<N>& ax, float2 (&w)[Shape<N>::B]) {
+  pf.fwd(w);
+#pragma unroll
+  for (int r = 0; r < Shape<N>::B; ++r) {
+    const float dd = ax.d[pf.kidx(r)];
+    w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
+  }
+  pf.inv(w);
+}
 
 template <int N>
 __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
@@ -59,6 +79,8 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
   PF pf{0, t, S.buf, S.ax.twf, S.ax.twi};
   load_axis<N>(S.ax, a.ax);
   float* U = a.U + (long)blockIdx.x * a.solve_stride;
+  float* const s_un = Step1DGlobal<N>::value ? a.scratch + (long)blockIdx.x * 6 * N : S.un;
+  float* const s_acc = Step1DGlobal<N>::value ? s_un + 3 * N : S.acc;
   // private slots: (c*B + n2)*A + t  <-> position t + A*n2
   auto sl = [&](int c, int n2) { return (c * B + n2) * A + t; };
   const float er = U[2 * N];  // E_ref; U is written only after the last step
@@ -68,7 +90,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
     for (int n2 = 0; n2 < B; ++n2) {
       float v = U[c * N + t + A * n2];
       if (c == 2) v -= er;
-      S.un[sl(c, n2)] = v;
+      s_un[sl(c, n2)] = v;
       S.us[sl(c, n2)] = v;
     }
   __syncthreads();
@@ -81,16 +103,6 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
   const float href = a.gamma * er;
   const float pmin_shift = a.p_min - g1 * er;
 
-  // w <- scale * D w for a packed pair (two real pencils)
-  auto deriv_pair = [&](float2 (&w)[B], float scale) {
-    pf.fwd(w);
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-      const float dd = scale * S.ax.d[pf.kidx(r)];
-      w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
-    }
-    pf.inv(w);
-  };
   auto filter_pair = [&](float2 (&w)[B]) {  // complementary form
     float2 w0[B];
 #pragma unroll
@@ -115,9 +127,9 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
       float sm = 0.0f;
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        const float rho = S.un[sl(0, n2)];
-        const float u = S.un[sl(1, n2)] / rho;
-        const float pp = g1 * (S.un[sl(2, n2)] - 0.5f * rho * u * u) + g1 * er;  // true pressure
+        const float rho = s_un[sl(0, n2)];
+        const float u = s_un[sl(1, n2)] / rho;
+        const float pp = g1 * (s_un[sl(2, n2)] - 0.5f * rho * u * u) + g1 * er;  // true pressure
         sm = fmaxf(sm, fabsf(u) + sqrtf(a.gamma * pp / rho));
       }
       sm = block_max(sm, S.red);
@@ -175,16 +187,16 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
         float qv[B];
 #pragma unroll
         for (int n2 = 0; n2 < B; ++n2) qv[n2] = g0[n2].x;
-        deriv_pair(g0, 1.0f);
-        deriv_pair(g1v, 1.0f);
+        deriv_pair<N>(pf, S.ax, g0);
+        deriv_pair<N>(pf, S.ax, g1v);
 #pragma unroll
         for (int n2 = 0; n2 < B; ++n2) {
           const float nu = av_nu(a.av, fabsf(g0[n2].x), qv[n2]);
           g0[n2] = make_float2(a.av.w[0] * nu * g0[n2].y, a.av.w[1] * nu * g1v[n2].x);
           g1v[n2] = make_float2(a.av.w[2] * nu * g1v[n2].y, 0.0f);
         }
-        deriv_pair(g0, 1.0f);
-        deriv_pair(g1v, 1.0f);
+        deriv_pair<N>(pf, S.ax, g0);
+        deriv_pair<N>(pf, S.ax, g1v);
 #pragma unroll
         for (int n2 = 0; n2 < B; ++n2) {
           w01[n2].x += g0[n2].x;
@@ -206,11 +218,11 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
         for (int c = 0; c < 3; ++c) {
           const int s = sl(c, n2);
           if (stage == 3) {
-            u3[c] = fmaf(rc.wacc, k[c], S.acc[s]);
+            u3[c] = fmaf(rc.wacc, k[c], s_acc[s]);
           } else {
-            const float un = S.un[s];
-            const float ac = (stage == 0) ? un : S.acc[s];
-            S.acc[s] = fmaf(rc.wacc, k[c], ac);
+            const float un = s_un[s];
+            const float ac = (stage == 0) ? un : s_acc[s];
+            s_acc[s] = fmaf(rc.wacc, k[c], ac);
             u3[c] = fmaf(rc.wnext, k[c], un);
           }
         }
@@ -238,7 +250,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
       const float v[3] = {w01[n2].x, w01[n2].y, w2[n2].x};
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        S.un[sl(c, n2)] = v[c];
+        s_un[sl(c, n2)] = v[c];
         S.us[sl(c, n2)] = v[c];
       }
     }
@@ -252,7 +264,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int n2 = 0; n2 < B; ++n2) U[c * N + t + A * n2] = S.un[sl(c, n2)] + (c == 2 ? er : 0.0f);
+    for (int n2 = 0; n2 < B; ++n2) U[c * N + t + A * n2] = s_un[sl(c, n2)] + (c == 2 ? er : 0.0f);
 }
 
 }  // namespace ps

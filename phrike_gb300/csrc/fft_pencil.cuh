@@ -147,6 +147,8 @@ template <> struct Shape<256> { static constexpr int A = 16, B = 16; };
 // N > 256: G = N/256 groups of 16 threads (see PencilGrp)
 template <> struct Shape<512> { static constexpr int A = 32, B = 16; };
 template <> struct Shape<1024> { static constexpr int A = 64, B = 16; };
+template <> struct Shape<2048> { static constexpr int A = 128, B = 16; };  // 1D plans only
+template <> struct Shape<4096> { static constexpr int A = 256, B = 16; };
 
 // Exchange-buffer layout for T pencils.  Element (q, s) of pencil p, with
 // q in [0,B) and s in [0,A).  In the contiguous-lane layout (the A threads of
@@ -293,9 +295,12 @@ struct PencilGrp {
       const bool upper = (gg & h) != 0;
       const int j = gg % h;  // position inside the 2h block
       float c = 1.0f, sn = 0.0f;
-      if (h > 1) {  // W_{2h}^{j}: only h = 2 (G = 4) needs a non-trivial factor
+      if (h == 2) {  // W_4^{j}
         c = (j == 0) ? 1.0f : 0.0f;
         sn = (j == 0) ? 0.0f : -1.0f;
+      } else if (h > 2) {  // W_{2h}^{j} = exp(-i pi j / h)
+        sincospif((float)j / (float)h, &sn, &c);
+        sn = -sn;
       }
 #pragma unroll
       for (int r = 0; r < B; ++r) {
@@ -320,9 +325,11 @@ struct PencilGrp {
       const bool upper = (gg & h) != 0;
       const int j = gg % h;
       float c = 1.0f, sn = 0.0f;
-      if (h > 1) {  // conj(W_{2h}^{j})
+      if (h == 2) {  // conj(W_4^{j})
         c = (j == 0) ? 1.0f : 0.0f;
         sn = (j == 0) ? 0.0f : 1.0f;
+      } else if (h > 2) {  // conj(W_{2h}^{j}) = exp(+i pi j / h)
+        sincospif((float)j / (float)h, &sn, &c);
       }
 #pragma unroll
       for (int r = 0; r < B; ++r) {

@@ -35,6 +35,8 @@ template <int N> cudaError_t launch_proj_xi(const ProjArgs& a, cudaStream_t s);
 inline bool supported_n(int n) {
   return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512 || n == 1024;
 }
+// 1D plans (one CTA per solve, whole steps in shared memory) also take 2048 and 4096
+inline bool supported_n_1d(int n) { return supported_n(n) || n == 2048 || n == 4096; }
 
 // Calls f(std::integral_constant<int, N>) for the supported pencil length n.
 template <typename F>
@@ -50,6 +52,15 @@ cudaError_t dispatch_n(int n, F&& f) {
     case 1024: return f(std::integral_constant<int, 1024>{});
     default: return cudaErrorInvalidValue;
   }
+}
+
+// As dispatch_n, with the 1D-only lengths 2048 and 4096 (kern_n2048.cu,
+// kern_n4096.cu instantiate the 1D step kernel and the contiguous operator).
+template <typename F>
+cudaError_t dispatch_n_1d(int n, F&& f) {
+  if (n == 2048) return f(std::integral_constant<int, 2048>{});
+  if (n == 4096) return f(std::integral_constant<int, 4096>{});
+  return dispatch_n(n, f);
 }
 
 // Dynamic shared memory above 48 KB needs an opt-in; every pass kernel also
@@ -172,6 +183,29 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_proj_xi<NN, T>, sm)) != cudaSuccess) return e;                                \
     k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                   \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_step1d<NN>(const Step1DArgs& a, int nsolve, cudaStream_t s) {                    \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
+    k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
+    return cudaGetLastError();                                                                        \
+  }
+
+// Launchers of the 1D-only pencil lengths: the whole-step kernel and the
+// contiguous operator (ps_derivative / ps_filter / 1D ps_rhs).
+#define PS_DEFINE_LAUNCHERS_1D(NN)                                                                    \
+  template <>                                                                                         \
+  cudaError_t launch_op<NN>(bool strided, const OpArgs& a, cudaStream_t s) {                          \
+    if (strided) return cudaErrorInvalidValue;                                                        \
+    constexpr int T = Tile<NN>::TC;                                                                   \
+    const dim3 grid((a.rows + T - 1) / T);                                                            \
+    const size_t sm = sizeof(StridedSmem<NN, T, false>);                                              \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_op<NN, T, false>, sm)) != cudaSuccess) return e;                              \
+    k_op<NN, T, false><<<grid, Shape<NN>::A * T, sm, s>>>(a);                                         \
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \

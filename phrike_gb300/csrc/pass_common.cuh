@@ -57,6 +57,8 @@ template <> struct Tile<128> { static constexpr int TC = 16, TS = 16; };
 template <> struct Tile<256> { static constexpr int TC = 8, TS = 16; };
 template <> struct Tile<512> { static constexpr int TC = 4, TS = 16; };
 template <> struct Tile<1024> { static constexpr int TC = 2, TS = 8; };
+template <> struct Tile<2048> { static constexpr int TC = 1, TS = 1; };  // 1D plans only
+template <> struct Tile<4096> { static constexpr int TC = 1, TS = 1; };
 
 // Non-negative float max via integer compare (valid for x >= 0).
 __device__ __forceinline__ void atomic_max_nonneg(float* addr, float x) {

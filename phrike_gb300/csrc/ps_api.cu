@@ -90,8 +90,9 @@ int validate(const ps_plan_desc* d) {
   for (int a = 0; a < d->ndim; ++a) {
     if (d->basis[a] != PS_BASIS_FOURIER)
       return fail(PS_ERR_UNSUPPORTED, "axis %d: only the Fourier basis is supported by this plan type", a);
-    if (!ps::supported_n(d->n[a]))
-      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 8..1024)", a, d->n[a]);
+    if (d->ndim == 1 ? !ps::supported_n_1d(d->n[a]) : !ps::supported_n(d->n[a]))
+      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 8..%d)", a, d->n[a],
+                  d->ndim == 1 ? 4096 : 1024);
     if (!(d->length[a] > 0.0)) return fail(PS_ERR_INVALID, "axis %d: length must be positive", a);
   }
   if (!(d->gamma > 1.0)) return fail(PS_ERR_INVALID, "gamma must exceed 1");
@@ -260,7 +261,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
     a.deriv = deriv;
     a.scale = scale;
     a.complement = complement ? 1 : 0;
-    e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_op<decltype(nc)::value>(false, a, s); });
+    e = ps::dispatch_n_1d(p->n[0], [&](auto nc) { return ps::launch_op<decltype(nc)::value>(false, a, s); });
   } else {
     if (nf > 63) return fail(PS_ERR_INVALID, "at most 63 fields per operator call");
     CUtensorMap m;
@@ -423,8 +424,9 @@ int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, doub
   a.dx = (float)(p->desc.length[0] / p->n[0]);
   a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
   a.av = p->av;
+  a.scratch = p->acc;  // N >= 4096: U^n and accumulator in global scratch
   ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3 * p->nsolve);
-  cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
+  cudaError_t e = ps::dispatch_n_1d(p->n[0], [&](auto nc) {
     return ps::launch_step1d<decltype(nc)::value>(a, p->nsolve, s);
   });
   if (e != cudaSuccess) return cuda_fail(e, "1D step");
@@ -684,6 +686,7 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   const long c = p->cells * nsolve;
   if (p->nd == 1) {
     if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
+    if (p->n[0] >= 4096 && (rc = dalloc(p, &p->acc, 6 * c)) != PS_OK) return cleanup(rc);
   } else {
     const int ng = p->mhd ? 16 : (p->nd == 3) ? 15 : 8;
     if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
@@ -769,6 +772,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
+  if (d->ndim == 1 && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
   *bytes = fields * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }

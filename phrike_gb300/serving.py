@@ -372,7 +372,7 @@ def request_stream(count: int, rate: float = 200.0, seed: int = 20261203,
                    ) -> List[Request]:
     """Seeded Poisson stream mixing the five families with uniform size draws
     and t_end ~ U[t_end_range]."""
-    fam = families or {"sod1d": [256, 512, 1024], "khi2d": [128, 256, 512, 1024], "ot2d": [128, 256, 512],
+    fam = families or {"sod1d": [256, 512, 1024, 2048, 4096], "khi2d": [128, 256, 512, 1024], "ot2d": [128, 256, 512],
                        "tgv3d": [32, 64, 128], "lgl2d": [65, 129, 257, 513]}
     names = sorted(fam)
     rng = np.random.default_rng(seed)
