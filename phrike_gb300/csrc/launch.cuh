@@ -81,6 +81,55 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   return e;
 }
 
+// Strided passes at tile width T (2D plans choose 4, 8 or 16 columns; 3D
+// plans and the 1024-point pencils use TmaTile<N>::T only).
+template <int NN, int T>
+cudaError_t last_t_T(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, const CUtensorMap& mAcc,
+                     const LastTArgs& a, cudaStream_t s) {
+  constexpr int R = TmaTile<NN>::R;
+  const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);
+  const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);
+  cudaError_t e;
+  if (nd == 3) {
+    if constexpr (T == TmaTile<NN>::T) {
+      if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;
+      k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  } else if (a.mhd) {
+    if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;
+    k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+  } else {
+    if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;
+    k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+  }
+  return cudaGetLastError();
+}
+
+template <int NN, int T>
+cudaError_t op_t_T(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {
+  constexpr int R = TmaTile<NN>::R;
+  const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);
+  const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);
+  cudaError_t e;
+  if ((e = set_smem(k_op_t<NN, T, R>, sm)) != cudaSuccess) return e;
+  k_op_t<NN, T, R><<<grid, Shape<NN>::A * T, sm, s>>>(mIn, a);
+  return cudaGetLastError();
+}
+
+// Calls f(std::integral_constant<int, T>) for the tile width of a launch.
+template <int NN, typename F>
+cudaError_t dispatch_tcols(int tcols, F&& f) {
+  const int T = (tcols > 0) ? tcols : TmaTile<NN>::T;
+  if (T == 4) return f(std::integral_constant<int, 4>{});
+  if (T == 8) return f(std::integral_constant<int, 8>{});
+  if constexpr (TmaTile<NN>::T == 16) {
+    if (T == 16) return f(std::integral_constant<int, 16>{});
+  }
+  return cudaErrorInvalidValue;
+}
+
 #define PS_DEFINE_LAUNCHERS(NN)                                                                       \
   template <>                                                                                         \
   cudaError_t launch_xfirst<NN>(int nd, const XFirstArgs& a, cudaStream_t s) {                        \
@@ -123,31 +172,13 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   template <>                                                                                         \
   cudaError_t launch_last_t<NN>(int nd, const CUtensorMap& mAB, const CUtensorMap& mU,                \
                                 const CUtensorMap& mAcc, const LastTArgs& a, cudaStream_t s) {        \
-    constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
-    const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
-    cudaError_t e;                                                                                    \
-    if (nd == 3) {                                                                                    \
-      if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;                  \
-      k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);              \
-    } else if (a.mhd) {                                                                               \
-      if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;                \
-      k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);            \
-    } else {                                                                                          \
-      if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;                   \
-      k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);               \
-    }                                                                                                 \
-    return cudaGetLastError();                                                                        \
+    return dispatch_tcols<NN>(a.tcols, [&](auto tc) {                                                 \
+      return last_t_T<NN, decltype(tc)::value>(nd, mAB, mU, mAcc, a, s);                              \
+    });                                                                                               \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_op_t<NN>(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {             \
-    constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
-    const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_op_t<NN, T, R>, sm)) != cudaSuccess) return e;                                \
-    k_op_t<NN, T, R><<<grid, Shape<NN>::A * T, sm, s>>>(mIn, a);                                      \
-    return cudaGetLastError();                                                                        \
+    return dispatch_tcols<NN>(a.tcols, [&](auto tc) { return op_t_T<NN, decltype(tc)::value>(mIn, a, s); }); \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_xfirst_mhd<NN>(const MhdXArgs& a, cudaStream_t s) {                              \

@@ -277,6 +277,7 @@ struct LastTArgs {
   int filter_last;
   int* status;
   int mhd;             // 1: 2D ideal MHD (8 components, the PHYS = 1 kernel)
+  int tcols;           // 2D: columns per tile (4, 8, 16; 0: default) = the maps' box width
   // constant gravity (solver.py:453-464, 1193-1206): rhs_m += rho g, rhs_E += g . m,
   // from the stage input Uin (same layout and solve stride as Un)
   const float* Uin;
@@ -559,6 +560,7 @@ struct OpTArgs {
   float scale;
   int complement;
   int* status;
+  int tcols;       // columns per tile (4, 8, 16; 0: default) = the map's box width
 };
 
 template <int N, int T, int R>

@@ -44,6 +44,7 @@ struct ps_plan_s {
   const float* map_U_ptr = nullptr;
   CUtensorMap map_U_last{};  // state, last-pass pencils
   long step_counter = 0;
+  int tcols = 0;  // 2D: columns per strided-pass tile (0: the default for the pencil length)
   std::vector<void*> allocations;
   // launch profiling: CUDA events around every pass launch
   struct LaunchRec {

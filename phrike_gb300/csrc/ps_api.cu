@@ -196,11 +196,11 @@ namespace ps {
 // 4-D map over a [nf][Nz][Ny][Nx] float32 buffer (n = {Nx, Ny, Nz}) with the
 // tile box of the TMA strided passes for pencils along `axis` (1 = y, 2 = z).
 // Host-only: fills the 128-byte map, allocates nothing.
-int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis) {
+int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis, int tcols) {
   auto fn = encode_fn();
   if (!fn) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   const int naxis = n[axis];
-  const int T = (naxis >= 1024) ? 8 : 16;
+  const int T = (tcols > 0) ? tcols : (naxis >= 1024) ? 8 : 16;
   const cuuint32_t rows = (cuuint32_t)(naxis < 256 ? naxis : 256);
   const cuuint64_t cells = (cuuint64_t)n[0] * n[1] * n[2];
   const cuuint64_t dims[4] = {(cuuint64_t)n[0], (cuuint64_t)n[1], (cuuint64_t)n[2], (cuuint64_t)nf};
@@ -220,7 +220,7 @@ namespace {
 
 // maps over the batch: a buffer of nsolve solves x nf fields is nsolve*nf fields
 int make_map(CUtensorMap* m, const float* base, const ps_plan_s* p, int nf, int axis) {
-  return ps::encode_field_map(m, base, p->n, p->nsolve * nf, axis);
+  return ps::encode_field_map(m, base, p->n, p->nsolve * nf, axis, p->tcols);
 }
 
 // maps of the caller's state pointer (re-encoded when the pointer changes)
@@ -281,6 +281,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
     a.scale = scale;
     a.complement = complement ? 1 : 0;
     a.status = p->status;
+    a.tcols = (p->nd == 2) ? p->tcols : 0;
     e = ps::dispatch_n(p->n[axis], [&](auto nc) { return ps::launch_op_t<decltype(nc)::value>(m, a, s); });
   }
   if (e != cudaSuccess) return cuda_fail(e, "operator pass");
@@ -379,6 +380,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   a.eref = p->eref;
   a.filter_last = filter_last ? 1 : 0;
   a.status = p->status;
+  a.tcols = (p->nd == 2) ? p->tcols : 0;
   a.Uin = (stage <= 0) ? Un : p->Us;  // the stage input: U^n at stage 0 and for a bare rhs
   a.gravity = 0;
   for (int d = 0; d < p->nd && d < 3; ++d) {
@@ -697,6 +699,19 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
   }
   p->av = av_params(d);
+  if (p->nd == 2 && !lgl) {
+    // columns per strided-pass tile: the widest of 16, 8, 4 that still gives
+    // about two CTAs per SM (small grids get more, narrower CTAs)
+    const int cap = (p->n[1] >= 1024) ? 8 : 16;
+    p->tcols = 4;
+    for (int T = cap; T >= 4; T /= 2) {
+      if ((long)((p->n[0] + T - 1) / T) * nsolve >= 2L * 148) {
+        p->tcols = T;
+        break;
+      }
+    }
+    if (p->mhd && p->n[1] >= 512 && p->tcols > 8) p->tcols = 8;  // 8-component last pass: 256 threads
+  }
   if (d->av_mode != PS_AV_OFF && p->nd == 2 && (rc = dalloc(p, &p->av_buf, 21 * c)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->speed, nsolve)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->eref, nsolve)) != PS_OK) return cleanup(rc);

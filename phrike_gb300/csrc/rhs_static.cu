@@ -37,7 +37,7 @@
 
 namespace ps {
 int record_error(int code, const char* msg);
-int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis);
+int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis, int tcols = 0);
 }
 
 namespace {
