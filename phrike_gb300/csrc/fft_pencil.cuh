@@ -155,7 +155,11 @@ template <> struct Shape<4096> { static constexpr int A = 256, B = 16; };
 // a pencil are adjacent lanes) each pencil owns a padded block; in the strided
 // layout (lanes run over pencils) pencils are interleaved innermost.  Both are
 // bank-conflict free for the access patterns below.
-template <int N, int T, bool STRIDED>
+//
+// WSYNC: every pencil's threads sit in one warp and every warp is full
+// (contiguous layout, A <= 32, A*T a multiple of 32), so the exchanges only
+// need a warp barrier; warps then run their transforms independently.
+template <int N, int T, bool STRIDED, bool WSYNC = false>
 struct PencilBase {
   static constexpr int A = Shape<N>::A;
   static constexpr int B = Shape<N>::B;
@@ -163,6 +167,12 @@ struct PencilBase {
   static_assert(B % A == 0, "pencil shape needs B multiple of A");
   static constexpr int PAD = STRIDED ? 0 : 1;
   static constexpr int BUF = T * B * (A + PAD);  // float2 elements
+  static_assert(!WSYNC || (!STRIDED && A <= 32 && (A * T) % 32 == 0), "warp barrier needs warp-local pencils");
+
+  static __device__ __forceinline__ void bar() {
+    if constexpr (WSYNC) __syncwarp();
+    else __syncthreads();
+  }
 
   int p;   // pencil within the tile
   int t;   // thread within the pencil
@@ -183,12 +193,12 @@ struct PencilBase {
       constexpr int k2 = decltype(kc)::value;
       v[k2] = cmul(v[k2], twf[k2 * A + t]);
     });
-    __syncthreads();
+    bar();
     sfor<0, B>([&](auto kc) {
       constexpr int k2 = decltype(kc)::value;
       buf[xi(k2, t)] = v[k2];
     });
-    __syncthreads();
+    bar();
     sfor<0, J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       sfor<0, A>([&](auto nc) {
@@ -208,7 +218,7 @@ struct PencilBase {
         v[j * A + n1] = cmul(v[j * A + n1], twi[n1 * B + t + A * j]);
       });
     });
-    __syncthreads();
+    bar();
     sfor<0, J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       sfor<0, A>([&](auto nc) {
@@ -216,7 +226,7 @@ struct PencilBase {
         buf[xi(t + A * j, n1)] = v[j * A + n1];
       });
     });
-    __syncthreads();
+    bar();
     sfor<0, B>([&](auto kc) {
       constexpr int k2 = decltype(kc)::value;
       v[k2] = buf[xi(k2, t)];
@@ -226,12 +236,12 @@ struct PencilBase {
 
   // vn[r] = X[-k(r) mod N] for a pencil in spectral layout.
   __device__ __forceinline__ void negk(const float2 (&v)[B], float2 (&vn)[B]) const {
-    __syncthreads();
+    bar();
     sfor<0, B>([&](auto rc) {
       constexpr int r = decltype(rc)::value;
       buf[xi(t + A * (r / A), r % A)] = v[r];
     });
-    __syncthreads();
+    bar();
     sfor<0, B>([&](auto rc) {
       constexpr int r = decltype(rc)::value;
       constexpr int k1 = r % A;
@@ -262,7 +272,8 @@ struct PencilGrp {
   static constexpr int A = Shape<N>::A;  // 16 * G
   static constexpr int B = Shape<N>::B;  // 16
   static constexpr int LG = ilog2(G);
-  using Sub = PencilBase<256, T * G, STRIDED>;
+  // a pencil of A <= 32 threads is one full warp: its sub-pencils exchange within it
+  using Sub = PencilBase<256, T * G, STRIDED, (!STRIDED && A <= 32 && (A * T) % 32 == 0)>;
   static constexpr int BUF = Sub::BUF;
   static_assert(!STRIDED || T * G <= 32, "all groups of a pencil must share a warp");
 
@@ -351,6 +362,8 @@ struct PencilGrp {
 };
 
 template <int N, int T, bool STRIDED>
-using Pencil = typename std::conditional<(N > 256), PencilGrp<N, T, STRIDED>, PencilBase<N, T, STRIDED>>::type;
+using Pencil = typename std::conditional<
+    (N > 256), PencilGrp<N, T, STRIDED>,
+    PencilBase<N, T, STRIDED, (!STRIDED && Shape<N>::A <= 32 && (Shape<N>::A * T) % 32 == 0)>>::type;
 
 }  // namespace ps
