@@ -355,7 +355,8 @@ def run_ensemble(args):
         "data": "synthetic (seeded KHI initial conditions)",
         "config": {"workload": f"{args.nsolve} KHI 2D solves, N uniform on 64..512, CFL 0.4, t_end={args.t_end}",
                    "chunk_steps_per_graph": args.chunk},
-        "seconds": stats["seconds"], "cell_updates_per_s": stats["cell_updates_per_s"],
+        "seconds": stats["seconds"], "graph_capture_seconds": stats["capture_seconds"],
+        "cell_updates_per_s": stats["cell_updates_per_s"],
         "status": stats["status"],
         "plain_device_loop_solves_per_s": args.nsolve / plain_dev,
         "plain_host_loop_solves_per_s": args.nsolve / plain_host,
@@ -524,6 +525,116 @@ def run_ot(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adaptive(args):
+    """Adaptive embedded RK45 with the reference's shipped settings.
+    (a) configs/sod.yaml: 1D Sod N=1024, rk45, rtol 1e-6, atol 1e-8,
+        artificial viscosity (sensor, nu_max 1e-3), filter p=8 alpha=36, to
+        t_end=0.2: a batch of --nsolve solves with every attempt loop and
+        decision on the device (k_ark1d), against the float64 oracle run of
+        one solve on the host cores.
+    (b) configs/tgv3d.yaml: 3D TGV at --n^3, rk45, rtol 1e-5, atol 1e-7:
+        ms per attempt and cell-updates/s per accepted step.
+    Synthetic smoothed Sod (tanh edges) instead of the sharp step."""
+    import torch
+    from oracle import adaptive as A
+    from oracle import spectral as O
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.engine import Plan
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    f64 = dict(dtype=torch.float64, device=device)
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    av = {"enabled": True, "mode": "sensor", "nu_max": 1e-3, "s_ref": 1.0, "s_min": 0.1, "p": 2.0,
+          "epsilon": 1e-12, "sensor_variable": "density"}
+    N, t_end, ns = 1024, 0.2, args.nsolve
+    plan = Plan((N,), (1.0,), filter_params=fp, cfl=0.4, av_config=av, device=device, nsolve=ns)
+    ad = Plan.adaptive_desc({"scheme": "rk45", "rtol": 1e-6, "atol": 1e-8})
+    U0 = problems.sod_smoothed(N)
+    # a seeded spread of initial states so the solves take different step sequences
+    rng = np.random.default_rng(20261203)
+    amps = 1.0 + 0.2 * rng.random(ns)
+    base = np.stack([U0 * a for a in amps])
+    s1 = O.EulerSolver(O.FourierBox((N,), (1.0,), dealias=True, filter_enabled=True), cfl=0.4, av=av)
+    dt0 = np.array([s1.compute_dt(base[i]) for i in range(ns)])
+
+    def fresh():
+        U = torch.as_tensor(base, dtype=torch.float32, device=device).contiguous()
+        return (U, torch.zeros(ns, **f64), torch.full((ns,), t_end, **f64), torch.as_tensor(dt0, **f64),
+                torch.zeros((ns, 2), dtype=torch.int32, device=device))
+
+    U, t, te, dtv, cnt = fresh()
+    plan.run_adaptive_(U, 100000, ad, t, te, dtv, None, cnt)  # warm-up run (also builds the slope storage)
+    torch.cuda.synchronize()
+    U, t, te, dtv, cnt = fresh()
+    plan.adaptive_reset()
+    sampler = ClockSampler(0)
+    sampler.start()
+    st = torch.cuda.current_stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    plan.run_adaptive_(U, 100000, ad, t, te, dtv, None, cnt)
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    sec = e0.elapsed_time(e1) * 1e-3
+    c = cnt.cpu().numpy()
+    done = bool((t.cpu().numpy() >= t_end - 1e-12).all())
+    # CPU baseline: the float64 oracle's adaptive run of solve 0, bounded
+    cpu = None
+    if not args.no_cpu_baseline:
+        rhs, post = A.euler_hooks(s1)
+        t0 = time.perf_counter()
+        _, tc, log, _, _ = A.run_adaptive(rhs, post, base[0], 0.0, t_end, dt0[0], "rk45", A.Controller(),
+                                          max_attempts=200)
+        cs = time.perf_counter() - t0
+        per_attempt = cs / max(len(log), 1)
+        cpu = {"value": 1.0 / (per_attempt * (int(c[0].sum()))), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"{len(log)} attempts of solve 0 with the float64 oracle ({cs:.1f} s), scaled to its "
+                         f"{int(c[0].sum())} attempts"}
+    line1 = {
+        "metric": "adaptive RK45 1D Sod solves/s (decisions on the device)", "value": ns / sec, "unit": "solves/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic (smoothed Sod, seeded amplitudes)",
+        "config": {"workload": f"{ns} x Sod N={N}, rk45 rtol 1e-6 atol 1e-8, AV sensor nu_max 1e-3, "
+                               f"filter p=8 alpha=36, t_end={t_end}"},
+        "seconds": sec, "attempts_per_solve": float(c.sum(axis=1).mean()),
+        "accepted_per_solve": float(c[:, 0].mean()), "rejected_per_solve": float(c[:, 1].mean()),
+        "all_finished": done, "state_finite": bool(torch.isfinite(U).all().item()), "cpu_baseline": cpu,
+        "clocks": clocks, "gpu_launches": 1,
+    }
+    print(json.dumps(line1), flush=True)
+
+    # (b) 3D TGV
+    n = args.n
+    plan3 = Plan((n, n, n), (2 * np.pi,) * 3, cfl=0.25, device=device)
+    ad3 = Plan.adaptive_desc({"scheme": "rk45", "rtol": 1e-5, "atol": 1e-7})
+    T0 = torch.as_tensor(problems.taylor_green_3d(n), dtype=torch.float32, device=device).contiguous()
+    dt3 = float(plan3.max_wave_speed(T0).item())
+    dt3 = 0.25 * (2 * np.pi / n) / dt3
+    T = T0.clone()
+    t, te, dtv = torch.zeros(1, **f64), torch.full((1,), 1e9, **f64), torch.full((1,), dt3, **f64)
+    cnt = torch.zeros((1, 2), dtype=torch.int32, device=device)
+    plan3.run_adaptive_(T, max(args.warmup, 3), ad3, t, te, dtv, None, cnt)
+    torch.cuda.synchronize()
+    c0 = cnt.clone()
+    K = max(args.steps // 10, 5)
+    e0.record(st)
+    plan3.run_adaptive_(T, K, ad3, t, te, dtv, None, cnt)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    acc = int((cnt - c0)[0, 0].item())
+    line2 = {
+        "metric": "adaptive RK45 3D TGV: cell-updates/s per accepted step", "value": n ** 3 * acc / (ms * K * 1e-3),
+        "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (analytic Taylor-Green initial condition)",
+        "config": {"workload": f"TGV {n}^3, rk45 rtol 1e-5 atol 1e-7 (7 stages, FSAL not used, as the reference)"},
+        "ms_per_attempt": ms, "attempts": K, "accepted": acc, "status": plan3.status(),
+        "state_finite": bool(torch.isfinite(T).all().item()),
+    }
+    print(json.dumps(line2), flush=True)
+
+
 def run_serving(args):
     """Serving: a seeded Poisson stream (200 requests/s) mixing Sod 1D,
     KHI 2D, Orszag-Tang MHD, TGV 3D and LGL acoustic solves with t_end ~
@@ -582,7 +693,7 @@ def run_serving(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot"], default="tgv")
+    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive"], default="tgv")
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
@@ -620,6 +731,9 @@ def main():
         elif args.workload == "ot":
             if rank == 0:
                 run_ot(args)
+        elif args.workload == "adaptive":
+            if rank == 0:
+                run_adaptive(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:

@@ -83,7 +83,15 @@ typedef struct {
   int av_sensor;               /* PS_AV_Q_*: the sensor variable q              */
   double av_nu_max, av_nu_constant, av_s_ref, av_s_min, av_p, av_epsilon;
   double av_weight[5];         /* w_c per state component                       */
+  /* Fixed-step scheme of ps_step_rk4 / ps_run_steps / ps_run_cfl: classical
+   * RK4 (default) or the midpoint RK2 of _rk2_step / _rk2_step_2d /
+   * _rk2_step_3d / _rk_substages (solver.py:96-105, 492-500, 1211-1216,
+   * 992-996), with the same clamp, projection and filter placement. */
+  int scheme;                  /* PS_SCHEME_RK4 or PS_SCHEME_RK2                */
 } ps_plan_desc;
+
+#define PS_SCHEME_RK4 0
+#define PS_SCHEME_RK2 1
 
 #define PS_AV_OFF 0
 #define PS_AV_SENSOR 1
@@ -151,6 +159,47 @@ int ps_run_steps(ps_plan plan, float* U, int nsteps, double dt, const double* d_
  * happen): advance in chunks and read d_t between chunks.  Replaces the
  * while-loop of SpectralSolver*.run (solver.py:384-417, 773-800, 1480-1505). */
 int ps_run_cfl(ps_plan plan, float* U, int nsteps, double* d_t, const double* d_tend, void* stream);
+
+/* Adaptive embedded Runge-Kutta (adaptive.py:23-437).  Methods: */
+#define PS_ARK_RK23 0 /* Bogacki-Shampine 3(2)                                   */
+#define PS_ARK_RK45 1 /* Dormand-Prince 5(4)                                     */
+#define PS_ARK_RK78 2 /* the reference's simplified 8-stage "rk78" table        */
+typedef struct ps_adaptive_desc {
+  int method;            /* PS_ARK_*                                          */
+  double rtol, atol;     /* tol = atol + rtol * max|U|                        */
+  double safety_factor;  /* dt_new = dt * clip(safety (tol/err)^(1/order),    */
+  double min_dt_factor;  /*                     min_dt_factor, max_dt_factor) */
+  double max_dt_factor;
+  int max_rejections;    /* forced acceptance after this many in a row        */
+} ps_adaptive_desc;
+/* The reference's defaults: rk45, rtol 1e-6, atol 1e-8, safety 0.9, factors
+ * 0.1 and 5, 10 rejections (solver.py:182-193, adaptive.py:38-43). */
+void ps_adaptive_desc_init(ps_adaptive_desc* ad);
+
+/* Up to nattempts adaptive attempts per solve with every decision on the
+ * device.  Replaces the adaptive branch of SpectralSolver*.run
+ * (_adaptive_run_step, solver.py:295-323, 671-691, 1067-1084, 1360-1380).
+ * Per solve, an attempt runs while t < t_end - 1e-12 (and, if d_tout is
+ * non-NULL, while t + 1e-12 < t_out, so the host can record outputs at the
+ * reference's times): dt = min(d_dt, t_end - t); the embedded pair gives
+ * U_high and err = max|U_high - U_low|; the controller accepts when
+ * err <= atol + rtol * max|U| (or after max_rejections rejections in a row)
+ * and writes dt_next to d_dt.  An accepted attempt advances d_t and applies
+ * the solver's post-step operator: the spectral filter (Euler), or filter,
+ * clamp and projection (2D MHD).  The stage right-hand sides carry gravity;
+ * 1D ones also carry artificial viscosity (the 2D/3D reference passes none
+ * there).  No clamp inside the stages.
+ * d_t, d_dt: nsolve doubles (in/out); d_tend: nsolve doubles; d_tout:
+ * nullable; d_counts: nullable, nsolve x 2 ints to which accepted and
+ * rejected attempts are added.  Consecutive-rejection counts stay in the plan
+ * between calls (ps_adaptive_reset clears them).  The first call with a given
+ * method allocates the stage storage (stages x state size): make it outside
+ * any stream capture.  For 2D/3D grids nattempts is also the number of
+ * attempt launch sequences issued (paused or finished solves skip their
+ * work).  LGL grids return PS_ERR_UNSUPPORTED. */
+int ps_run_adaptive(ps_plan plan, float* U, int nattempts, const ps_adaptive_desc* ad, double* d_t,
+                    const double* d_tend, double* d_dt, const double* d_tout, int* d_counts, void* stream);
+int ps_adaptive_reset(ps_plan plan, void* stream);
 
 /* out = dx1/dy1/dz1(f) for nfields fields (axis 0 = x).  Replaces
  * Grid1D.dx1 (grid.py:512-522), Grid2D.dx1/dy1 (grid.py:1226-1252),

@@ -97,7 +97,8 @@ class LGLSolver2D:
     then BCs after the step."""
 
     def __init__(self, nx: int, ny: int, lx: float = 2.0, ly: float = 2.0, gamma: float = 1.4,
-                 filter_params: Optional[dict] = None, cfl: float = 0.3, gravity: Optional[Tuple[float, float]] = None):
+                 filter_params: Optional[dict] = None, cfl: float = 0.3, gravity: Optional[Tuple[float, float]] = None,
+                 scheme: str = "rk4"):
         self.ax = LGLAxis(nx, lx)
         self.ay = LGLAxis(ny, ly)
         self.gamma = gamma
@@ -109,6 +110,7 @@ class LGLSolver2D:
         self.step_counter = 0
         self.interval = max(1, int(fp.get("interval", 1) or 1))
         self.gravity = gravity
+        self.scheme = scheme
 
     def dx(self, f):
         return f @ self.ax.D.T
@@ -139,13 +141,17 @@ class LGLSolver2D:
         """The reference mutates U through the BCs of the first stage; the
         caller's array is modified the same way here."""
         k1 = self.rhs(U)
-        U2 = self.clamp(U + 0.5 * dt * k1)
-        k2 = self.rhs(U2)
-        U3 = self.clamp(U + 0.5 * dt * k2)
-        k3 = self.rhs(U3)
-        U4 = self.clamp(U + dt * k3)
-        k4 = self.rhs(U4)
-        Un = self.clamp(U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4))
+        if self.scheme == "rk2":  # _rk2_step_2d (solver.py:492-500)
+            U1 = self.clamp(U + dt * 0.5 * k1)
+            Un = self.clamp(U + dt * self.rhs(U1))
+        else:
+            U2 = self.clamp(U + 0.5 * dt * k1)
+            k2 = self.rhs(U2)
+            U3 = self.clamp(U + 0.5 * dt * k2)
+            k3 = self.rhs(U3)
+            U4 = self.clamp(U + dt * k3)
+            k4 = self.rhs(U4)
+            Un = self.clamp(U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4))
         if self.step_counter % self.interval == 0:
             if self.filter:
                 Un = np.matmul(self.Fy, Un @ self.Fx.T)

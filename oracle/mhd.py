@@ -95,7 +95,7 @@ class MHDSolver2D:
     def __init__(self, nx: int, ny: int, lx: float = 2 * np.pi, ly: float = 2 * np.pi, gamma: float = 5.0 / 3.0,
                  dealias: bool = True, filter_params: Optional[dict] = None, cfl: float = 0.3,
                  rho_min: float = 1e-10, p_min: float = 1e-12, project_each_substage: bool = True,
-                 divergence_clean: str = "projection"):
+                 divergence_clean: str = "projection", scheme: str = "rk4"):
         fp = filter_params or {}
         self.box = FourierBox((ny, nx), (ly, lx), dealias=dealias, filter_enabled=bool(fp.get("enabled", False)),
                               filter_p=int(fp.get("p", 8)), filter_alpha=float(fp.get("alpha", 36.0)))
@@ -106,6 +106,7 @@ class MHDSolver2D:
         self.divergence_clean = divergence_clean
         self.interval = max(1, int(fp.get("interval", 1) or 1))
         self.step_counter = 0
+        self.scheme = scheme
 
     def rhs(self, U: np.ndarray) -> np.ndarray:
         Fx, Fy = fluxes(U, self.gamma)
@@ -132,6 +133,13 @@ class MHDSolver2D:
     def step(self, U: np.ndarray, dt: float) -> np.ndarray:
         proj = self.project if self.project_each_substage else (lambda x: x)
         k1 = self.rhs(U)
+        if self.scheme == "rk2":  # _rk_substages midpoint branch (solver.py:992-996)
+            U1 = proj(self.clamp(U + 0.5 * dt * k1))
+            Un = proj(self.clamp(U + dt * self.rhs(U1)))
+            if self.step_counter % self.interval == 0:
+                Un = self.project(self.box.filt(Un))
+            self.step_counter += 1
+            return Un
         U2 = proj(self.clamp(U + 0.5 * dt * k1))
         k2 = self.rhs(U2)
         U3 = proj(self.clamp(U + 0.5 * dt * k2))

@@ -232,6 +232,7 @@ class EulerSolver:
     gravity: Optional[Sequence[float]] = None
     step_counter: int = 0
     av: Optional[Dict] = None  # artificial-viscosity config (1D/2D), see av_terms
+    scheme: str = "rk4"        # "rk4" or the midpoint "rk2"
 
     @property
     def ndim(self) -> int:
@@ -329,8 +330,19 @@ class EulerSolver:
             Un = self.box.filt(Un)  # inside _rk4_step (solver.py:119-120)
         return Un
 
+    def rk2(self, U: np.ndarray, dt: float) -> np.ndarray:
+        """Midpoint RK2 with the per-dimension clamp (solver.py:96-105,
+        492-500, 1211-1216)."""
+        k1 = self.rhs(U)
+        U1 = self.clamp(U + dt * 0.5 * k1)
+        k2 = self.rhs(U1)
+        Un = self.clamp(U + dt * k2)
+        if self.ndim == 1:
+            Un = self.box.filt(Un)  # inside _rk2_step (solver.py:104)
+        return Un
+
     def step(self, U: np.ndarray, dt: float) -> np.ndarray:
-        Un = self.rk4(U, dt)
+        Un = self.rk2(U, dt) if self.scheme == "rk2" else self.rk4(U, dt)
         if self.ndim == 3:
             Un = self.box.filt(Un)  # every step (solver.py:1336)
         elif self.step_counter % self.filter_interval == 0:

@@ -21,6 +21,7 @@ PS_EQ_EULER = 0
 PS_EQ_MHD = 1
 PS_AV_OFF, PS_AV_SENSOR, PS_AV_CONSTANT = 0, 1, 2
 PS_AV_Q_DENSITY, PS_AV_Q_PRESSURE, PS_AV_Q_SPEED = 0, 1, 2
+PS_SCHEME_RK4, PS_SCHEME_RK2 = 0, 1
 PS_GEMM_FP32 = 0
 PS_GEMM_FP64 = 1
 PS_GEMM_BF16X3 = 2
@@ -61,6 +62,24 @@ class PlanDesc(C.Structure):
         ("av_p", C.c_double),
         ("av_epsilon", C.c_double),
         ("av_weight", C.c_double * 5),
+        ("scheme", C.c_int),
+    ]
+
+
+PS_ARK_RK23, PS_ARK_RK45, PS_ARK_RK78 = 0, 1, 2
+ARK_METHODS = {"rk23": PS_ARK_RK23, "rk45": PS_ARK_RK45, "rk78": PS_ARK_RK78}
+
+
+class AdaptiveDesc(C.Structure):
+    """ps_adaptive_desc (include/phrike_gb300.h)."""
+    _fields_ = [
+        ("method", C.c_int),
+        ("rtol", C.c_double),
+        ("atol", C.c_double),
+        ("safety_factor", C.c_double),
+        ("min_dt_factor", C.c_double),
+        ("max_dt_factor", C.c_double),
+        ("max_rejections", C.c_int),
     ]
 
 
@@ -75,6 +94,10 @@ _SIGNATURES = [
     ("ps_plan_nsolve", C.c_int, [C.c_void_p]),
     ("ps_plan_steps_done", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("ps_run_cfl", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_adaptive_desc_init", None, [C.POINTER(AdaptiveDesc)]),
+    ("ps_run_adaptive", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(AdaptiveDesc), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_adaptive_reset", C.c_int, [C.c_void_p, C.c_void_p]),
     ("ps_rhs", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_step_rk4", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
     ("ps_run_steps", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),

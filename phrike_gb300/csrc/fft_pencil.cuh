@@ -166,7 +166,12 @@ struct PencilBase {
   static constexpr int J = B / A;
   static_assert(B % A == 0, "pencil shape needs B multiple of A");
   static constexpr int PAD = STRIDED ? 0 : 1;
-  static constexpr int BUF = T * B * (A + PAD);  // float2 elements
+  // contiguous layout: pencil blocks of B*(A+1) float2, rounded up to = A
+  // (mod 16) when A < 16, so that the pencils sharing a warp fall on
+  // different banks (A lanes x 8 bytes each)
+  static constexpr int PBLK0 = B * (A + PAD);
+  static constexpr int PBLK = (STRIDED || A >= 16) ? PBLK0 : PBLK0 + (((A - PBLK0 % 16) % 16) + 16) % 16;
+  static constexpr int BUF = STRIDED ? T * B * A : T * PBLK;  // float2 elements
   static_assert(!WSYNC || (!STRIDED && A <= 32 && (A * T) % 32 == 0), "warp barrier needs warp-local pencils");
 
   static __device__ __forceinline__ void bar() {
@@ -182,7 +187,7 @@ struct PencilBase {
 
   __device__ __forceinline__ int xi(int q, int s) const {
     if constexpr (STRIDED) return (q * A + s) * T + p;
-    else return p * (B * (A + PAD)) + q * (A + PAD) + s;
+    else return p * PBLK + q * (A + PAD) + s;
   }
   // spectral index of register r = j*A + k1
   __device__ __forceinline__ int kidx(int r) const { return t + A * (r / A) + B * (r % A); }

@@ -15,6 +15,7 @@ namespace ps {
 template <int N> cudaError_t launch_xfirst(int nd, const XFirstArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
+template <int N> cudaError_t launch_ark1d(const Ark1DArgs& a, int nsolve, cudaStream_t s);
 
 // TMA strided passes: columns per tile and ring depth per pencil length
 template <int N> struct TmaTile {
@@ -223,6 +224,14 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
     if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
     k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
     return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_ark1d<NN>(const Ark1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
+    k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
+    return cudaGetLastError();                                                                        \
   }
 
 // Launchers of the 1D-only pencil lengths: the whole-step kernel and the
@@ -245,6 +254,14 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
     k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_ark1d<NN>(const Ark1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
+    k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
     return cudaGetLastError();                                                                        \
   }
 

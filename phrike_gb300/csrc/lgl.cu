@@ -352,7 +352,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
   const long so = (long)sol * a.ss;
   const float* __restrict__ Gx = a.Gx + so;
   const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
-  const RKCoef rk = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
+  const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   const float pmin_shift = a.p_min - (a.gamma - 1.0f) * a.eref[sol];
 #pragma unroll
   for (int m = 0; m < TM; ++m) {

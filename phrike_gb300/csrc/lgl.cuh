@@ -60,6 +60,7 @@ struct LglStageArgs {
   int nsolve;
   float g[2];            // constant gravity (solver.py:453-464); gravity = 0: off
   int gravity;
+  int rk2;               // midpoint RK2 coefficients (stages 0 and 3 only)
 };
 
 cudaError_t launch_lgl_build(int n, double length, double* x, double* w, double* D, float* D32, cudaStream_t s);

@@ -68,6 +68,7 @@ LglStageArgs stage_args(ps_plan p, const float* in, int stage, const float* Un, 
   a.g[0] = (float)p->desc.gravity[0];
   a.g[1] = (float)p->desc.gravity[1];
   a.gravity = (p->desc.gravity[0] != 0.0 || p->desc.gravity[1] != 0.0) ? 1 : 0;
+  a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
   return a;
 }
 
@@ -156,6 +157,7 @@ int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, do
   u.g[0] = (float)p->desc.gravity[0];
   u.g[1] = (float)p->desc.gravity[1];
   u.gravity = (p->desc.gravity[0] != 0.0 || p->desc.gravity[1] != 0.0) ? 1 : 0;
+  u.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
   const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
   ProfScope prof(p, s, PS_KIND_LAST, words * field_bytes(p));
   LGL_CU(launch_lgl_update(u, s), "LGL stage update");
@@ -375,6 +377,7 @@ int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
              "step control");
     }
     for (int st = 0; st < 4; ++st) {
+      if (p->desc.scheme == PS_SCHEME_RK2 && (st == 1 || st == 2)) continue;  // midpoint RK2
       float* in = (st == 0) ? U : p->Us;
       float* out = (st < 3) ? p->Us : U;
       if ((rc = stage(p, in, st, U, out, dt, dtp, act, s)) != PS_OK) return rc;

@@ -372,7 +372,7 @@ __global__ void k_lgl_update(LglUpdateArgs a) {
   const long cells = a.cells;
   const long so = (long)sol * 4 * cells;
   const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
-  const RKCoef rk = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
+  const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   const float pmin_shift = a.p_min - (a.gamma - 1.0f) * a.eref[sol];
   for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < cells; o += (long)gridDim.x * blockDim.x) {
     float k[4];

@@ -61,6 +61,7 @@ struct LglUpdateArgs {
   const float* Uin;  // stage input (gravity source)
   float g[2];
   int gravity;
+  int rk2;  // midpoint RK2 coefficients (stages 0 and 3 only)
 };
 cudaError_t launch_lgl_update(const LglUpdateArgs& a, cudaStream_t s);
 

@@ -94,6 +94,15 @@ __device__ __forceinline__ RKCoef rk4_coef(int stage, float dt) {
   c.wnext = (stage == 2) ? dt : 0.5f * dt;
   return c;
 }
+// Midpoint RK2 (solver.py:96-105) on the same stage slots, stages 0 and 3
+// only: stage 0: acc = U, next = U + dt/2 k1; stage 3: new = acc + dt k2.
+__device__ __forceinline__ RKCoef rk_coef(int stage, float dt, int rk2) {
+  if (!rk2) return rk4_coef(stage, dt);
+  RKCoef c;
+  c.wacc = (stage == 0) ? 0.0f : dt;
+  c.wnext = 0.5f * dt;
+  return c;
+}
 
 // Energy-perturbation form.  Inside the engine the energy slot of a state holds
 // E' = E - E_ref for a per-run constant E_ref (the energy of the first cell

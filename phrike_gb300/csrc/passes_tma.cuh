@@ -283,6 +283,7 @@ struct LastTArgs {
   const float* Uin;
   float grav[3];
   int gravity;
+  int rk2;             // midpoint RK2 coefficients (stages 0 and 3 only)
 };
 
 // Gravity source at one point of solve-local offset o (element index of
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_block
   const long base = (long)outer * a.g.os + col + (long)t * a.g.as;  // within a solve
   const long step = (long)A * a.g.as;
   const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
-  const RKCoef rk = rk4_coef(a.stage < 0 ? 0 : a.stage, dt);
+  const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   const float pmin_shift = a.p_min - (a.gamma - 1.0f) * a.eref[sol];
   float* const acc_s = (a.acc != nullptr) ? a.acc + (long)sol * a.ssAcc : nullptr;
   float* const out_s = a.out + (long)sol * a.ssOut;

@@ -69,6 +69,13 @@ struct ps_plan_s {
   // artificial viscosity (1D in the step kernel; 2D through av_buf, 21 fields per solve)
   ps::AVParams av{};
   float* av_buf = nullptr;
+  // adaptive embedded RK: per-solve controller state and the stage slopes
+  int* ark_rej = nullptr;    // consecutive rejections
+  int* ark_ok = nullptr;     // attempt accepted
+  float* ark_err = nullptr;  // max |U_high - U_low|
+  float* ark_scale = nullptr;
+  float* ark_K = nullptr;    // allocated on first use: stages x state (1D N >= 4096: + U^n)
+  size_t ark_cap = 0;        // floats in ark_K
   // 2D ideal MHD (PS_EQ_MHD): half spectra of the Helmholtz projection
   bool mhd = false;
   float2* H = nullptr;                    // [nsolve][2][ny][nx/2+1]

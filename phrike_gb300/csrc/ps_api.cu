@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/phrike_gb300.h"
+#include "adaptive.cuh"
 #include "av.cuh"
 #include "launch.cuh"
 #include "lgl.cuh"
@@ -77,6 +78,8 @@ bool is_lgl(const ps_plan_desc* d) {
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
   if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
+  if (d->scheme != PS_SCHEME_RK4 && d->scheme != PS_SCHEME_RK2)
+    return fail(PS_ERR_INVALID, "scheme must be PS_SCHEME_RK4 or PS_SCHEME_RK2 (got %d)", d->scheme);
   if (is_lgl(d)) return ps::lgl_validate(d);
   if (d->equations == PS_EQ_MHD) {
     if (d->ndim != 2) return fail(PS_ERR_UNSUPPORTED, "MHD plans are 2D (got ndim %d)", d->ndim);
@@ -388,6 +391,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
     if (p->desc.gravity[d] != 0.0) a.gravity = 1;
   }
   if (p->mhd) a.gravity = 0;
+  a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
@@ -427,6 +431,7 @@ int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, doub
   a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
   a.av = p->av;
   a.scratch = p->acc;  // N >= 4096: U^n and accumulator in global scratch
+  a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
   ProfScope prof(p, s, PS_KIND_STEP1D, 2.0 * 4.0 * p->cells * 3 * p->nsolve);
   cudaError_t e = ps::dispatch_n_1d(p->n[0], [&](auto nc) {
     return ps::launch_step1d<decltype(nc)::value>(a, p->nsolve, s);
@@ -514,6 +519,7 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
   for (int it = 0; it < nsteps; ++it) {
     const bool filt = filter_due(p, p->step_counter);
     for (int stage = 0; stage < 4; ++stage) {
+      if (p->desc.scheme == PS_SCHEME_RK2 && (stage == 1 || stage == 2)) continue;  // midpoint RK2
       const float* src = (stage == 0) ? U : p->Us;
       float* Uw = (stage == 0 && pending_px) ? U : nullptr;
       if (p->av_buf && (rc = av_prepass(p, src, s, act)) != PS_OK) return rc;
@@ -626,6 +632,7 @@ int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
   for (int it = 0; it < nsteps; ++it) {
     const bool due = (p->step_counter % p->desc.filter_interval) == 0;
     for (int stage = 0; stage < 4; ++stage) {
+      if (p->desc.scheme == PS_SCHEME_RK2 && (stage == 1 || stage == 2)) continue;  // midpoint RK2
       const float* src = (stage == 0) ? U : p->Us;
       float* out = (stage < 3) ? p->Us : U;
       if ((rc = xfirst_mhd(p, src, (cfl && stage == 0) ? p->speed : nullptr, s, act)) != PS_OK) return rc;
@@ -644,6 +651,147 @@ int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
       PS_CU(ps::launch_step_advance(d_t, p->dt, p->speed, p->active, p->steps_done, p->nsolve, s), "step advance");
     p->step_counter += 1;
   }
+  return PS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adaptive embedded RK (adaptive.py:23-437 driven by the run loops of
+// solver.py).  1D: whole attempt loops in k_ark1d.  2D/3D and MHD: one launch
+// sequence per attempt, every decision on the device (adaptive.cu).
+// ---------------------------------------------------------------------------
+// stage-slope storage, grown on demand (the old buffer is released)
+int ark_ensure(ps_plan p, size_t floats) {
+  if (p->ark_cap >= floats) return PS_OK;
+  if (p->ark_K != nullptr) {
+    cudaFree(p->ark_K);
+    for (auto it = p->allocations.begin(); it != p->allocations.end(); ++it)
+      if (*it == p->ark_K) {
+        p->allocations.erase(it);
+        break;
+      }
+    p->ark_K = nullptr;
+    p->ark_cap = 0;
+  }
+  const int rc = dalloc(p, &p->ark_K, floats);
+  if (rc == PS_OK) p->ark_cap = floats;
+  return rc;
+}
+
+// nonzero a[i][j], j < i
+ps::ArkComb ark_row(const ps::ArkTableau& t, int i) {
+  ps::ArkComb c{};
+  for (int j = 0; j < i; ++j)
+    if (t.a[i][j] != 0.0) {
+      c.idx[c.m] = j;
+      c.c[c.m++] = t.a[i][j];
+    }
+  return c;
+}
+
+// U_high weights and the error weights bh - bl over the union of their supports
+void ark_final_combs(const ps::ArkTableau& t, ps::ArkComb* high, ps::ArkComb* diff) {
+  *high = ps::ArkComb{};
+  *diff = ps::ArkComb{};
+  for (int j = 0; j < t.stages; ++j) {
+    const double e = t.bh[j] - t.bl[j];
+    if (t.bh[j] == 0.0 && e == 0.0) continue;
+    high->idx[high->m] = j;
+    diff->idx[diff->m] = j;
+    high->c[high->m++] = t.bh[j];
+    diff->c[diff->m++] = e;
+  }
+}
+
+// k = rhs(src) of the adaptive stages: Euler flux divergence plus gravity (no
+// artificial viscosity, as the 2D/3D reference passes none), or the ideal MHD
+// flux divergence
+int ark_rhs(ps_plan p, const float* src, float* k, const int* act, cudaStream_t s) {
+  int rc;
+  if (p->mhd) {
+    if ((rc = xfirst_mhd(p, src, nullptr, s, act)) != PS_OK) return rc;
+  } else {
+    if ((rc = xfirst(p, src, nullptr, nullptr, s, false, act)) != PS_OK) return rc;
+    if (p->nd == 3 && (rc = ymid(p, s, act)) != PS_OK) return rc;
+  }
+  return last(p, -1, src, k, 0.0, nullptr, false, s, act);
+}
+
+int run_adaptive_nd(ps_plan p, float* U, int nattempts, const ps::ArkTableau& tab, const ps::ArkCtrl& ctrl,
+                    double* d_t, const double* d_tend, double* d_dt, const double* d_tout, int* d_counts,
+                    cudaStream_t s) {
+  int rc;
+  const int nc = p->nc;
+  const long n = (long)nc * p->cells;
+  const long ssU = p->ss(nc);
+  const long kstride = ssU * p->nsolve;
+  if ((rc = ark_ensure(p, (size_t)tab.stages * kstride)) != PS_OK) return rc;
+  const bool eprime = !p->mhd;  // Euler states run in the energy-perturbation form
+  float* UE = U + (long)(nc - 1) * p->cells;
+  if (eprime) {
+    PS_CU(ps::launch_eref_set(UE, ssU, p->nsolve, p->eref, s), "energy reference");
+    PS_CU(ps::launch_energy_shift(UE, p->cells, ssU, p->nsolve, p->eref, -1.0f, s), "energy shift");
+  }
+  const ps::ArkState st{d_t, d_tend, d_dt, d_tout, p->dt, p->active, p->ark_ok, p->ark_rej,
+                        p->ark_err, p->ark_scale, d_counts, p->nsolve};
+  ps::ArkComb high, diff;
+  ark_final_combs(tab, &high, &diff);
+  for (int it = 0; it < nattempts; ++it) {
+    PS_CU(ps::launch_ark_begin(st, s), "adaptive begin");
+    PS_CU(ps::launch_ark_scale(U, n, ssU, p->cells, eprime ? nc - 1 : -1, eprime ? p->eref : nullptr, st, s),
+          "adaptive scale");
+    for (int i = 0; i < tab.stages; ++i) {
+      const float* src = U;
+      if (i > 0) {
+        PS_CU(ps::launch_ark_stage(U, p->ark_K, kstride, p->Us, n, ssU, ark_row(tab, i), st, s), "adaptive stage");
+        src = p->Us;
+      }
+      if ((rc = ark_rhs(p, src, p->ark_K + (long)i * kstride, p->active, s)) != PS_OK) return rc;
+    }
+    PS_CU(ps::launch_ark_final(U, p->ark_K, kstride, p->acc, n, ssU, high, diff, st, s), "adaptive final");
+    PS_CU(ps::launch_ark_decide(st, tab.order, ctrl, s), "adaptive controller");
+    // post-step operator of accepted attempts: U <- filter(U_high) (Euler,
+    // solver.py:683-689, 1375-1380); MHD then clamps and projects (1077-1079)
+    if ((rc = apply_op(p, 0, p->acc, U, nc, 0, 1.0f, s, true, p->ark_ok)) != PS_OK) return rc;
+    for (int ax = 1; ax < p->nd; ++ax)
+      if ((rc = apply_op(p, ax, U, U, nc, 0, 1.0f, s, true, p->ark_ok)) != PS_OK) return rc;
+    if (p->mhd) {
+      PS_CU(ps::launch_ark_clamp_mhd(U, p->cells, ssU, p->nsolve, (float)p->desc.gamma, (float)p->desc.mhd_rho_min,
+                                     (float)p->desc.mhd_p_min, p->ark_ok, s),
+            "MHD clamp");
+      if ((rc = project_state(p, U, p->ark_ok, s)) != PS_OK) return rc;
+    }
+  }
+  if (eprime) PS_CU(ps::launch_energy_shift(UE, p->cells, ssU, p->nsolve, p->eref, 1.0f, s), "energy shift");
+  return PS_OK;
+}
+
+int run_adaptive_1d(ps_plan p, float* U, int nattempts, const ps::ArkTableau& tab, const ps::ArkCtrl& ctrl,
+                    double* d_t, const double* d_tend, double* d_dt, const double* d_tout, int* d_counts,
+                    cudaStream_t s) {
+  const int N = p->n[0];
+  const long per = (N >= 4096 ? 3L * N : 0L) + (long)tab.stages * 3 * N;
+  int rc;
+  if ((rc = ark_ensure(p, (size_t)per * p->nsolve)) != PS_OK) return rc;
+  ps::Ark1DArgs a{};
+  a.U = U;
+  a.solve_stride = p->ss(3);
+  a.ax = p->ax(0);
+  a.gamma = (float)p->desc.gamma;
+  a.av = p->av;
+  a.gx = (float)p->desc.gravity[0];
+  a.nattempts = nattempts;
+  a.tab = tab;
+  a.ctrl = ctrl;
+  a.t = d_t;
+  a.tend = d_tend;
+  a.dtp = d_dt;
+  a.tout = d_tout;
+  a.rej = p->ark_rej;
+  a.counts = d_counts;
+  a.scratch = p->ark_K;
+  a.scratch_stride = per;
+  cudaError_t e = ps::dispatch_n_1d(N, [&](auto nn) { return ps::launch_ark1d<decltype(nn)::value>(a, p->nsolve, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "1D adaptive kernel");
   return PS_OK;
 }
 
@@ -719,6 +867,11 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   if ((rc = dalloc(p, &p->active, nsolve)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->steps_done, nsolve)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->status, 1)) != PS_OK) return cleanup(rc);
+  if ((rc = dalloc(p, &p->ark_rej, nsolve)) != PS_OK || (rc = dalloc(p, &p->ark_ok, nsolve)) != PS_OK ||
+      (rc = dalloc(p, &p->ark_err, nsolve)) != PS_OK || (rc = dalloc(p, &p->ark_scale, nsolve)) != PS_OK)
+    return cleanup(rc);
+  if (cudaMemset(p->ark_rej, 0, sizeof(int) * nsolve) != cudaSuccess)
+    return cleanup(cuda_fail(cudaGetLastError(), "adaptive state"));
   if (cudaMemset(p->eref, 0, sizeof(float) * nsolve) != cudaSuccess ||
       cudaMemset(p->speed, 0, sizeof(float) * nsolve) != cudaSuccess ||
       cudaMemset(p->steps_done, 0, sizeof(int) * nsolve) != cudaSuccess ||
@@ -906,6 +1059,41 @@ int ps_run_cfl(ps_plan p, float* U, int nsteps, double* d_t, const double* d_ten
   if (p->mhd) return steps_mhd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   if (p->nd == 1) return step_1d(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
   return steps_nd(p, U, nsteps, 0.0, nullptr, d_t, d_tend, s);
+}
+
+void ps_adaptive_desc_init(ps_adaptive_desc* ad) {
+  if (!ad) return;
+  ad->method = PS_ARK_RK45;
+  ad->rtol = 1e-6;
+  ad->atol = 1e-8;
+  ad->safety_factor = 0.9;
+  ad->min_dt_factor = 0.1;
+  ad->max_dt_factor = 5.0;
+  ad->max_rejections = 10;
+}
+
+int ps_run_adaptive(ps_plan p, float* U, int nattempts, const ps_adaptive_desc* ad, double* d_t,
+                    const double* d_tend, double* d_dt, const double* d_tout, int* d_counts, void* stream) {
+  if (!p || !U || !ad || !d_t || !d_tend || !d_dt) return fail(PS_ERR_INVALID, "null argument");
+  if (nattempts < 0) return fail(PS_ERR_INVALID, "nattempts must be >= 0");
+  if (p->lgl) return fail(PS_ERR_UNSUPPORTED, "adaptive stepping is not supported on LGL grids");
+  ps::ArkTableau tab;
+  if (ps::ark_tableau(ad->method, &tab) != 0) return fail(PS_ERR_INVALID, "unknown adaptive method %d", ad->method);
+  if (!(ad->rtol >= 0.0) || !(ad->atol >= 0.0) || !(ad->safety_factor > 0.0) || !(ad->min_dt_factor > 0.0) ||
+      !(ad->max_dt_factor >= ad->min_dt_factor))
+    return fail(PS_ERR_INVALID, "adaptive tolerances and factors out of range");
+  if (nattempts == 0) return PS_OK;
+  const ps::ArkCtrl ctrl{ad->rtol, ad->atol, ad->safety_factor, ad->min_dt_factor, ad->max_dt_factor,
+                         ad->max_rejections};
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->nd == 1) return run_adaptive_1d(p, U, nattempts, tab, ctrl, d_t, d_tend, d_dt, d_tout, d_counts, s);
+  return run_adaptive_nd(p, U, nattempts, tab, ctrl, d_t, d_tend, d_dt, d_tout, d_counts, s);
+}
+
+int ps_adaptive_reset(ps_plan p, void* stream) {
+  if (!p) return fail(PS_ERR_INVALID, "null argument");
+  PS_CU(cudaMemsetAsync(p->ark_rej, 0, sizeof(int) * p->nsolve, (cudaStream_t)stream), "adaptive reset");
+  return PS_OK;
 }
 
 int ps_derivative(ps_plan p, int axis, const float* f, float* out, int nf, void* stream) {

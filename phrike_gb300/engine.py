@@ -53,7 +53,7 @@ class Plan:
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
                  gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None,
-                 av_config: Optional[Dict] = None):
+                 av_config: Optional[Dict] = None, scheme: str = "rk4"):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -116,6 +116,11 @@ class Plan:
             wts = av_config.get("variable_weights", None) or {}
             for c in range(5):
                 desc.av_weight[c] = float(wts.get(names[c], 1.0))
+        scheme = str(scheme).lower()
+        if scheme not in ("rk4", "rk2"):
+            raise ValueError(f"fixed-step scheme must be 'rk4' or 'rk2' (got {scheme!r})")
+        self.scheme = scheme
+        desc.scheme = _lib.PS_SCHEME_RK2 if scheme == "rk2" else _lib.PS_SCHEME_RK4
         desc.gamma = float(gamma)
         desc.dealias = 1 if dealias else 0
         fp = filter_params or {}
@@ -205,6 +210,48 @@ class Plan:
         _lib.check(self._lib.ps_run_cfl(self._handle, _ptr(U), int(nsteps), _ptr(t), _ptr(t_end),
                                         _stream(self.device)))
         return U
+
+    @staticmethod
+    def adaptive_desc(adaptive_config: Optional[dict] = None) -> "_lib.AdaptiveDesc":
+        """ps_adaptive_desc from the reference's adaptive_config keys
+        (scheme, rtol, atol, safety_factor, min_dt_factor, max_dt_factor,
+        max_rejections; solver.py:182-193)."""
+        cfg = dict(adaptive_config or {})
+        ad = _lib.AdaptiveDesc()
+        _lib.load().ps_adaptive_desc_init(C.byref(ad))
+        scheme = str(cfg.get("scheme", "rk45")).lower()
+        if scheme not in _lib.ARK_METHODS:
+            raise ValueError(f"Unknown adaptive method: {scheme}. Supported methods: rk23, rk45, rk78")
+        ad.method = _lib.ARK_METHODS[scheme]
+        for key in ("rtol", "atol", "safety_factor", "min_dt_factor", "max_dt_factor"):
+            if key in cfg:
+                setattr(ad, key, float(cfg[key]))
+        if "max_rejections" in cfg:
+            ad.max_rejections = int(cfg["max_rejections"])
+        return ad
+
+    def run_adaptive_(self, U: torch.Tensor, nattempts: int, ad: "_lib.AdaptiveDesc", t: torch.Tensor,
+                      t_end: torch.Tensor, dt: torch.Tensor, t_out: Optional[torch.Tensor] = None,
+                      counts: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Up to nattempts adaptive embedded-RK attempts per solve, decisions
+        on the device (ps_run_adaptive).  ``t``, ``t_end``, ``dt`` (proposed
+        step, replaced by dt_next) and ``t_out`` (optional pause time) are
+        float64 device tensors of nsolve entries; ``counts`` (optional) is an
+        int32 device tensor [nsolve, 2] of accepted and rejected attempts."""
+        self._check_state(U)
+        for x in [t, t_end, dt] + ([t_out] if t_out is not None else []):
+            if x.dtype != torch.float64 or x.device != self.device or x.numel() != self.nsolve:
+                raise RuntimeError("t, t_end, dt and t_out must be float64 device tensors with one entry per solve")
+        if counts is not None and (counts.dtype != torch.int32 or counts.device != self.device
+                                   or counts.numel() != 2 * self.nsolve):
+            raise RuntimeError("counts must be an int32 device tensor of nsolve x 2 entries")
+        _lib.check(self._lib.ps_run_adaptive(self._handle, _ptr(U), int(nattempts), C.byref(ad), _ptr(t),
+                                             _ptr(t_end), _ptr(dt), _ptr(t_out) if t_out is not None else None,
+                                             _ptr(counts) if counts is not None else None, _stream(self.device)))
+        return U
+
+    def adaptive_reset(self) -> None:
+        _lib.check(self._lib.ps_adaptive_reset(self._handle, _stream(self.device)))
 
     def derivative(self, f: torch.Tensor, axis: int, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """axis 0 = x (last array axis)."""

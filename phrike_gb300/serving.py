@@ -84,6 +84,12 @@ class Request:
     arrival: float = 0.0
     params: Dict = field(default_factory=dict)
     U0: Optional[np.ndarray] = None
+    t0: float = 0.0  # start time (a resumed snapshot starts at its own time)
+
+    @staticmethod
+    def resume(rid: int, snap, arrival: float = 0.0) -> "Request":
+        """A request that continues a paused solve (phrike_gb300.io.Snapshot)."""
+        return Request(rid, snap.family, snap.n, snap.t_end, arrival, dict(snap.params), np.asarray(snap.U), snap.t)
 
     @property
     def shape(self) -> Tuple[int, ...]:
@@ -132,7 +138,7 @@ def run_alone(req: Request, device, chunk: int = 20) -> Tuple[torch.Tensor, floa
     plan = make_plan(req.family, req.n, 1, device)
     proj = plan if req.family == "ot2d" else None
     U = _prepare_state(req, device, proj)
-    t = torch.zeros(1, dtype=torch.float64, device=device)
+    t = torch.full((1,), float(req.t0), dtype=torch.float64, device=device)
     te = torch.full((1,), float(req.t_end), dtype=torch.float64, device=device)
     torch.cuda.synchronize(device)
     t0 = time.perf_counter()
@@ -194,6 +200,8 @@ class Server:
         self.used = 0
         self.projectors: Dict[int, Plan] = {}
         self.results: Dict[int, np.ndarray] = {}
+        self.paused: Dict[int, object] = {}
+        self.pause_at: Dict[int, float] = {}
         self.completion: Dict[int, float] = {}
         self.admitted_at: Dict[int, float] = {}
         self.max_live = 0
@@ -270,7 +278,7 @@ class Server:
         U0.record_stream(g.stream)
         with torch.cuda.stream(g.stream):
             g.U[k].copy_(U0, non_blocking=True)
-            g.t[k] = 0.0
+            g.t[k] = float(req.t0)
             g.tend[k] = float(req.t_end)
         g.slots[k] = req
         self.admitted_at[req.rid] = now
@@ -299,11 +307,49 @@ class Server:
                     self.completion[req.rid] = now
                     g.slots[k] = None
                     done += 1
+                elif req is not None and req.rid in self.pause_at and t[k] >= self.pause_at[req.rid]:
+                    self.paused[req.rid] = self.preempt(req.rid)  # between two chunks
+                    self.completion[req.rid] = now
+                    done += 1
         return done
 
-    def serve(self, requests: List[Request], realtime: bool = True, max_seconds: float = 3600.0) -> Dict:
+    def _find(self, rid: int):
+        for g in self.groups:
+            for k, req in enumerate(g.slots):
+                if req is not None and req.rid == rid:
+                    return g, k
+        raise KeyError(f"request {rid} is not resident")
+
+    def snapshot(self, rid: int):
+        """Copy a resident solve out between two chunks (a Snapshot with its
+        current time); the solve keeps running."""
+        from .io import Snapshot
+        g, k = self._find(rid)
+        with torch.cuda.stream(g.stream):
+            U = g.U[k].cpu().numpy()
+            t = float(g.t[k].item())
+        req = g.slots[k]
+        return Snapshot(req.family, req.n, t, float(req.t_end), U, dict(req.params))
+
+    def preempt(self, rid: int):
+        """Pause a resident solve: snapshot it and free its slot.  Resume it
+        later with serve([Request.resume(rid, snapshot)])."""
+        g, k = self._find(rid)
+        snap = self.snapshot(rid)
+        with torch.cuda.stream(g.stream):
+            g.tend[k] = g.t[k]  # a free slot: t >= t_end, the captured chunk skips it
+        g.slots[k] = None
+        self.admitted_at.pop(rid, None)
+        return snap
+
+    def serve(self, requests: List[Request], realtime: bool = True, max_seconds: float = 3600.0,
+              pause_at: Optional[Dict[int, float]] = None) -> Dict:
         """Serve a request stream; arrival times are honoured on the host
-        clock (``realtime``) or all requests arrive at once."""
+        clock (``realtime``) or all requests arrive at once.  ``pause_at``
+        (request id -> time) pauses a solve at the first chunk boundary at or
+        after that time: its Snapshot goes to ``self.paused`` and its slot is
+        freed; serve(..) with Request.resume(rid, snapshot) continues it."""
+        self.pause_at = dict(pause_at or {})
         reqs = sorted(requests, key=lambda r: r.arrival)
         pending: List[Request] = []
         nxt, finished = 0, 0

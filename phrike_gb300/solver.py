@@ -1,11 +1,13 @@
-"""Fixed-step RK4 solvers with the reference's interface (backend "gb300").
+"""Solvers with the reference's interface (backend "gb300").
 
 Mirrors SpectralSolver1D/2D/3D of phrike/solver.py (lines 135-422, 527-812,
 1237-1513): same constructor arguments, compute_dt / step / run methods, the
-same history keys and the same CFL run loop.  A step is one call into the C
-ABI (ps_step_rk4), which runs the fused pass kernels including the clamp and
-the filter cadence; the plan's step counter plays the role of the
-reference's _step_counter.  step() is functional like the reference: it
+same history keys and the same CFL run loop.  A fixed step (scheme "rk4" or
+the midpoint "rk2") is one call into the C ABI (ps_step_rk4), which runs the
+fused pass kernels including the clamp and the filter cadence; the plan's
+step counter plays the role of the reference's _step_counter.  With an
+adaptive_config (rk23 / rk45 / rk78) run() drives the device-side embedded
+RK loop (ps_run_adaptive).  step() is functional like the reference: it
 returns a new tensor and leaves its argument untouched.
 """
 from __future__ import annotations
@@ -25,10 +27,20 @@ class _SpectralSolverBase:
     def __init__(self, grid, equations, U0: Optional[Any] = None, scheme: str = "rk4", cfl: float = 0.4,
                  adaptive_config: Optional[Dict] = None, artificial_viscosity_config: Optional[Dict] = None,
                  gravity_config: Optional[Dict] = None):
-        if str(scheme).lower() != "rk4":
-            raise NotImplementedError(f"backend 'gb300' implements the fixed-step rk4 scheme (got {scheme!r})")
+        # adaptive_config (solver.py:178-204): rk23 / rk45 / rk78 run the
+        # device-side embedded-RK loop; another scheme falls back to fixed steps
+        adaptive = None
         if adaptive_config and adaptive_config.get("enabled", False):
-            raise NotImplementedError("backend 'gb300': adaptive embedded RK is not implemented")
+            method = str(adaptive_config.get("scheme", "rk45")).lower()
+            if method in ("rk23", "rk45", "rk78"):
+                adaptive = dict(adaptive_config, scheme=method)
+                scheme = method
+            else:
+                scheme = adaptive_config.get("fallback_scheme", "rk4")
+        if adaptive is None and str(scheme).lower() not in ("rk4", "rk2"):
+            raise NotImplementedError(f"backend 'gb300': fixed-step schemes are rk4 and rk2 (got {scheme!r})")
+        if adaptive is not None and getattr(grid, "_basis", "fourier") != "fourier":
+            raise NotImplementedError("backend 'gb300': adaptive stepping on LGL grids is not implemented")
         av = None
         if artificial_viscosity_config and artificial_viscosity_config.get("enabled", False):
             if self._ndim == 3:
@@ -41,11 +53,12 @@ class _SpectralSolverBase:
             gravity = [float(gravity_config.get(k, 0.0)) for k in ("gx", "gy", "gz")[: self._ndim]]
         self.grid = grid
         self.equations = equations
-        self.scheme = "rk4"
+        self.scheme = str(scheme).lower()
         self.cfl = float(cfl)
         self.t = 0.0
         self.U = U0
-        self.adaptive_enabled = False
+        self.adaptive_enabled = adaptive is not None
+        self.adaptive_config = adaptive
         self.gravity_config = gravity_config
         fp = dict(getattr(grid, "filter_params", None) or {})
         interval = fp.get("interval", None)
@@ -58,7 +71,9 @@ class _SpectralSolverBase:
                          filter_params=fp, cfl=self.cfl, gravity=gravity, device=grid.device,
                          basis=getattr(grid, "_basis", "fourier"),
                          gemm_precision=getattr(grid, "gemm_precision", "fp32"), equations=self._equations,
-                         mhd_config=getattr(grid, "mhd_config", None), av_config=av)
+                         mhd_config=getattr(grid, "mhd_config", None), av_config=av,
+                         scheme="rk2" if self.scheme == "rk2" else "rk4")
+        self._ark = Plan.adaptive_desc(adaptive) if adaptive is not None else None
 
     # -- reference interface -----------------------------------------------
     def _spacing(self) -> float:
@@ -71,7 +86,17 @@ class _SpectralSolverBase:
         return self.cfl * self._spacing() / s
 
     def step(self, U: Any, dt: float) -> torch.Tensor:
+        """One step of size dt; with adaptive_config one embedded-RK attempt
+        (_adaptive_step: the filtered U_high when accepted, else U).  The
+        reference's 2D/3D _adaptive_step passes an extra argument and raises
+        (solver.py:662, 1351); here every dimension takes the 1D behaviour."""
         V = self.grid.to_device(U).clone()
+        if self.adaptive_enabled:
+            f64 = dict(dtype=torch.float64, device=self.plan.device)
+            t = torch.zeros((1,), **f64)
+            h = torch.full((1,), float(dt), **f64)
+            self.plan.run_adaptive_(V, 1, self._ark, t, h.clone(), h)
+            return V
         self.plan.step_(V, float(dt))
         return V
 
@@ -93,11 +118,18 @@ class _SpectralSolverBase:
         self.U = self.grid.to_device(U0).clone()
         self.t = float(t0)
         next_output = self.t + output_interval
+        # snapshots every checkpoint_interval into outdir (solver.py:357-361, 408-417)
+        self._outdir = outdir
+        self._next_ckpt = (self.t + checkpoint_interval
+                           if outdir and checkpoint_interval and checkpoint_interval > 0 else float("inf"))
+        self._ckpt_interval = checkpoint_interval
         history: Dict[str, List[float]] = {"time": [], **{k: [] for k in self._history_keys}}
         self._record(history)
         if on_output is not None:
             on_output(self.t, self.U)
         step_dt = float(dt) if dt is not None else self.compute_dt(self.U)
+        if self.adaptive_enabled:
+            return self._run_adaptive(history, step_dt, t_end, output_interval, next_output, on_output, on_step)
         step_count = 0
         while self.t < t_end - 1e-12:
             h = min(step_dt, t_end - self.t)
@@ -113,9 +145,61 @@ class _SpectralSolverBase:
                 if on_output is not None:
                     on_output(self.t, self.U)
                 next_output += output_interval
+            self._checkpoint()
         self._record(history)
         if on_output is not None:
             on_output(self.t, self.U)
+        return history
+
+
+    def _checkpoint(self) -> None:
+        if self._outdir and self.t + 1e-12 >= self._next_ckpt:
+            from .io import save_solution_snapshot
+            save_solution_snapshot(self._outdir, self.t, self.U, self.grid, self.equations)
+            self._next_ckpt += self._ckpt_interval
+
+    def _run_adaptive(self, history, dt0, t_end, output_interval, next_output, on_output, on_step,
+                      chunk: int = 16) -> Dict[str, List[float]]:
+        """The adaptive branch of the reference's run loop (solver.py:384-417
+        with _adaptive_run_step): attempts run on the device and pause at
+        the next output time, so outputs are recorded after the same attempts
+        as in the reference.  With on_step every attempt is a separate call
+        and on_step sees each accepted attempt (step_count counts attempts,
+        rejected ones included)."""
+        dev = self.plan.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        t = torch.full((1,), self.t, **f64)
+        te = torch.full((1,), float(t_end), **f64)
+        dtv = torch.full((1,), float(dt0), **f64)
+        tout = torch.empty((1,), **f64)
+        counts = torch.zeros((1, 2), dtype=torch.int32, device=dev)
+        step_count = 0
+        while self.t < t_end - 1e-12:
+            # an output or a checkpoint is still due after this attempt
+            behind = self.t + 1e-12 >= min(next_output, self._next_ckpt)
+            if on_step is not None or behind:
+                dt_used = min(float(dtv.item()), t_end - self.t)
+                before = counts[0, 0].item()
+                self.plan.run_adaptive_(self.U, 1, self._ark, t, te, dtv, None, counts)
+                self.t = float(t.item())
+                if counts[0, 0].item() > before and on_step is not None:
+                    on_step(step_count, dt_used, self.U)
+                step_count += 1
+            else:
+                tout.fill_(min(next_output, self._next_ckpt))
+                self.plan.run_adaptive_(self.U, chunk, self._ark, t, te, dtv, tout, counts)
+                self.t = float(t.item())
+                step_count = int(counts.sum().item())
+            if self.t + 1e-12 >= next_output:
+                self._record(history)
+                if on_output is not None:
+                    on_output(self.t, self.U)
+                next_output += output_interval
+            self._checkpoint()
+        self._record(history)
+        if on_output is not None:
+            on_output(self.t, self.U)
+        self.adaptive_counts = counts[0].tolist()
         return history
 
 

@@ -1,0 +1,107 @@
+"""Adaptive embedded-RK cases shared by the oracle pin test and the GPU parity
+test.  Each case mirrors one run of tests/golden/make_golden.py's "adaptive"
+section (grid, solver options, adaptive_config, end time)."""
+import numpy as np
+
+from oracle import adaptive as A
+from oracle import mhd as M
+from oracle import spectral as O
+
+FILTER = {"enabled": True, "p": 8, "alpha": 36.0}
+AV = {"enabled": True, "mode": "sensor", "nu_max": 2e-3, "s_ref": 1.0, "s_min": 0.1, "p": 2.0,
+      "epsilon": 1e-12, "sensor_variable": "density"}
+
+CASES = {
+    "sod_rk45": dict(kind="euler", shape=(128,), lengths=(1.0,), filt=True, cfl=0.4, method="rk45", ctrl={},
+                     t_end=0.01),
+    "sod_rk23_tight": dict(kind="euler", shape=(128,), lengths=(1.0,), filt=True, cfl=0.4, method="rk23",
+                           ctrl=dict(rtol=1e-9, atol=1e-11, max_rejections=2), t_end=0.003),
+    "sod_av_grav_rk45": dict(kind="euler", shape=(128,), lengths=(1.0,), filt=True, cfl=0.4, method="rk45",
+                             ctrl={}, t_end=0.005, av=AV, gravity=[-2.0]),
+    "khi_rk23": dict(kind="euler", shape=(32, 32), lengths=(1.0, 1.0), filt=True, cfl=0.4, method="rk23",
+                     ctrl=dict(rtol=1e-7), t_end=0.02, gravity=[0.3, -1.0]),
+    "tgv_rk78": dict(kind="euler", shape=(16, 16, 16), lengths=(2 * np.pi,) * 3, filt=False, cfl=0.25,
+                     method="rk78", ctrl=dict(rtol=1e-7), t_end=0.05),
+    "ot_rk45": dict(kind="mhd", shape=(32, 32), lengths=(2 * np.pi,) * 2, filt=True, cfl=0.3, method="rk45",
+                    ctrl={}, t_end=0.15),
+}
+
+
+# Cases for the CUDA path.  Its stage slopes are float32, so an error
+# estimate carries float32 rounding of order 1e-7 relative to the slopes; with
+# the reference's rtol = 1e-6 that noise is a few percent of the tolerance and
+# can flip an accept/reject decision that sits within a few percent of it.
+# These cases use tolerances at which every decision of the float64 oracle
+# clears the threshold by a wide margin (checked by the tests), so the
+# decision sequence itself is comparable.
+GPU_CASES = {  # names distinct from CASES
+    "sod256_rk45": dict(kind="euler", shape=(256,), lengths=(1.0,), filt=True, cfl=0.4, method="rk45",
+                        ctrl=dict(rtol=1e-4, atol=1e-8), t_end=0.02),
+    "sod256_rk45_forced": dict(kind="euler", shape=(256,), lengths=(1.0,), filt=True, cfl=0.4, method="rk45",
+                               ctrl=dict(rtol=1e-4, atol=1e-8, max_rejections=1), t_end=0.02),
+    "sod128_av_grav_rk45": dict(kind="euler", shape=(128,), lengths=(1.0,), filt=True, cfl=0.4, method="rk45",
+                                ctrl=dict(rtol=1e-4), t_end=0.01, av=AV, gravity=[-2.0]),
+    "khi32_rk23_grav": dict(kind="euler", shape=(32, 32), lengths=(1.0, 1.0), filt=True, cfl=0.4, method="rk23",
+                            ctrl=dict(rtol=1e-4), t_end=0.05, gravity=[0.3, -1.0]),
+    "tgv16_rk78": dict(kind="euler", shape=(16, 16, 16), lengths=(2 * np.pi,) * 3, filt=False, cfl=0.25,
+                       method="rk78", ctrl=dict(rtol=3e-7), t_end=0.05),
+    "ot32_rk45": dict(kind="mhd", shape=(32, 32), lengths=(2 * np.pi,) * 2, filt=True, cfl=0.3, method="rk45",
+                      ctrl=dict(rtol=1e-4), t_end=0.15),
+}
+
+
+def oracle_case(tag):
+    """(rhs, post, compute_dt, initial-state map) of the oracle for a case."""
+    c = GPU_CASES[tag] if tag in GPU_CASES else CASES[tag]
+    if c["kind"] == "mhd":
+        ny, nx = c["shape"]
+        s = M.MHDSolver2D(nx, ny, c["lengths"][1], c["lengths"][0], filter_params=FILTER if c["filt"] else None,
+                          cfl=c["cfl"])
+        rhs, post = A.mhd_hooks(s)
+        return rhs, post, s.compute_dt, s.project
+    box = O.FourierBox(c["shape"], c["lengths"], dealias=True, filter_enabled=c["filt"])
+    s = O.EulerSolver(box, cfl=c["cfl"], gravity=c.get("gravity"), av=c.get("av"))
+    rhs, post = A.euler_hooks(s)
+    return rhs, post, s.compute_dt, (lambda U: U)
+
+
+def run_oracle(tag, U0, max_attempts=None, margins=None, dt0=None):
+    """The oracle's adaptive run of a case; ``margins`` (a list) receives
+    |log(err / tol)| of every attempt."""
+    c = GPU_CASES[tag] if tag in GPU_CASES else CASES[tag]
+    rhs, post, cdt, prep = oracle_case(tag)
+    U = prep(np.asarray(U0, dtype=np.float64))
+    ctrl = A.Controller(**c["ctrl"])
+    if margins is not None:
+        base = ctrl.new_dt
+
+        def new_dt(dt, err, scale, order):
+            margins.append(abs(np.log(max(err, 1e-300) / (ctrl.atol + ctrl.rtol * scale))))
+            return base(dt, err, scale, order)
+        ctrl.new_dt = new_dt
+    return A.run_adaptive(rhs, post, U, 0.0, c["t_end"], cdt(U) if dt0 is None else dt0, c["method"], ctrl,
+                          max_attempts=max_attempts)
+
+
+def initial_state(tag):
+    """Initial state of a GPU case (float64)."""
+    from phrike_gb300 import problems
+    c = GPU_CASES[tag]
+    if c["kind"] == "mhd":
+        ny, nx = c["shape"]
+        U0 = problems.orszag_tang_2d(nx, ny, gamma=5.0 / 3.0)
+        x = np.linspace(0.0, c["lengths"][1], nx, endpoint=False)
+        y = np.linspace(0.0, c["lengths"][0], ny, endpoint=False)
+        X, Y = np.meshgrid(x, y, indexing="xy")
+        U0[5] += 0.05 * np.cos(X) * np.cos(2.0 * Y)
+        return U0
+    if len(c["shape"]) == 1:
+        return problems.sod_smoothed(c["shape"][0], L=c["lengths"][0])
+    if len(c["shape"]) == 2:
+        return problems.kelvin_helmholtz_2d(c["shape"][1], c["shape"][0], U0=1.2, A=0.015)
+    return problems.taylor_green_3d(c["shape"][2], c["shape"][1], c["shape"][0])
+
+
+def accepted_steps(log):
+    """[(attempt index, dt)] of the accepted attempts, as on_step reports them."""
+    return np.array([(i, dt) for i, (dt, ok) in enumerate(log) if ok], dtype=np.float64).reshape(-1, 2)

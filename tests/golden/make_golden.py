@@ -45,6 +45,10 @@ def main(ref_path: str, only: str = "") -> None:
         return mhd_fixtures(grid, equations, solver, problems)
     if only == "sources":
         return source_fixtures(grid, equations, solver, problems)
+    if only == "adaptive":
+        return adaptive_fixtures(grid, equations, solver, problems)
+    if only == "rk2":
+        return rk2_fixtures(grid, equations, solver, problems)
 
     out = {}
 
@@ -199,6 +203,106 @@ def source_fixtures(grid, equations, solver, problems) -> None:
         out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
                                                            None)
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+def rk2_fixtures(grid, equations, solver, problems) -> None:
+    """scheme="rk2" (midpoint) fixed steps of every solver: 1D Sod (filter on,
+    cadence 2), 2D KHI, 3D TGV and 2D MHD Orszag-Tang."""
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    out = {}
+    g1 = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params=dict(fp, interval=2))
+    s1 = solver.SpectralSolver1D(g1, equations.EulerEquations1D(gamma=1.4), scheme="rk2", cfl=0.4)
+    U = problems.sod_smoothed(128)
+    out["sod_U0"] = U
+    for _ in range(5):
+        U = s1.step(U, 2e-4)
+    out["sod_U"] = U
+    g2 = grid.Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, dealias=True, filter_params=fp)
+    s2 = solver.SpectralSolver2D(g2, equations.EulerEquations2D(gamma=1.4), scheme="rk2", cfl=0.4)
+    V = problems.kelvin_helmholtz_2d(32, 32, U0=1.2, A=0.015)
+    out["khi_U0"] = V
+    for _ in range(4):
+        V = s2.step(V, 1e-3)
+    out["khi_U"] = V
+    g3 = grid.Grid3D(Nx=16, Ny=16, Nz=16, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, dealias=True)
+    s3 = solver.SpectralSolver3D(g3, equations.EulerEquations3D(gamma=1.4), scheme="rk2", cfl=0.25)
+    T = problems.taylor_green_3d(16)
+    out["tgv_U0"] = T
+    for _ in range(3):
+        T = s3.step(T, 1e-3)
+    out["tgv_U"] = T
+    L = 2.0 * np.pi
+    gm = grid.Grid2D(Nx=32, Ny=32, Lx=L, Ly=L, dealias=True, filter_params=fp)
+    gm.mhd_config = {"resistivity": 0.0, "viscosity": 0.0, "project_each_substage": True,
+                     "divergence_clean": "projection"}
+    sm = solver.SpectralSolverMHD2D(gm, equations.MHDEquations2D(gamma=5.0 / 3.0), scheme="rk2", cfl=0.3)
+    M = problems.orszag_tang_2d(32, 32, gamma=5.0 / 3.0)
+    M = sm._project_B(M)
+    out["ot_U0"] = M
+    for _ in range(3):
+        M = sm.step(M, 2e-3)
+    out["ot_U"] = M
+    np.savez_compressed(os.path.join(HERE, "rk2.npz"), **out)
+
+
+def adaptive_fixtures(grid, equations, solver, problems) -> None:
+    """Adaptive embedded RK through the reference's own run loops: every
+    accepted attempt's (step_count, dt) from on_step, the final state and
+    time.  step_count counts attempts, so its gaps are the rejections."""
+    out = {}
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+
+    def run(tag, s, U0, t_end):
+        seen = []
+        hist = s.run(U0.copy(), 0.0, t_end, output_interval=t_end / 2,
+                     on_step=lambda n, dt, U: seen.append((n, dt)))
+        out[f"{tag}_U0"] = U0
+        out[f"{tag}_U"] = np.asarray(s.U)
+        out[f"{tag}_t"] = s.t
+        out[f"{tag}_steps"] = np.array(seen, dtype=np.float64).reshape(-1, 2)
+        out[f"{tag}_hist_t"] = np.asarray(hist["time"])
+
+    cases = [
+        # tag, dim, scheme, controller overrides, t_end
+        ("sod_rk45", 1, "rk45", {}, 0.01),
+        ("sod_rk23_tight", 1, "rk23", {"rtol": 1e-9, "atol": 1e-11, "max_rejections": 2}, 0.003),
+    ]
+    for tag, _, scheme, extra, t_end in cases:
+        g = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params=fp)
+        cfg = dict({"enabled": True, "scheme": scheme}, **extra)
+        s = solver.SpectralSolver1D(g, equations.EulerEquations1D(gamma=1.4), cfl=0.4, adaptive_config=cfg)
+        run(tag, s, problems.sod_smoothed(128), t_end)
+    # 1D with artificial viscosity and gravity in the stage right-hand sides
+    av = {"enabled": True, "mode": "sensor", "nu_max": 2e-3, "s_ref": 1.0, "s_min": 0.1, "p": 2.0,
+          "epsilon": 1e-12, "sensor_variable": "density"}
+    g = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params=fp)
+    s = solver.SpectralSolver1D(g, equations.EulerEquations1D(gamma=1.4), cfl=0.4,
+                                adaptive_config={"enabled": True, "scheme": "rk45"},
+                                artificial_viscosity_config=av, gravity_config={"enabled": True, "gx": -2.0})
+    run("sod_av_grav_rk45", s, problems.sod_smoothed(128), 0.005)
+    # 2D KHI with gravity (its adaptive right-hand side has no viscosity)
+    g2 = grid.Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, dealias=True, filter_params=fp)
+    s2 = solver.SpectralSolver2D(g2, equations.EulerEquations2D(gamma=1.4), cfl=0.4,
+                                 adaptive_config={"enabled": True, "scheme": "rk23", "rtol": 1e-7},
+                                 gravity_config={"enabled": True, "gx": 0.3, "gy": -1.0})
+    run("khi_rk23", s2, problems.kelvin_helmholtz_2d(32, 32, U0=1.2, A=0.015), 0.02)
+    # 3D TGV with the reference's 8-stage "rk78"
+    g3 = grid.Grid3D(Nx=16, Ny=16, Nz=16, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, dealias=True)
+    s3 = solver.SpectralSolver3D(g3, equations.EulerEquations3D(gamma=1.4), cfl=0.25,
+                                 adaptive_config={"enabled": True, "scheme": "rk78", "rtol": 1e-7})
+    run("tgv_rk78", s3, problems.taylor_green_3d(16), 0.05)
+    # 2D MHD Orszag-Tang with a divergent B perturbation (run projects U0 first)
+    L = 2.0 * np.pi
+    gm = grid.Grid2D(Nx=32, Ny=32, Lx=L, Ly=L, dealias=True, filter_params=fp)
+    gm.mhd_config = {"resistivity": 0.0, "viscosity": 0.0, "project_each_substage": True,
+                     "divergence_clean": "projection"}
+    sm = solver.SpectralSolverMHD2D(gm, equations.MHDEquations2D(gamma=5.0 / 3.0), cfl=0.3,
+                                    adaptive_config={"enabled": True, "scheme": "rk45"})
+    M0 = problems.orszag_tang_2d(32, 32, gamma=5.0 / 3.0)
+    X, Y = np.meshgrid(np.asarray(gm.x), np.asarray(gm.y), indexing="xy")
+    M0[5] += 0.05 * np.cos(X) * np.cos(2.0 * Y)
+    run("ot_rk45", sm, M0, 0.15)
+    np.savez_compressed(os.path.join(HERE, "adaptive.npz"), **out)
+
 
 def mhd_fixtures(grid, equations, solver, problems) -> None:
     """2D ideal MHD: Orszag-Tang (rho = gamma^2, p = gamma, B0 = 1 on

@@ -75,3 +75,26 @@ def test_run_simulation_sod_fixed_dt(cuda_device):
     out = solver.U.double().cpu().numpy()
     assert rel_l2(out[0], ref[0]) < 1e-5 and rel_l2(out[2], ref[2]) < 1e-5
     assert len(hist["time"]) >= 3
+
+
+def test_run_writes_reference_snapshots(cuda_device, tmp_path):
+    """run(..., checkpoint_interval, outdir) writes snapshot_t*.npz files in
+    the reference's layout, readable by load_checkpoint, at the same
+    times as the reference's loop (after the step that reaches each
+    checkpoint time)."""
+    import numpy as np
+    from phrike_gb300 import EulerEquations2D, Grid2D, problems
+    from phrike_gb300.io import load_checkpoint
+    from phrike_gb300.solver import SpectralSolver2D
+    g = Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, backend="gb300")
+    s = SpectralSolver2D(g, EulerEquations2D(gamma=1.4), cfl=0.4)
+    U0 = problems.kelvin_helmholtz_2d(32, 32)
+    times = []
+    s.run(U0, 0.0, 0.02, output_interval=0.01, checkpoint_interval=0.005, outdir=str(tmp_path),
+          on_step=lambda n, dt, U: times.append(s.t))
+    files = sorted(p.name for p in tmp_path.glob("snapshot_t*.npz"))
+    assert len(files) >= 3
+    d = load_checkpoint(str(tmp_path / files[-1]))
+    assert d["U"].shape == (4, 32, 32) and set(d["primitive_vars"]) == {"rho", "ux", "uy", "p"}
+    assert d["meta"]["Nx"] == 32 and abs(d["meta"]["gamma"] - 1.4) < 1e-12
+    assert np.isfinite(d["U"]).all() and d["t"] in times

@@ -48,3 +48,27 @@ def test_serving_under_a_tight_hbm_budget(cuda_device):
     assert stats["requests"] == len(reqs)
     assert srv.used <= 3 * one
     _check_alone(srv, reqs, cuda_device)
+
+
+def test_serving_pause_and_resume(cuda_device, tmp_path):
+    """A served solve paused at a chunk boundary (its Snapshot written to
+    disk and read back) and resumed later in the mix ends bit-identical to the
+    resumed solve run alone, and within float32 rounding of the solve run
+    without the pause."""
+    from conftest import rel_l2
+    from phrike_gb300.io import Snapshot
+    from phrike_gb300.serving import Request, Server, run_alone
+    reqs = [Request(0, "khi2d", 64, 0.04, 0.0, {"U0": 1.1, "A": 0.012}),
+            Request(1, "sod1d", 256, 0.03, 0.0), Request(2, "khi2d", 64, 0.02, 0.0, {"U0": 0.8, "A": 0.01})]
+    srv = Server(cuda_device, chunk=5)
+    srv.serve(reqs, realtime=False, pause_at={0: 0.015})
+    assert 0 in srv.paused and 0 not in srv.results
+    snap = srv.paused[0]
+    assert 0.015 <= snap.t < 0.04
+    snap = Snapshot.load(snap.save(str(tmp_path / "paused.npz")))
+    later = [Request.resume(0, snap), Request(3, "khi2d", 64, 0.01, 0.0, {"U0": 1.3, "A": 0.02})]
+    srv.serve(later, realtime=False)
+    U, _ = run_alone(Request.resume(0, snap), cuda_device, chunk=srv.chunk)
+    assert np.array_equal(srv.results[0], U.cpu().numpy())
+    W, _ = run_alone(Request(9, "khi2d", 64, 0.04, 0.0, {"U0": 1.1, "A": 0.012}), cuda_device, chunk=srv.chunk)
+    assert rel_l2(srv.results[0], W.cpu().numpy()) < 1e-5

@@ -196,3 +196,51 @@ def test_gravity_and_artificial_viscosity_match_reference():
         for _ in range(3):
             V = s2.step(V, 2e-3)
         assert rel_l2(V, z[f"av2d_{mode}_U"]) < 1e-13, mode
+
+
+@pytest.mark.parametrize("tag", ["sod_rk45", "sod_rk23_tight", "sod_av_grav_rk45", "khi_rk23", "tgv_rk78",
+                                 "ot_rk45"])
+def test_adaptive_rk_matches_reference(tag):
+    """Embedded RK23 / RK45 / the reference's 8-stage "rk78" with its step
+    controller, rejections and forced acceptance, through the reference's run
+    loops (1D with viscosity and gravity; 2D with gravity; 3D; 2D MHD)."""
+    from adaptive_cases import accepted_steps, run_oracle
+    z = golden("adaptive.npz")
+    U, t, log, _, _ = run_oracle(tag, z[f"{tag}_U0"])
+    ref = z[f"{tag}_steps"]
+    got = accepted_steps(log)
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    np.testing.assert_array_equal(got[:, 0], ref[:, 0])
+    np.testing.assert_allclose(got[:, 1], ref[:, 1], rtol=1e-9)
+    assert abs(t - float(z[f"{tag}_t"])) < 1e-12
+    assert rel_l2(U, z[f"{tag}_U"]) < 1e-10
+    if tag == "sod_rk23_tight":  # rejections and forced acceptances both occur
+        assert len(log) > len(got)
+
+
+def test_rk2_scheme_matches_reference():
+    """scheme="rk2" (midpoint) fixed steps of the 1D (filter cadence 2), 2D,
+    3D and MHD solvers against the reference's own runs."""
+    from oracle import mhd as M
+    z = golden("rk2.npz")
+    fbox = dict(dealias=True, filter_enabled=True)
+    s1 = O.EulerSolver(O.FourierBox((128,), (1.0,), **fbox), filter_interval=2, scheme="rk2")
+    U = z["sod_U0"].copy()
+    for _ in range(5):
+        U = s1.step(U, 2e-4)
+    assert rel_l2(U, z["sod_U"]) < 1e-13
+    s2 = O.EulerSolver(O.FourierBox((32, 32), (1.0, 1.0), **fbox), scheme="rk2")
+    V = z["khi_U0"].copy()
+    for _ in range(4):
+        V = s2.step(V, 1e-3)
+    assert rel_l2(V, z["khi_U"]) < 1e-13
+    s3 = O.EulerSolver(O.FourierBox((16, 16, 16), (2 * np.pi,) * 3, dealias=True), cfl=0.25, scheme="rk2")
+    T = z["tgv_U0"].copy()
+    for _ in range(3):
+        T = s3.step(T, 1e-3)
+    assert rel_l2(T, z["tgv_U"]) < 1e-13
+    sm = M.MHDSolver2D(32, 32, filter_params={"enabled": True, "p": 8, "alpha": 36.0}, scheme="rk2")
+    W = z["ot_U0"].copy()
+    for _ in range(3):
+        W = sm.step(W, 2e-3)
+    assert rel_l2(W, z["ot_U"]) < 1e-12
