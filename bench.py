@@ -313,6 +313,12 @@ def run_ensemble(args):
     _build.build()
     device = torch.device("cuda", 0)
     specs = khi_ensemble_specs(args.nsolve, t_end=args.t_end)
+    # warm-up: the same groups for a short time, so that lazy kernel loading
+    # (about 2 s for this library on first use) stays out of the timed run
+    from phrike_gb300.ensemble import SolveSpec
+    Ensemble([SolveSpec(sp.shape, sp.lengths, sp.U0, 1e-4) for sp in specs], cfl=0.4,
+             device=device).run(chunk=args.chunk, use_graphs=True)
+    torch.cuda.synchronize()
     ens = Ensemble(specs, cfl=0.4, device=device)
     sampler = ClockSampler(0)
     sampler.start()
@@ -650,6 +656,12 @@ def run_serving(args):
     _build.build()
     device = torch.device("cuda", 0)
     reqs = request_stream(args.requests, rate=200.0)
+    # warm-up: one short request per (family, size) on a separate server with
+    # the same group shapes, so that lazy kernel loading stays out of the timed run
+    keys = sorted({(r.family, r.n) for r in reqs})
+    Server(device, chunk=args.chunk).serve([Request(-1 - i, f, n, 1e-4) for i, (f, n) in enumerate(keys)],
+                                          realtime=False)
+    torch.cuda.synchronize()
     srv = Server(device, chunk=args.chunk)
     sampler = ClockSampler(0)
     sampler.start()

@@ -73,8 +73,8 @@ typedef struct {
   double mhd_p_min;
   int mhd_project_substages;   /* project B after every RK stage (default 1)   */
   int mhd_divergence_clean;    /* 1: Helmholtz projection, 0: none (default 1) */
-  double mhd_resistivity;      /* eta; must be 0 (explicit diffusion not built) */
-  double mhd_viscosity;        /* nu;  must be 0                                */
+  double mhd_resistivity;      /* eta: rhs_B += eta lap(B) (solver.py:945-950)  */
+  double mhd_viscosity;        /* nu: rhs_(rho u) += nu lap(rho u) (951-954)    */
   /* Artificial viscosity, 1D/2D Euler (SpectralArtificialViscosity,
    * artificial_viscosity.py:37-403): rhs_c += div(w_c nu grad U_c) with
    * nu = av_nu_max ((s > av_s_min ? s : 0) / av_s_ref)^av_p and
@@ -88,6 +88,10 @@ typedef struct {
    * _rk2_step_3d / _rk_substages (solver.py:96-105, 492-500, 1211-1216,
    * 992-996), with the same clamp, projection and filter placement. */
   int scheme;                  /* PS_SCHEME_RK4 or PS_SCHEME_RK2                */
+  /* Parabolic CFL factor of explicit MHD diffusion (mhd_config "cfl_diff",
+   * solver.py:878-880): dt <= mhd_cfl_diff / (max(eta, nu) k^2_max).
+   * Default 1. */
+  double mhd_cfl_diff;
 } ps_plan_desc;
 
 #define PS_SCHEME_RK4 0

@@ -95,7 +95,8 @@ class MHDSolver2D:
     def __init__(self, nx: int, ny: int, lx: float = 2 * np.pi, ly: float = 2 * np.pi, gamma: float = 5.0 / 3.0,
                  dealias: bool = True, filter_params: Optional[dict] = None, cfl: float = 0.3,
                  rho_min: float = 1e-10, p_min: float = 1e-12, project_each_substage: bool = True,
-                 divergence_clean: str = "projection", scheme: str = "rk4"):
+                 divergence_clean: str = "projection", scheme: str = "rk4", resistivity: float = 0.0,
+                 viscosity: float = 0.0, cfl_diff: float = 1.0):
         fp = filter_params or {}
         self.box = FourierBox((ny, nx), (ly, lx), dealias=dealias, filter_enabled=bool(fp.get("enabled", False)),
                               filter_p=int(fp.get("p", 8)), filter_alpha=float(fp.get("alpha", 36.0)))
@@ -107,10 +108,20 @@ class MHDSolver2D:
         self.interval = max(1, int(fp.get("interval", 1) or 1))
         self.step_counter = 0
         self.scheme = scheme
+        self.resistivity, self.viscosity, self.cfl_diff = resistivity, viscosity, cfl_diff
 
     def rhs(self, U: np.ndarray) -> np.ndarray:
+        """_compute_rhs (solver.py:942-954): flux divergence plus the explicit
+        resistivity eta lap(B) and viscosity nu lap(rho u)."""
         Fx, Fy = fluxes(U, self.gamma)
-        return -(self.box.deriv(Fx, 1) + self.box.deriv(Fy, 0))
+        r = -(self.box.deriv(Fx, 1) + self.box.deriv(Fy, 0))
+        if self.resistivity != 0.0:
+            for c in (5, 6, 7):
+                r[c] = r[c] + self.resistivity * self.box.laplacian(U[c])
+        if self.viscosity != 0.0:
+            for c in (1, 2, 3):
+                r[c] = r[c] + self.viscosity * self.box.laplacian(U[c])
+        return r
 
     def clamp(self, U: np.ndarray) -> np.ndarray:
         """_clamp (solver.py:956-964)"""
@@ -157,7 +168,70 @@ class MHDSolver2D:
         s = max_wave_speed(U, self.gamma)
         if s <= 0.0:
             return 1e-6
-        return self.cfl * min(self.box.spacing) / s
+        dt = self.cfl * min(self.box.spacing) / s
+        dif = max(self.resistivity, self.viscosity)
+        if dif > 0.0:  # parabolic limit (solver.py:1028-1033) with k2_max of the grid (916-929)
+            k2max = sum(float(np.max(k * k)) for k in self.box.k)
+            dt = min(dt, self.cfl_diff / (dif * k2max))
+        return dt
 
     def max_div_b(self, U: np.ndarray) -> float:
         return float(np.max(np.abs(self.box.deriv(U[5], 1) + self.box.deriv(U[6], 0))))
+
+
+def max_wave_speed_1d(U: np.ndarray, gamma: float) -> float:
+    """MHDEquations1D.max_wave_speed (equations.py:735-750): |u_x| + c_f."""
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    a2 = gamma * p / rho
+    b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+    cax2 = Bx * Bx / rho
+    disc = np.maximum((a2 + b2) ** 2 - 4.0 * a2 * cax2, 0.0)
+    return float(np.max(np.abs(ux) + np.sqrt(0.5 * (a2 + b2 + np.sqrt(disc)))))
+
+
+class MHDSolver1D(MHDSolver2D):
+    """SpectralSolverMHD with dim 1 (solver.py:840-1049, 1165-1166): the x
+    flux of MHDEquations1D (equations.py:698-733, F_Bx = 0), the 1D projection
+    Bx <- mean(Bx) with the thermal pressure held fixed (grid.py:554-567,
+    solver.py:966-986), clamp, filter cadence and diffusion as in 2D."""
+
+    def __init__(self, n: int, lx: float = 1.0, **kw):
+        super().__init__(n, 1, lx, 1.0, **kw)
+        fp = kw.get("filter_params") or {}
+        self.box = FourierBox((n,), (lx,), dealias=kw.get("dealias", True),
+                              filter_enabled=bool(fp.get("enabled", False)), filter_p=int(fp.get("p", 8)),
+                              filter_alpha=float(fp.get("alpha", 36.0)))
+
+    def rhs(self, U: np.ndarray) -> np.ndarray:
+        Fx, _ = fluxes(U, self.gamma)
+        Fx[5] = 0.0
+        r = -self.box.deriv(Fx, 0)
+        if self.resistivity != 0.0:
+            for c in (5, 6, 7):
+                r[c] = r[c] + self.resistivity * self.box.laplacian(U[c])
+        if self.viscosity != 0.0:
+            for c in (1, 2, 3):
+                r[c] = r[c] + self.viscosity * self.box.laplacian(U[c])
+        return r
+
+    def project(self, U: np.ndarray) -> np.ndarray:
+        if self.divergence_clean == "none":
+            return U
+        rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, self.gamma)
+        V = U.copy()
+        V[5] = np.full_like(U[5], U[5].mean())
+        V[4] = p / (self.gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * (V[5] ** 2 + By * By + Bz * Bz)
+        return V
+
+    def compute_dt(self, U: np.ndarray) -> float:
+        s = max_wave_speed_1d(U, self.gamma)
+        if s <= 0.0:
+            return 1e-6
+        dt = self.cfl * self.box.spacing[0] / s
+        dif = max(self.resistivity, self.viscosity)
+        if dif > 0.0:
+            dt = min(dt, self.cfl_diff / (dif * float(np.max(self.box.k[0] ** 2))))
+        return dt
+
+    def max_div_b(self, U: np.ndarray) -> float:
+        return float(np.max(np.abs(self.box.deriv(U[5], 0))))

@@ -125,6 +125,13 @@ class FourierBox:
         F = F * (1j * self._kview(a))
         return ifftn(F, self.axes).real
 
+    def laplacian(self, f: np.ndarray) -> np.ndarray:
+        """Re IFFT(-|k|^2 * mask * sigma * FFT f) (grid.py:569-579, 1329-1338,
+        1696-1703)."""
+        F = fftn(f, self.axes) * self.mult
+        k2 = sum(self._kview(a) ** 2 for a in range(self.ndim))
+        return ifftn(-k2 * F, self.axes).real
+
     def filt(self, f: np.ndarray) -> np.ndarray:
         """apply_spectral_filter: Re IFFT(mask * sigma * FFT f) (grid.py:524-538,
         1254-1287, 1723-1726)."""

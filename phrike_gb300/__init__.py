@@ -47,7 +47,8 @@ def _filter_params(cfg: Dict[str, Any]) -> Optional[Dict[str, Any]]:
 
 def run_simulation(problem_name: str, config_path: Optional[str] = None, config: Optional[Dict[str, Any]] = None,
                    backend: str = "gb300", device: Optional[str] = "cuda", precision: str = "single",
-                   generate_video: bool = False, debug: bool = False) -> Tuple[Any, Dict[str, Any]]:
+                   generate_video: bool = False, debug: bool = False,
+                   outdir: Optional[str] = None) -> Tuple[Any, Dict[str, Any]]:
     """Run one of the built-in problems and return (solver, history), like
     phrike.run_simulation (phrike/__init__.py:14-56).
 
@@ -78,13 +79,26 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
     kw = dict(dealias=dealias, filter_params=fp, backend=backend, torch_device=device, precision=precision,
               debug=debug)
     name = problem_name.lower()
+    # adaptive (integration.adaptive), artificial viscosity and gravity sections,
+    # with the reference's defaults (problems/base.py:110-176)
+    ad = integ.get("adaptive", None)
+    opts: Dict[str, Any] = {}
+    if ad:
+        opts["adaptive_config"] = dict({"scheme": "rk45", "rtol": 1e-6, "atol": 1e-8, "safety_factor": 0.9,
+                                        "min_dt_factor": 0.1, "max_dt_factor": 5.0, "max_rejections": 10,
+                                        "fallback_scheme": "rk4"}, **ad, enabled=bool(ad.get("enabled", False)))
+    if cfg.get("artificial_viscosity"):
+        opts["artificial_viscosity_config"] = dict(cfg["artificial_viscosity"])
+    if cfg.get("gravity"):
+        opts["gravity_config"] = dict(cfg["gravity"])
     if name == "sod":
         N = int(g.get("N", 1024))
         Lx = float(g.get("Lx", 1.0))
         grid = G.Grid1D(N=N, Lx=Lx, **kw)
         eqs = E.EulerEquations1D(gamma=gamma)
         U0 = P.sod_smoothed(N, Lx, gamma, float(ic.get("width", 0.005)))
-        solver = S.SpectralSolver1D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.4)))
+        solver = S.SpectralSolver1D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.4)),
+                                    **opts)
     elif name == "tgv3d":
         N = int(g.get("N", 64))
         Nx, Ny, Nz = int(g.get("Nx", N)), int(g.get("Ny", N)), int(g.get("Nz", N))
@@ -92,14 +106,16 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
         grid = G.Grid3D(Nx=Nx, Ny=Ny, Nz=Nz, Lx=L, Ly=float(g.get("Ly", L)), Lz=float(g.get("Lz", L)), **kw)
         eqs = E.EulerEquations3D(gamma=gamma)
         U0 = P.taylor_green_3d(Nx, Ny, Nz, gamma, L)
-        solver = S.SpectralSolver3D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.25)))
+        solver = S.SpectralSolver3D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.25)),
+                                    **opts)
     elif name == "khi2d":
         N = int(g.get("N", 128))
         Nx, Ny = int(g.get("Nx", N)), int(g.get("Ny", N))
         grid = G.Grid2D(Nx=Nx, Ny=Ny, Lx=1.0, Ly=1.0, **kw)
         eqs = E.EulerEquations2D(gamma=gamma)
         U0 = P.kelvin_helmholtz_2d(Nx, Ny, float(ic.get("U0", 1.0)), float(ic.get("A", 0.01)), gamma)
-        solver = S.SpectralSolver2D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.4)))
+        solver = S.SpectralSolver2D(grid, eqs, scheme=integ.get("scheme", "rk4"), cfl=float(integ.get("cfl", 0.4)),
+                                    **opts)
     elif name == "orszag_tang2d":
         N = int(g.get("N", 128))
         Nx, Ny = int(g.get("Nx", N)), int(g.get("Ny", N))
@@ -110,12 +126,26 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
         eqs = E.MHDEquations2D(gamma=gamma)
         U0 = P.orszag_tang_2d(Nx, Ny, gamma, ic.get("rho0"), ic.get("p0"), float(ic.get("B0", 1.0)), L)
         solver = S.SpectralSolverMHD2D(grid, eqs, scheme=integ.get("scheme", "rk4"),
-                                       cfl=float(integ.get("cfl", 0.3)))
+                                       cfl=float(integ.get("cfl", 0.3)), **opts)
+    elif name == "alfven1d":
+        N = int(g.get("N", 128))
+        Lx = float(g.get("Lx", 1.0))
+        gamma = float(phys.get("gamma", 5.0 / 3.0))
+        grid = G.Grid1D(N=N, Lx=Lx, **kw)
+        grid.mhd_config = (phys.get("mhd", {}) or {})
+        eqs = E.MHDEquations1D(gamma=gamma)
+        U0 = P.alfven_cp_1d(N, Lx, 0.0, float(ic.get("rho0", 1.0)), float(ic.get("p0", 0.1)),
+                            float(ic.get("B0", 1.0)), float(ic.get("b1", 0.1)), int(ic.get("m", 1)),
+                            int(ic.get("direction", 1)), gamma)
+        solver = S.SpectralSolverMHD1D(grid, eqs, scheme=integ.get("scheme", "rk4"),
+                                       cfl=float(integ.get("cfl", 0.4)), **opts)
     else:
-        raise ValueError(f"unknown problem {problem_name!r} (available: sod, tgv3d, khi2d, orszag_tang2d)")
+        raise ValueError(f"unknown problem {problem_name!r} "
+                         "(available: sod, tgv3d, khi2d, orszag_tang2d, alfven1d)")
     dt = integ.get("dt", None)
     history = solver.run(U0, float(integ.get("t0", 0.0)), float(integ.get("t_end", 0.01)),
                          output_interval=float(integ.get("output_interval", 0.1)),
+                         checkpoint_interval=float(integ.get("checkpoint_interval", 0.0)), outdir=outdir,
                          dt=float(dt) if dt is not None else None)
     return solver, history
 
@@ -125,10 +155,11 @@ def __getattr__(name: str):
     if name in ("Grid1D", "Grid2D", "Grid3D"):
         from . import grid
         return getattr(grid, name)
-    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D", "MHDEquations2D"):
+    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D", "MHDEquations1D", "MHDEquations2D"):
         from . import equations
         return getattr(equations, name)
-    if name in ("SpectralSolver1D", "SpectralSolver2D", "SpectralSolver3D", "SpectralSolverMHD2D"):
+    if name in ("SpectralSolver1D", "SpectralSolver2D", "SpectralSolver3D", "SpectralSolverMHD1D",
+                "SpectralSolverMHD2D"):
         from . import solver
         return getattr(solver, name)
     raise AttributeError(name)

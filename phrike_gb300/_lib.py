@@ -63,6 +63,7 @@ class PlanDesc(C.Structure):
         ("av_epsilon", C.c_double),
         ("av_weight", C.c_double * 5),
         ("scheme", C.c_int),
+        ("mhd_cfl_diff", C.c_double),
     ]
 
 

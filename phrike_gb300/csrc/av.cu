@@ -47,6 +47,17 @@ __global__ void k_av_sub(float* __restrict__ G, long ssG, const float* __restric
   }
 }
 
+// 2D MHD explicit diffusion (SpectralSolverMHD._compute_rhs, solver.py:942-954):
+// G[solve][f0 + f] -= coef (T1 + T2)[solve][f], f < 3, with T1 = L_x X and
+// T2 = (-k_y^2) P_x X, so that the last pass's P_y G carries
+// coef (P_y L_x + L_y P_x) X = coef lap(X) (grid.py:1329-1338).
+__global__ void k_mhd_diff_fold(float* __restrict__ G, long ssG, const float* __restrict__ T1,
+                                const float* __restrict__ T2, long ssT, long cells, int f0, float coef) {
+  const long go = (long)blockIdx.y * ssG + (long)f0 * cells, to = (long)blockIdx.y * ssT;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < 3 * cells; i += (long)gridDim.x * blockDim.x)
+    G[go + i] -= coef * (T1[to + i] + T2[to + i]);
+}
+
 static int grid_x(long n, int nsolve) {
   const long want = (n + 255) / 256;
   const long cap = (2048 + nsolve - 1) / nsolve;
@@ -66,6 +77,12 @@ cudaError_t launch_av_flux(const AVFluxArgs& a, int nsolve, cudaStream_t s) {
 cudaError_t launch_av_sub(float* G, long ssG, const float* T, const float* T2, long ssT, long cells, int nsolve,
                           cudaStream_t s) {
   k_av_sub<<<dim3(grid_x(4 * cells, nsolve), nsolve), 256, 0, s>>>(G, ssG, T, T2, ssT, cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mhd_diff_fold(float* G, long ssG, const float* T1, const float* T2, long ssT, long cells,
+                                 int nsolve, int f0, float coef, cudaStream_t s) {
+  k_mhd_diff_fold<<<dim3(grid_x(3 * cells, nsolve), nsolve), 256, 0, s>>>(G, ssG, T1, T2, ssT, cells, f0, coef);
   return cudaGetLastError();
 }
 

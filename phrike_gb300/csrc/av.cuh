@@ -20,5 +20,8 @@ cudaError_t launch_av_uy(const float* S, long cells, long ssS, int nsolve, float
 cudaError_t launch_av_flux(const AVFluxArgs& a, int nsolve, cudaStream_t s);
 cudaError_t launch_av_sub(float* G, long ssG, const float* T, const float* T2, long ssT, long cells, int nsolve,
                           cudaStream_t s);
+// 2D MHD resistivity / viscosity: G[f0 .. f0+2] -= coef (T1 + T2) per solve
+cudaError_t launch_mhd_diff_fold(float* G, long ssG, const float* T1, const float* T2, long ssT, long cells,
+                                 int nsolve, int f0, float coef, cudaStream_t s);
 
 }  // namespace ps

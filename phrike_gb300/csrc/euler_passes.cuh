@@ -324,10 +324,12 @@ struct OpArgs {
   int rps;           // rows per solve
   StridedGeom g;     // strided geometry
   AxisOps ax;
-  int deriv;         // 0: P, 1: D
+  int deriv;         // 0: P, 1: D, 2: L (Laplacian factor), 3: raw second derivative (op_symbol)
   float scale;       // multiplies the symbol (e.g. -1 for a right-hand side)
   int complement;    // P only: out = in - IFFT((1/N - P) FFT in)  (exact, see AxisOps)
   const int* active; // contiguous only, nullable: rows of inactive solves are left as they are
+  float kunit;       // 2 pi / L of the axis (deriv 2, 3)
+  long ss_in;        // contiguous only: solve stride of in (0: ss)
 };
 
 template <int N, int T, bool STRIDED>
@@ -337,14 +339,14 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& S = *reinterpret_cast<StridedSmem<N, T, STRIDED>*>(smem_raw);
   int p, t;
-  long base, step;
+  long base_in, base_out, step;
   bool valid;
   if constexpr (STRIDED) {
     p = threadIdx.x % T;
     t = threadIdx.x / T;
     const int col = blockIdx.x * T + p;
     valid = col < a.g.ncol;
-    base = (long)blockIdx.y * a.g.os + col + (long)t * a.g.as;
+    base_in = base_out = (long)blockIdx.y * a.g.os + col + (long)t * a.g.as;
     step = (long)A * a.g.as;
   } else {
     t = threadIdx.x % A;
@@ -353,7 +355,10 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
     valid = row < a.rows;
     const int r = valid ? row : 0;
     if (a.active != nullptr && a.active[r / a.rps] == 0) valid = false;
-    base = (long)(r / a.rps) * a.ss + (long)(r % a.rps) * N + t;
+    // in may be a field subset of a wider state (its own solve stride)
+    const long loc = (long)(r % a.rps) * N + t;
+    base_in = (long)(r / a.rps) * (a.ss_in ? a.ss_in : a.ss) + loc;
+    base_out = (long)(r / a.rps) * a.ss + loc;
     step = A;
   }
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
   for (int c = 0; c < a.nf; c += 2) {
     const bool two = c + 1 < a.nf;
     float2 w[B], w0[B];
-    load_pair<N>(w, a.in + c * a.fs, two ? a.in + (c + 1) * a.fs : nullptr, base, step, valid);
+    load_pair<N>(w, a.in + c * a.fs, two ? a.in + (c + 1) * a.fs : nullptr, base_in, step, valid);
     const bool comp = a.complement && !a.deriv;
 #pragma unroll
     for (int r = 0; r < B; ++r) w0[r] = w[r];
@@ -371,13 +376,12 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
 #pragma unroll
     for (int r = 0; r < B; ++r) {
       const int k = pf.kidx(r);
-      if (a.deriv) {
-        const float dd = a.scale * S.ax.d[k];
-        w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
-      } else {
-        const float s = comp ? (1.0f / N) - S.ax.P[k] : a.scale * S.ax.P[k];
+      if (comp) {
+        const float s = (1.0f / N) - S.ax.P[k];
         w[r].x *= s;
         w[r].y *= s;
+      } else {
+        w[r] = op_symbol<N>(w[r], k, a.deriv, a.scale, a.kunit, S.ax.P, S.ax.d);
       }
     }
     pf.inv(w);
@@ -388,8 +392,8 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_op(OpArgs a) {
     if (valid) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
-        a.out[c * a.fs + base + n2 * step] = w[n2].x;
-        if (two) a.out[(c + 1) * a.fs + base + n2 * step] = w[n2].y;
+        a.out[c * a.fs + base_out + n2 * step] = w[n2].x;
+        if (two) a.out[(c + 1) * a.fs + base_out + n2 * step] = w[n2].y;
       }
     }
   }

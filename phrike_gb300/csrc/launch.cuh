@@ -7,6 +7,7 @@
 #include <unordered_set>
 
 #include "euler1d.cuh"
+#include "mhd1d.cuh"
 #include "euler_passes.cuh"
 #include "passes_tma.cuh"
 
@@ -16,6 +17,7 @@ template <int N> cudaError_t launch_xfirst(int nd, const XFirstArgs& a, cudaStre
 template <int N> cudaError_t launch_op(bool strided, const OpArgs& a, cudaStream_t s);
 template <int N> cudaError_t launch_step1d(const Step1DArgs& a, int nsolve, cudaStream_t s);
 template <int N> cudaError_t launch_ark1d(const Ark1DArgs& a, int nsolve, cudaStream_t s);
+template <int N> cudaError_t launch_mhd1d(const Mhd1DArgs& a, int nsolve, cudaStream_t s);
 
 // TMA strided passes: columns per tile and ring depth per pencil length
 template <int N> struct TmaTile {
@@ -232,6 +234,18 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
     if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
     k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
     return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_mhd1d<NN>(const Mhd1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    if constexpr (NN > 2048) {                                                                        \
+      return cudaErrorInvalidValue; /* 1D MHD pencils up to 2048 points */                            \
+    } else {                                                                                          \
+      const size_t sm = sizeof(Mhd1DSmem<NN>);                                                        \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_mhd1d<NN>, sm)) != cudaSuccess) return e;                                   \
+      k_mhd1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                \
+      return cudaGetLastError();                                                                      \
+    }                                                                                                 \
   }
 
 // Launchers of the 1D-only pencil lengths: the whole-step kernel and the
@@ -263,6 +277,18 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
     if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
     k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
     return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_mhd1d<NN>(const Mhd1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    if constexpr (NN > 2048) {                                                                        \
+      return cudaErrorInvalidValue; /* 1D MHD pencils up to 2048 points */                            \
+    } else {                                                                                          \
+      const size_t sm = sizeof(Mhd1DSmem<NN>);                                                        \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_mhd1d<NN>, sm)) != cudaSuccess) return e;                                   \
+      k_mhd1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                \
+      return cudaGetLastError();                                                                      \
+    }                                                                                                 \
   }
 
 }  // namespace ps

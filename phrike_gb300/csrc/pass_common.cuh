@@ -65,8 +65,18 @@ __device__ __forceinline__ void atomic_max_nonneg(float* addr, float x) {
   atomicMax(reinterpret_cast<int*>(addr), __float_as_int(x));
 }
 
+// Lanes of the first warp that exist (blocks of fewer than 32 threads are a
+// power of two wide); shuffles stay within them.
+__device__ __forceinline__ int warp_width() { return blockDim.x < 32 ? (int)blockDim.x : 32; }
+__device__ __forceinline__ unsigned warp_mask() {
+  return blockDim.x < 32 ? ((1u << blockDim.x) - 1u) : 0xffffffffu;
+}
+
 __device__ __forceinline__ float block_max(float v, float* red) {
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int ww = warp_width();
+  const unsigned mask = warp_mask();
+  for (int o = 16; o > 0; o >>= 1)
+    if (o < ww) v = fmaxf(v, __shfl_xor_sync(mask, v, o));
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
   if (l == 0) red[w] = v;
@@ -74,7 +84,8 @@ __device__ __forceinline__ float block_max(float v, float* red) {
   if (w == 0) {
     const int nw = (blockDim.x + 31) >> 5;
     v = (l < nw) ? red[l] : 0.0f;
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1)
+      if (o < ww) v = fmaxf(v, __shfl_xor_sync(mask, v, o));
   }
   return v;  // valid in thread 0
 }
@@ -104,7 +115,28 @@ __device__ __forceinline__ RKCoef rk_coef(int stage, float dt, int rk2) {
   return c;
 }
 
-// Energy-perturbation form.  Inside the engine the energy slot of a state holds
+// Multiplier of the one-axis operators at spectral index k (tables hold
+// m s / N and k m s / N):
+//   deriv 0: P  = m s / N
+//   deriv 1: D  = i k m s / N (Nyquist term zero)
+//   deriv 2: L  = -k^2 m s / N, the one-axis factor of the spectral Laplacian
+//            (grid.py:569-579, 1329-1338: -(kx^2 + ky^2) m s, Nyquist kept)
+//   deriv 3: -k^2 / N, the second derivative without mask or filter (so that
+//            P applied after it gives L exactly, Nyquist included)
+// kunit = 2 pi / L of the axis; the result is scaled by `scale`.
+template <int N>
+__device__ __forceinline__ float2 op_symbol(float2 w, int k, int deriv, float scale, float kunit, const float* P,
+                                           const float* d) {
+  if (deriv == 1) {
+    const float dd = scale * d[k];
+    return make_float2(-w.y * dd, w.x * dd);
+  }
+  const float kk = (float)((k <= N / 2) ? k : k - N) * kunit;
+  const float s = (deriv == 0) ? scale * P[k] : (deriv == 2) ? -kk * kk * scale * P[k] : -kk * kk * scale * (1.0f / N);
+  return make_float2(w.x * s, w.y * s);
+}
+
+// Energy-perturbation form.// Energy-perturbation form.  Inside the engine the energy slot of a state holds
 // E' = E - E_ref for a per-run constant E_ref (the energy of the first cell
 // when the run starts).  With p_ref = (gamma-1) E_ref the primitive pressure
 // becomes p' = p - p_ref = (gamma-1)(E' - rho|u|^2/2), computed from small

@@ -301,10 +301,21 @@ __device__ __forceinline__ void gravity_source(const LastTArgs& a, const float* 
   k[ND + 1] += gm;
 }
 
+// Resident CTAs the register allocation must allow.  The clamped variants
+// hold every component's right-hand side until the clamp: about 170
+// registers (2D Euler) without spilling; MHD needs all 255.
+template <int N, int T, bool CLAMP, int PHYS>
+constexpr int clamp_min_blocks() {
+  if (PHYS == 1) return 1;
+  if (!CLAMP) return tma_min_blocks<N, T>();
+  const int m = 65536 / (Shape<N>::A * T * 168);
+  return m > 0 ? m : 1;
+}
+
 // PHYS 0: Euler (ND + 2 components, energy-perturbation clamp); PHYS 1: 2D
 // ideal MHD (8 components, MHD clamp, mhd_passes.cuh).
 template <int N, int T, int ND, bool CLAMP, int R, int PHYS = 0>
-__global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_blocks<N, T>())
+__global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP, PHYS>())
     k_last_t(const __grid_constant__ CUtensorMap mAB, const __grid_constant__ CUtensorMap mU,
              const __grid_constant__ CUtensorMap mAcc, LastTArgs a) {
   constexpr int NC = (PHYS == 1) ? 8 : ND + 2;
@@ -454,8 +465,33 @@ __global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_block
     }
   } else {
     float2 kk[(NC + 1) / 2][B];
+    if constexpr (PHYS == 1) {
 #pragma unroll
-    for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
+      for (int c = 0; c < NC; c += 2) rhs_pair(c, kk[c / 2]);
+    } else {
+    // one pencil-transform body for all pairs (a rolled loop; the switch keeps
+    // kk in registers): unrolled, the pairs' FFTs overflow the instruction cache
+#pragma unroll 1
+    for (int c = 0; c < NC; c += 2) {
+      float2 w[B];
+      rhs_pair(c, w);
+      switch (c / 2) {
+#define PS_KK_SET(J)                                                    \
+  case J:                                                               \
+    if constexpr (J < (NC + 1) / 2) {                                   \
+      _Pragma("unroll") for (int r = 0; r < B; ++r) kk[J][r] = w[r];    \
+    }                                                                   \
+    break;
+        PS_KK_SET(0)
+        PS_KK_SET(1)
+        PS_KK_SET(2)
+        PS_KK_SET(3)
+#undef PS_KK_SET
+        default:
+          break;
+      }
+    }
+    }
     if constexpr (PHYS == 0) {
       if (a.gravity && valid) {
         const float* uin = a.Uin + (long)sol * a.ssUn;
@@ -526,14 +562,30 @@ __global__ void __launch_bounds__(Shape<N>::A * T, PHYS == 1 ? 1 : tma_min_block
             for (int c = 0; c < NC; ++c) acc_s[addr(c, n0 + j)] = ac[j][c];
         }
       }
-#pragma unroll
+#pragma unroll 1
       for (int c = 0; c < NC; c += 2) {
-        if (a.stage == 3 && a.filter_last) filter_pair(kk[c / 2]);
+        float2 w[B];
+        switch (c / 2) {
+#define PS_KK_GET(J)                                                    \
+  case J:                                                               \
+    if constexpr (J < (NC + 1) / 2) {                                   \
+      _Pragma("unroll") for (int r = 0; r < B; ++r) w[r] = kk[J][r];    \
+    }                                                                   \
+    break;
+          PS_KK_GET(0)
+          PS_KK_GET(1)
+          PS_KK_GET(2)
+          PS_KK_GET(3)
+#undef PS_KK_GET
+          default:
+            break;
+        }
+        if (a.stage == 3 && a.filter_last) filter_pair(w);
         if (valid) {
 #pragma unroll
           for (int n2 = 0; n2 < B; ++n2) {
-            out_s[addr(c, n2)] = kk[c / 2][n2].x;
-            if (c + 1 < NC) out_s[addr(c + 1, n2)] = kk[c / 2][n2].y;
+            out_s[addr(c, n2)] = w[n2].x;
+            if (c + 1 < NC) out_s[addr(c + 1, n2)] = w[n2].y;
           }
         }
       }
@@ -557,11 +609,12 @@ struct OpTArgs {
   StridedGeom g;   // geometry of one solve; blockIdx.y runs over nsolve * g.nouter
   int axis;
   AxisOps ax;
-  int deriv;
+  int deriv;       // 0 P, 1 D, 2 L (Laplacian factor), 3 raw second derivative (op_symbol)
   float scale;
   int complement;
   int* status;
   int tcols;       // columns per tile (4, 8, 16; 0: default) = the map's box width
+  float kunit;     // 2 pi / L of the axis (deriv 2, 3)
 };
 
 template <int N, int T, int R>
@@ -606,13 +659,12 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 #pragma unroll
     for (int r = 0; r < B; ++r) {
       const int k = pf.kidx(r);
-      if (a.deriv) {
-        const float dd = a.scale * S.ax.d[k];
-        w[r] = make_float2(-w[r].y * dd, w[r].x * dd);
-      } else {
-        const float s = comp ? (1.0f / N) - S.ax.P[k] : a.scale * S.ax.P[k];
+      if (comp) {
+        const float s = (1.0f / N) - S.ax.P[k];
         w[r].x *= s;
         w[r].y *= s;
+      } else {
+        w[r] = op_symbol<N>(w[r], k, a.deriv, a.scale, a.kunit, S.ax.P, S.ax.d);
       }
     }
     pf.inv(w);

@@ -79,6 +79,7 @@ struct ps_plan_s {
   // 2D ideal MHD (PS_EQ_MHD): half spectra of the Helmholtz projection
   bool mhd = false;
   float2* H = nullptr;                    // [nsolve][2][ny][nx/2+1]
+  float* dif_buf = nullptr;               // explicit diffusion: per group T1, T2 (3 fields each)
   // tensor-core split-bf16 contractions: hi/lo planes and their TMA maps
   int pitch[2] = {0, 0};                  // bf16 row pitch along x / y (multiple of 8)
   void* Dsplit[2] = {nullptr, nullptr};   // [2][n][pitch] of D_x, D_y
@@ -90,6 +91,19 @@ struct ps_plan_s {
   ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
   long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
   int rows() const { return (int)(cells / n[0]); }     // x-pencil rows of one solve
+  // parabolic CFL cap of explicit MHD diffusion: cfl_diff / (max(eta, nu)
+  // k^2_max), k^2_max = sum over axes of (pi n / L)^2 (solver.py:916-929,
+  // 1018-1034); 0 when there is no diffusion
+  double dt_diff() const {
+    const double dif = fmax(desc.mhd_resistivity, desc.mhd_viscosity);
+    if (!mhd || !(dif > 0.0)) return 0.0;
+    double k2 = 0.0;
+    for (int a = 0; a < nd; ++a) {
+      const double km = M_PI * n[a] / desc.length[a];
+      k2 += km * km;
+    }
+    return desc.mhd_cfl_diff / (dif * k2);
+  }
   double hmin() const {                                 // smallest grid spacing (CFL)
     if (lgl) return lgl_hmin;
     double h = desc.length[0] / n[0];

@@ -82,9 +82,11 @@ int validate(const ps_plan_desc* d) {
     return fail(PS_ERR_INVALID, "scheme must be PS_SCHEME_RK4 or PS_SCHEME_RK2 (got %d)", d->scheme);
   if (is_lgl(d)) return ps::lgl_validate(d);
   if (d->equations == PS_EQ_MHD) {
-    if (d->ndim != 2) return fail(PS_ERR_UNSUPPORTED, "MHD plans are 2D (got ndim %d)", d->ndim);
-    if (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0)
-      return fail(PS_ERR_UNSUPPORTED, "explicit resistivity / viscosity are not implemented (ideal MHD only)");
+    if (d->ndim == 3) return fail(PS_ERR_UNSUPPORTED, "MHD plans are 1D or 2D (got ndim 3)");
+    if (d->ndim == 1 && d->n[0] > 2048)
+      return fail(PS_ERR_UNSUPPORTED, "1D MHD pencils are limited to 2048 points (got %d)", d->n[0]);
+    if (!(d->mhd_resistivity >= 0.0) || !(d->mhd_viscosity >= 0.0) || !(d->mhd_cfl_diff > 0.0))
+      return fail(PS_ERR_INVALID, "MHD resistivity and viscosity must be >= 0 and cfl_diff > 0");
     if (!(d->mhd_rho_min >= 0.0) || !(d->mhd_p_min >= 0.0))
       return fail(PS_ERR_INVALID, "MHD clamp floors must be non-negative");
   } else if (d->equations != PS_EQ_EULER) {
@@ -130,8 +132,8 @@ ps::AVParams av_params(const ps_plan_desc* d) {
 
 size_t scratch_fields(int nd, bool mhd = false) {
   // G + AB + acc + Us (+ 1D flux); MHD: G (16) + acc + Us + half spectra (~2)
-  if (mhd) return 16 + 8 + 8 + 3;
   if (nd == 1) return 3;
+  if (mhd) return 16 + 8 + 8 + 3;
   if (nd == 2) return 8 + 4 + 4;
   return 15 + 10 + 5 + 5;
 }
@@ -246,12 +248,19 @@ ps::StridedGeom geom_z(const ps_plan_s* p) {
 }
 
 // One-axis operator on nf fields per solve (P, D or complementary P), axis 0 = x.
+// One-axis operator (deriv: 0 P, 1 D, 2 Laplacian factor L, 3 raw second derivative)
+// on nf fields.  ss_in (axis 0 only): solve stride of `in` when it is a field
+// subset of a wider state (0: the nf-field stride of `out`).
 int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s,
-             bool complement = false, const int* active = nullptr) {
+             bool complement = false, const int* active = nullptr, long ss_in = 0) {
   ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells * p->nsolve);
   cudaError_t e;
+  const float kunit = (float)(2.0 * M_PI / p->desc.length[axis]);
+  if (axis != 0 && ss_in != 0) return fail(PS_ERR_INVALID, "field-subset input is supported along x only");
   if (axis == 0) {
     ps::OpArgs a{};
+    a.kunit = kunit;
+    a.ss_in = ss_in;
     a.active = active;
     a.in = in;
     a.out = out;
@@ -285,6 +294,7 @@ int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv
     a.complement = complement ? 1 : 0;
     a.status = p->status;
     a.tcols = (p->nd == 2) ? p->tcols : 0;
+    a.kunit = kunit;
     e = ps::dispatch_n(p->n[axis], [&](auto nc) { return ps::launch_op_t<decltype(nc)::value>(m, a, s); });
   }
   if (e != cudaSuccess) return cuda_fail(e, "operator pass");
@@ -578,6 +588,25 @@ int xfirst_mhd(ps_plan p, const float* U, float* speed, cudaStream_t s, const in
   ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * p->nsolve * (8 + 16));
   cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) { return ps::launch_xfirst_mhd<decltype(nc)::value>(a, s); });
   if (e != cudaSuccess) return cuda_fail(e, "MHD x pass");
+  if (p->dif_buf == nullptr) return PS_OK;
+  // explicit viscosity (momenta, fields 1-3) and resistivity (B, fields 5-7):
+  // T1 = L_x X and T2 = (-k_y^2) P_x X, folded into G so that the last pass adds
+  // coef lap(X) (SpectralSolverMHD._compute_rhs, solver.py:942-954)
+  const double coef[2] = {p->desc.mhd_viscosity, p->desc.mhd_resistivity};
+  const int f0[2] = {1, 5};
+  const long c3 = 3 * p->cells * p->nsolve;
+  int rc;
+  for (int g = 0; g < 2; ++g) {
+    if (coef[g] == 0.0) continue;
+    float* T1 = p->dif_buf + 2 * g * c3;
+    float* T2 = T1 + c3;
+    const float* X = U + (long)f0[g] * p->cells;
+    if ((rc = apply_op(p, 0, X, T1, 3, 2, 1.0f, s, false, active, p->ss(8))) != PS_OK) return rc;
+    if ((rc = apply_op(p, 0, X, T2, 3, 0, 1.0f, s, false, active, p->ss(8))) != PS_OK) return rc;
+    if ((rc = apply_op(p, 1, T2, T2, 3, 3, 1.0f, s, false, active)) != PS_OK) return rc;
+    PS_CU(ps::launch_mhd_diff_fold(p->G, p->ss(16), T1, T2, p->ss(3), p->cells, p->nsolve, f0[g], (float)coef[g], s),
+          "MHD diffusion");
+  }
   return PS_OK;
 }
 
@@ -613,15 +642,56 @@ int project(ps_plan p, float* Bx, float* By, float* E, long ss, const int* activ
 
 int project_state(ps_plan p, float* U, const int* active, cudaStream_t s) {
   if (!p->desc.mhd_divergence_clean) return PS_OK;  // divergence_clean "none"
+  if (p->nd == 1) {
+    PS_CU(ps::launch_project_mhd1d(U, p->cells, p->ss(8), p->nsolve, active, s), "1D projection");
+    return PS_OK;
+  }
   return project(p, U + 5 * p->cells, U + 6 * p->cells, U + 4 * p->cells, p->ss(8), active, s);
 }
 
 // Fixed dt or CFL steps: every stage the x pass, the last pass with the MHD
 // clamp and (project_each_substage) the projection; after a step, at the
 // filter cadence, the spectral filter then the projection (solver.py:988-1049).
+// 1D MHD: whole steps in k_mhd1d (rhs_out non-null: the right-hand side only)
+int mhd1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+          float* rhs_out, cudaStream_t s) {
+  ps::Mhd1DArgs a{};
+  a.U = U;
+  a.solve_stride = p->ss(8);
+  a.ax = p->ax(0);
+  a.nsteps = nsteps;
+  a.dt_dev = d_dt;
+  a.dt = dt;
+  a.gamma = (float)p->desc.gamma;
+  a.rho_min = (float)p->desc.mhd_rho_min;
+  a.p_min = (float)p->desc.mhd_p_min;
+  a.filter_interval = p->desc.filter_interval;
+  a.step_counter0 = (int)(p->step_counter % p->desc.filter_interval);
+  a.project_stages = p->desc.mhd_project_substages;
+  a.clean = p->desc.mhd_divergence_clean;
+  a.eta = (float)p->desc.mhd_resistivity;
+  a.nu = (float)p->desc.mhd_viscosity;
+  a.kunit = (float)(2.0 * M_PI / p->desc.length[0]);
+  a.t = d_t;
+  a.tend = d_tend;
+  a.cfl = (float)p->desc.cfl;
+  a.dx = (float)(p->desc.length[0] / p->n[0]);
+  a.dt_cap = p->dt_diff();
+  a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
+  a.scratch = p->acc;
+  a.rhs_out = rhs_out;
+  a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+  ProfScope prof(p, s, PS_KIND_STEP1D, 4.0 * p->cells * p->nsolve * 8 * 2);
+  cudaError_t e = ps::dispatch_n_1d(p->n[0], [&](auto nn) { return ps::launch_mhd1d<decltype(nn)::value>(a, p->nsolve, s); });
+  if (e != cudaSuccess) return cuda_fail(e, "1D MHD kernel");
+  if (rhs_out == nullptr && d_t == nullptr) p->step_counter += nsteps;
+  return PS_OK;
+}
+
 int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
               cudaStream_t s) {
   int rc;
+  if (p->nd == 1) return mhd1d(p, U, nsteps, dt, d_dt, d_t, d_tend, nullptr, s);
   const bool cfl = d_t != nullptr;
   const int* act = cfl ? p->active : nullptr;
   const double* dtp = cfl ? p->dt : d_dt;
@@ -637,7 +707,8 @@ int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
       float* out = (stage < 3) ? p->Us : U;
       if ((rc = xfirst_mhd(p, src, (cfl && stage == 0) ? p->speed : nullptr, s, act)) != PS_OK) return rc;
       if (cfl && stage == 0)
-        PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
+        PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s,
+                                      p->dt_diff()),
               "step control");
       if ((rc = last(p, stage, U, out, dt, dtp, false, s, act)) != PS_OK) return rc;
       if (p->desc.mhd_project_substages && (rc = project_state(p, out, act, s)) != PS_OK) return rc;
@@ -836,11 +907,16 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   const long c = p->cells * nsolve;
   if (p->nd == 1) {
     if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
-    if (p->n[0] >= 4096 && (rc = dalloc(p, &p->acc, 6 * c)) != PS_OK) return cleanup(rc);
+    if (!p->mhd && p->n[0] >= 4096 && (rc = dalloc(p, &p->acc, 6 * c)) != PS_OK) return cleanup(rc);
+    // 1D MHD from 2048 points: U^n and the accumulator in global scratch
+    if (p->mhd && p->n[0] >= 2048 && (rc = dalloc(p, &p->acc, 16 * c)) != PS_OK) return cleanup(rc);
   } else {
     const int ng = p->mhd ? 16 : (p->nd == 3) ? 15 : 8;
     if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
     if (p->mhd && (rc = dalloc(p, &p->H, (size_t)2 * nsolve * p->n[1] * (p->n[0] / 2 + 1))) != PS_OK)
+      return cleanup(rc);
+    if (p->mhd && (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0) &&
+        (rc = dalloc(p, &p->dif_buf, 12 * c)) != PS_OK)
       return cleanup(rc);
     if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
@@ -850,7 +926,10 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   if (p->nd == 2 && !lgl) {
     // columns per strided-pass tile: the widest of 16, 8, 4 that still gives
     // about two CTAs per SM (small grids get more, narrower CTAs)
-    const int cap = (p->n[1] >= 1024) ? 8 : 16;
+    // 2D Euler: the clamped last pass runs at ~168 registers without spills
+    // with 128-thread CTAs (8 columns of 16-thread pencils at N <= 256, 4
+    // columns at 512 and up) and three CTAs per SM
+    const int cap = p->mhd ? ((p->n[1] >= 1024) ? 8 : 16) : ((p->n[1] >= 512) ? 4 : (p->n[1] >= 256) ? 8 : 16);
     p->tcols = 4;
     for (int T = cap; T >= 4; T /= 2) {
       if ((long)((p->n[0] + T - 1) / T) * nsolve >= 2L * 148) {
@@ -923,6 +1002,7 @@ int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   for (int c = 0; c < 5; ++c) d->av_weight[c] = 1.0;
   d->mhd_rho_min = 1e-10;
   d->mhd_p_min = 1e-12;
+  d->mhd_cfl_diff = 1.0;
   d->mhd_project_substages = 1;
   d->mhd_divergence_clean = 1;
   return PS_OK;
@@ -940,7 +1020,10 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
-  if (d->ndim == 1 && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
+  const bool mhd = d->equations == PS_EQ_MHD;
+  if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
+  if (d->ndim == 1 && mhd && d->n[0] >= 2048) fields += 16;
+  if (mhd && d->ndim == 2 && (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0)) fields += 12;
   *bytes = fields * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
@@ -1017,6 +1100,7 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
   int rc;
   if (p->lgl) return ps::lgl_rhs(p, U, rhs, s);
   if (p->mhd) {
+    if (p->nd == 1) return mhd1d(p, const_cast<float*>(U), 0, 0.0, nullptr, nullptr, nullptr, rhs, s);
     if ((rc = xfirst_mhd(p, U, nullptr, s, nullptr)) != PS_OK) return rc;
     return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
   }
@@ -1158,8 +1242,14 @@ int ps_project_state(ps_plan p, float* U, void* stream) {
 int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
   if (!p || !U || !d_out) return fail(PS_ERR_INVALID, "null argument");
   if (p->mhd) {
-    PS_CU(ps::launch_speed_mhd(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out, (cudaStream_t)stream),
-          "max wave speed");
+    if (p->nd == 1)
+      PS_CU(ps::launch_speed_mhd1d(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out,
+                                   (cudaStream_t)stream),
+            "max wave speed");
+    else
+      PS_CU(ps::launch_speed_mhd(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out,
+                                 (cudaStream_t)stream),
+            "max wave speed");
     return PS_OK;
   }
   PS_CU(ps::launch_speed(p->nd, U, p->cells, p->ss(p->nc), p->nsolve, (float)p->desc.gamma, d_out,

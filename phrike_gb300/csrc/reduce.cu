@@ -99,6 +99,49 @@ __global__ void k_speed_mhd(const float* __restrict__ U, long cells, long ss, fl
   if (threadIdx.x == 0) atomic_max_nonneg(out, m);
 }
 
+// 1D MHD CFL speed (MHDEquations1D.max_wave_speed, equations.py:735-750):
+// |u_x| + c_f with the exact fast magnetosonic speed along x
+__global__ void k_speed_mhd1d(const float* __restrict__ U, long cells, long ss, float gamma, float* out) {
+  __shared__ float red[32];
+  U += (long)blockIdx.y * ss;
+  out += blockIdx.y;
+  float m = 0.0f;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
+    const float rho = U[i];
+    const float ux = U[cells + i] / rho, uy = U[2 * cells + i] / rho, uz = U[3 * cells + i] / rho;
+    const float bx = U[5 * cells + i], by = U[6 * cells + i], bz = U[7 * cells + i];
+    const float b2 = bx * bx + by * by + bz * bz;
+    const float p = (gamma - 1.0f) * (U[4 * cells + i] - 0.5f * rho * (ux * ux + uy * uy + uz * uz) - 0.5f * b2);
+    const float a2 = gamma * p / rho, bb = b2 / rho, cax2 = bx * bx / rho;
+    const float disc = fmaxf((a2 + bb) * (a2 + bb) - 4.0f * a2 * cax2, 0.0f);
+    m = fmaxf(m, fabsf(ux) + sqrtf(0.5f * (a2 + bb + sqrtf(disc))));
+  }
+  m = block_max(m, red);
+  if (threadIdx.x == 0) atomic_max_nonneg(out, m);
+}
+
+// 1D projection (grid.py:554-567 with solver.py:966-986): Bx <- mean(Bx),
+// E += (Bx_new^2 - Bx_old^2) / 2; one block per solve
+__global__ void k_project_mhd1d(float* U, long n, long ss, const int* active) {
+  __shared__ float red[32];
+  if (active != nullptr && !active[blockIdx.x]) return;
+  U += (long)blockIdx.x * ss;
+  float sum = 0.0f;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) sum += U[5 * n + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  float tot = 0.0f;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+  const float mean = tot / (float)n;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    const float bo = U[5 * n + i];
+    U[4 * n + i] += 0.5f * (mean * mean - bo * bo);
+    U[5 * n + i] = mean;
+  }
+}
+
 // 2D ideal MHD conserved sums in float64 (equations.py:889-907): mass,
 // momentum x/y/z, energy rebuilt from primitives, magnetic energy, cross
 // helicity (and a zero pad to 8 values)
@@ -169,12 +212,13 @@ __global__ void k_energy_shift(float* E, long n, long ss, const float* eref, flo
 // Per-solve CFL step control before a step (solver.py:386-389, 235-240):
 // active = t < t_end - 1e-12; dt = active ? min(cfl h / speed, t_end - t) : 0.
 __global__ void k_step_control(const float* speed, double cfl, double hmin, const double* t, const double* tend,
-                               int nsolve, double* dt, int* active) {
+                               int nsolve, double* dt, int* active, double dt_cap) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsolve) return;
   const bool on = t[s] < tend[s] - 1e-12;
   const double sp = (double)speed[s];
   double d = (sp <= 0.0) ? 1e-6 : cfl * hmin / sp;
+  if (sp > 0.0 && dt_cap > 0.0) d = fmin(d, dt_cap);  // parabolic limit of explicit diffusion
   d = fmin(d, tend[s] - t[s]);
   dt[s] = on ? d : 0.0;
   active[s] = on ? 1 : 0;
@@ -215,8 +259,8 @@ cudaError_t launch_energy_shift(float* E, long n, long ss, int nsolve, const flo
 }
 
 cudaError_t launch_step_control(const float* speed, double cfl, double hmin, const double* t, const double* tend,
-                                int nsolve, double* dt, int* active, cudaStream_t s) {
-  k_step_control<<<(nsolve + 127) / 128, 128, 0, s>>>(speed, cfl, hmin, t, tend, nsolve, dt, active);
+                                int nsolve, double* dt, int* active, cudaStream_t s, double dt_cap) {
+  k_step_control<<<(nsolve + 127) / 128, 128, 0, s>>>(speed, cfl, hmin, t, tend, nsolve, dt, active, dt_cap);
   return cudaGetLastError();
 }
 
@@ -271,6 +315,19 @@ cudaError_t launch_speed_mhd(const float* U, long cells, long ss, int nsolve, fl
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * nsolve, s);
   if (e != cudaSuccess) return e;
   k_speed_mhd<<<dim3(reduce_blocks(cells, nsolve), nsolve), 256, 0, s>>>(U, cells, ss, gamma, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_speed_mhd1d(const float* U, long cells, long ss, int nsolve, float gamma, float* out,
+                               cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * nsolve, s);
+  if (e != cudaSuccess) return e;
+  k_speed_mhd1d<<<dim3(reduce_blocks(cells, nsolve), nsolve), 256, 0, s>>>(U, cells, ss, gamma, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_mhd1d(float* U, long n, long ss, int nsolve, const int* active, cudaStream_t s) {
+  k_project_mhd1d<<<nsolve, 256, 0, s>>>(U, n, ss, active);
   return cudaGetLastError();
 }
 

@@ -90,6 +90,7 @@ class Plan:
             desc.mhd_divergence_clean = 0 if str(mc.get("divergence_clean", "projection")) == "none" else 1
             desc.mhd_resistivity = float(mc.get("resistivity", 0.0))
             desc.mhd_viscosity = float(mc.get("viscosity", 0.0))
+            desc.mhd_cfl_diff = float(mc.get("cfl_diff", 1.0))
         if av_config and av_config.get("enabled", False):
             # ArtificialViscosityConfig fields and defaults (artificial_viscosity.py:37-105)
             mode = str(av_config.get("mode", "sensor")).lower().strip()

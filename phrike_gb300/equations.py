@@ -199,3 +199,23 @@ class MHDEquations2D:
                 "momentum_y": float((rho * uy).double().sum()), "momentum_z": float((rho * uz).double().sum()),
                 "energy": float(E.double().sum()), "magnetic_energy": float((0.5 * b2).double().sum()),
                 "cross_helicity": float((ux * Bx + uy * By + uz * Bz).double().sum())}
+
+
+@dataclass
+class MHDEquations1D(MHDEquations2D):
+    """Ideal compressible MHD varying along x only (phrike/equations.py:659-767):
+    the same 8-component state, the x flux alone (its Bx row is zero, so Bx
+    stays constant) and |u_x| + c_f (exact fast magnetosonic speed along x)."""
+
+    gamma: float = 5.0 / 3.0
+
+    def flux(self, U):
+        return super().flux(U)[0]
+
+    def max_wave_speed(self, U) -> float:
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        a2 = self.gamma * p / rho
+        b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+        cax2 = Bx * Bx / rho
+        disc = torch.clamp((a2 + b2) * (a2 + b2) - 4.0 * a2 * cax2, min=0.0)
+        return float(torch.max(torch.abs(ux) + torch.sqrt(0.5 * (a2 + b2 + torch.sqrt(disc)))).item())

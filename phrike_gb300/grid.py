@@ -145,9 +145,19 @@ class Grid1D(_FourierGridBase):
         self.ik = 1j * self.k
         self.dealias_mask = torch.as_tensor(_mask_1d(self.N, dealias), device=self.device)
         self.filter_sigma = torch.as_tensor(_sigma_1d(self.N, filter_params), device=self.device)
+        self.mhd_config: Optional[Dict[str, Any]] = None  # set by MHD problems (grid.mhd_config)
 
     def dx1(self, f: Any) -> torch.Tensor:
         return self._op(f, 0)
+
+    def divergence_x(self, Bx: Any) -> torch.Tensor:
+        """d(Bx)/dx with the masked derivative (grid.py:550-552)."""
+        return self.dx1(Bx)
+
+    def project_solenoidal_x(self, Bx: Any) -> torch.Tensor:
+        """The 1D Leray projection keeps only the mean of Bx (grid.py:554-567)."""
+        t = self.to_device(Bx)
+        return torch.full_like(t, float(t.double().mean().item()))
 
 
 class Grid2D(_FourierGridBase):

@@ -7,6 +7,7 @@ served workloads:
 * Taylor-Green vortex, 3D periodic [0, 2 pi)^3           (``taylor_green_3d``)
 * Kelvin-Helmholtz shear layer, 2D periodic [0, 1)^2     (``kelvin_helmholtz_2d``)
 * Orszag-Tang vortex (ideal MHD), 2D periodic [0, 2 pi)^2 (``orszag_tang_2d``)
+* circularly polarized Alfven wave (MHD), 1D periodic (``alfven_cp_1d``)
 * Gaussian acoustic pulse on Legendre-Gauss-Lobatto nodes (``acoustic_pulse_lgl_2d``)
 
 All return conservative states with component-first layout and spatial axes
@@ -96,6 +97,25 @@ def orszag_tang_2d(Nx: int, Ny: int = None, gamma: float = 5.0 / 3.0, rho0: floa
     Bz = np.zeros_like(X)
     E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
     return np.stack([rho, rho * u, rho * v, rho * w, E, Bx, By, Bz])
+
+
+def alfven_cp_1d(N: int, L: float = 1.0, t: float = 0.0, rho0: float = 1.0, p0: float = 0.1, B0: float = 1.0,
+                 b1: float = 0.1, m: int = 1, direction: int = 1, gamma: float = 5.0 / 3.0) -> np.ndarray:
+    """Circularly polarized Alfven wave on [0, L) (the reference's alfven1d
+    problem, problems/problem_list/alfven1d.py:30-82): rho = rho0, p = p0,
+    Bx = B0, (By, Bz) = b1 (cos, sin)(k x - k c_A t), u_perp = -direction
+    B_perp / sqrt(rho0), u_x = 0; 8 MHD components."""
+    x = np.linspace(0.0, L, N, endpoint=False)
+    cA = B0 / np.sqrt(rho0)
+    k = 2.0 * np.pi * m / L
+    phi = k * x - k * direction * cA * t
+    By, Bz = b1 * np.cos(phi), b1 * np.sin(phi)
+    rho = np.full_like(x, rho0)
+    ux = np.zeros_like(x)
+    uy, uz = -direction * By / np.sqrt(rho0), -direction * Bz / np.sqrt(rho0)
+    Bx = np.full_like(x, B0)
+    E = p0 / (gamma - 1.0) + 0.5 * rho * (uy * uy + uz * uz) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    return np.stack([rho, rho * ux, rho * uy, rho * uz, E, Bx, By, Bz])
 
 
 def acoustic_pulse_lgl_2d(x: np.ndarray, y: np.ndarray, gamma: float = 1.4,

@@ -12,6 +12,7 @@ returns a new tensor and leaves its argument untouched.
 """
 from __future__ import annotations
 
+import math
 from typing import Any, Callable, Dict, List, Optional
 
 import torch
@@ -253,12 +254,15 @@ class SpectralSolverMHD2D(_SpectralSolverBase):
     """2D (2.5D) ideal MHD, RK4 (phrike/solver.py:840-1049, 1169-1170).
 
     Options come from ``grid.mhd_config`` like the reference (resistivity,
-    viscosity, project_each_substage, divergence_clean, rho_min, p_min;
-    explicit resistivity/viscosity are not implemented).  Every RK stage is
-    clamped and projected on the device; after a step, at the filter cadence,
-    the spectral filter and the projection.  run() projects U0 first and
-    records magnetic energy, cross helicity and max |div B| as well.
-    CFL dt = cfl * min(dx, dy) / max(max(|ux|, |uy|) + sqrt(a^2 + b^2)).
+    viscosity, cfl_diff, project_each_substage, divergence_clean, rho_min,
+    p_min).  Every RK stage is clamped and projected on the device; after a
+    step, at the filter cadence, the spectral filter and the projection.
+    Explicit resistivity / viscosity add eta lap(B) / nu lap(rho u) to the
+    right-hand side (solver.py:942-954).  run() projects U0 first and records
+    magnetic energy, cross helicity and max |div B| as well.
+    CFL dt = cfl * min(dx, dy) / max(max(|ux|, |uy|) + sqrt(a^2 + b^2)),
+    capped by cfl_diff / (max(eta, nu) k^2_max) with diffusion
+    (solver.py:1018-1034).
     """
 
     _ndim = 2
@@ -273,17 +277,31 @@ class SpectralSolverMHD2D(_SpectralSolverBase):
         self.viscosity = float(cfg.get("viscosity", 0.0))
         self.project_each_substage = bool(cfg.get("project_each_substage", True))
         self.divergence_clean = str(cfg.get("divergence_clean", "projection"))
-        if self.resistivity != 0.0 or self.viscosity != 0.0:
-            raise NotImplementedError("backend 'gb300': explicit resistivity/viscosity are not implemented")
+        self.cfl_diff = float(cfg.get("cfl_diff", 1.0))
         if gravity_config and gravity_config.get("enabled", False):
             raise NotImplementedError("backend 'gb300': gravity is not implemented for MHD")
-        self.dim = 2
+        if adaptive_config and adaptive_config.get("enabled", False) and self._ndim == 1:
+            raise NotImplementedError("backend 'gb300': adaptive stepping of 1D MHD is not implemented")
+        self.dim = self._ndim
         # the reference's MHD solver takes artificial_viscosity_config for API
         # compatibility and does not use it
         super().__init__(grid, equations, U0, scheme, cfl, adaptive_config, None, None)
 
     def _spacing(self) -> float:
         return min(self.grid.dx, self.grid.dy)
+
+    def compute_dt(self, U: Any) -> float:
+        s = float(self.plan.max_wave_speed(self.grid.to_device(U)).item())
+        if s <= 0.0:
+            return 1e-6
+        dt = self.cfl * self._spacing() / s
+        dif = max(self.resistivity, self.viscosity)
+        if dif > 0.0:  # parabolic limit, k^2_max = sum over axes of (pi N / L)^2 (solver.py:916-929)
+            dt = min(dt, self.cfl_diff / (dif * self._k2_max()))
+        return dt
+
+    def _k2_max(self) -> float:
+        return (math.pi * self.grid.Nx / self.grid.Lx) ** 2 + (math.pi * self.grid.Ny / self.grid.Ly) ** 2
 
     def _project_B(self, U: Any) -> torch.Tensor:
         V = self.grid.to_device(U).clone()
@@ -305,3 +323,24 @@ class SpectralSolverMHD2D(_SpectralSolverBase):
         """solver.py:1092-1162: the initial state is projected first."""
         return super().run(self._project_B(U0), t0, t_end, output_interval, checkpoint_interval, outdir,
                            on_output, on_step, tracers, dt)
+
+
+class SpectralSolverMHD1D(SpectralSolverMHD2D):
+    """1D MHD (phrike/solver.py:840-1049, 1165-1166): the x flux of
+    MHDEquations1D, every RK stage clamped and (project_each_substage)
+    projected with Bx <- mean(Bx), the filter and the projection at the
+    cadence, explicit resistivity / viscosity; whole steps run in one kernel
+    per solve.  CFL dt = cfl * dx / max(|u_x| + c_f), c_f the exact fast
+    magnetosonic speed along x."""
+
+    _ndim = 1
+
+    def _spacing(self) -> float:
+        return self.grid.dx
+
+    def _k2_max(self) -> float:
+        return (math.pi * self.grid.N / self.grid.Lx) ** 2
+
+    def max_div_b(self, U: Any) -> float:
+        t = self.grid.to_device(U)
+        return float(torch.max(torch.abs(self.grid.dx1(t[5]))).item())

@@ -49,6 +49,10 @@ def main(ref_path: str, only: str = "") -> None:
         return adaptive_fixtures(grid, equations, solver, problems)
     if only == "rk2":
         return rk2_fixtures(grid, equations, solver, problems)
+    if only == "mhd_diffusion":
+        return mhd_diffusion_fixtures(grid, equations, solver, problems)
+    if only == "mhd1d":
+        return mhd1d_fixtures(grid, equations, solver, problems)
 
     out = {}
 
@@ -203,6 +207,64 @@ def source_fixtures(grid, equations, solver, problems) -> None:
         out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
                                                            None)
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+def mhd1d_fixtures(grid, equations, solver, problems) -> None:
+    """1D MHD (SpectralSolverMHD1D): the circularly polarized Alfven wave with
+    a compressive perturbation and a non-uniform Bx (so the projection acts),
+    filter on; ideal RK4 and resistive/viscous RK2 runs, plus a CFL run."""
+    out = {}
+    x = np.linspace(0.0, 1.0, 128, endpoint=False)
+    U0 = problems.alfven_cp_1d(128)
+    U0[0] *= 1.0 + 0.05 * np.sin(2 * np.pi * x)
+    U0[1] = 0.02 * np.cos(4 * np.pi * x)
+    U0[5] += 0.01 * np.sin(6 * np.pi * x)
+    out["U0"] = U0
+    for tag, cfg, scheme in (("ideal", {}, "rk4"), ("diff", {"resistivity": 0.01, "viscosity": 0.005}, "rk2")):
+        g = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params={"enabled": True, "p": 8, "alpha": 36.0})
+        g.mhd_config = dict(cfg)
+        s = solver.SpectralSolverMHD1D(g, equations.MHDEquations1D(gamma=5.0 / 3.0), scheme=scheme, cfl=0.4)
+        out[f"{tag}_rhs0"] = s._compute_rhs(U0.copy())
+        out[f"{tag}_P0"] = s._project_B(U0.copy())
+        U = U0.copy()
+        for _ in range(4):
+            U = s.step(U, 1e-3)
+        out[f"{tag}_U"] = U
+        out[f"{tag}_dt0"] = s.compute_dt(U0)
+    g = grid.Grid1D(N=128, Lx=1.0, dealias=True, filter_params={"enabled": True, "p": 8, "alpha": 36.0})
+    g.mhd_config = {}
+    s = solver.SpectralSolverMHD1D(g, equations.MHDEquations1D(gamma=5.0 / 3.0), cfl=0.4)
+    seen = []
+    s.run(U0.copy(), 0.0, 0.05, output_interval=0.05, on_step=lambda n, dt, U: seen.append(dt))
+    out["cfl_U"], out["cfl_t"], out["cfl_dts"] = np.asarray(s.U), s.t, np.asarray(seen)
+    np.savez_compressed(os.path.join(HERE, "mhd1d.npz"), **out)
+
+
+def mhd_diffusion_fixtures(grid, equations, solver, problems) -> None:
+    """2D MHD with explicit resistivity and viscosity: rhs, CFL dt (with the
+    parabolic limit) and RK4 steps, filter on (32x32) and off with dealias
+    off (32x16, so the Nyquist modes take part)."""
+    out = {}
+    for tag, (nx, ny), fp, dealias, eta, nu in (("a", (32, 32), {"enabled": True, "p": 8, "alpha": 36.0}, True,
+                                                  0.02, 0.01),
+                                                 ("b", (32, 16), None, False, 0.2, 0.0)):
+        L = 2.0 * np.pi
+        g = grid.Grid2D(Nx=nx, Ny=ny, Lx=L, Ly=L, dealias=dealias, filter_params=fp)
+        g.mhd_config = {"resistivity": eta, "viscosity": nu, "project_each_substage": True,
+                        "divergence_clean": "projection", "cfl_diff": 0.8}
+        s = solver.SpectralSolverMHD2D(g, equations.MHDEquations2D(gamma=5.0 / 3.0), cfl=0.3)
+        U0 = problems.orszag_tang_2d(nx, ny, gamma=5.0 / 3.0)
+        X, Y = np.meshgrid(np.asarray(g.x), np.asarray(g.y), indexing="xy")
+        U0[1] += 0.1 * np.sin(3 * X) * np.cos(2 * Y)
+        U0[7] = 0.1 * np.cos(X + Y)
+        U0 = s._project_B(U0)
+        U = U0.copy()
+        for _ in range(3):
+            U = s.step(U, 1e-3)
+        out[f"{tag}_U0"], out[f"{tag}_U"] = U0, U
+        out[f"{tag}_rhs0"] = s._compute_rhs(U0.copy())
+        out[f"{tag}_dt"] = s.compute_dt(U0)
+    np.savez_compressed(os.path.join(HERE, "mhd_diffusion.npz"), **out)
+
 
 def rk2_fixtures(grid, equations, solver, problems) -> None:
     """scheme="rk2" (midpoint) fixed steps of every solver: 1D Sod (filter on,

@@ -156,3 +156,38 @@ def test_mhd_solver_api_and_projection_helpers(cuda_device):
         assert key in hist and len(hist[key]) == len(hist["time"])
     assert max(hist["div_b_max"]) < 1e-4
     assert abs(hist["mass"][-1] - hist["mass"][0]) < 1e-6 * abs(hist["mass"][0])
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_mhd_resistivity_viscosity_match_reference(tag, cuda_device):
+    """Explicit resistivity eta lap(B) and viscosity nu lap(rho u) (the
+    spectral Laplacian with mask and filter; case b without dealiasing, so the
+    Nyquist modes take part) against the reference: right-hand side, the CFL
+    dt with the parabolic limit, and three RK4 steps."""
+    import torch
+    from phrike_gb300.engine import Plan
+    from phrike_gb300.grid import Grid2D
+    from phrike_gb300.equations import MHDEquations2D
+    from phrike_gb300.solver import SpectralSolverMHD2D
+    z = golden("mhd_diffusion.npz")
+    (nx, ny), fp, dealias, eta, nu = {"a": ((32, 32), {"enabled": True, "p": 8, "alpha": 36.0}, True, 0.02, 0.01),
+                                      "b": ((32, 16), None, False, 0.2, 0.0)}[tag]
+    mc = {"resistivity": eta, "viscosity": nu, "cfl_diff": 0.8}
+    plan = Plan((ny, nx), (2 * np.pi, 2 * np.pi), gamma=5.0 / 3.0, dealias=dealias, filter_params=fp,
+                equations="mhd", mhd_config=mc)
+    U0 = torch.as_tensor(z[f"{tag}_U0"], dtype=torch.float32, device=cuda_device).contiguous()
+    rhs = plan.rhs(U0).double().cpu().numpy()
+    assert max(_errs(rhs, z[f"{tag}_rhs0"])) < 2e-5, _errs(rhs, z[f"{tag}_rhs0"])
+    U = U0.clone()
+    plan.run_(U, 3, 1e-3)
+    assert max(_errs(U.double().cpu().numpy(), z[f"{tag}_U"])) < 2e-5
+    g = Grid2D(Nx=nx, Ny=ny, Lx=2 * np.pi, Ly=2 * np.pi, dealias=dealias, filter_params=fp, backend="gb300")
+    g.mhd_config = mc
+    s = SpectralSolverMHD2D(g, MHDEquations2D(gamma=5.0 / 3.0), cfl=0.3)
+    dt = s.compute_dt(U0)
+    assert abs(dt - float(z[f"{tag}_dt"])) < 1e-5 * float(z[f"{tag}_dt"])
+    # the device CFL loop applies the same cap: one step from t = 0 takes that dt
+    t = torch.zeros(1, dtype=torch.float64, device=cuda_device)
+    te = torch.ones(1, dtype=torch.float64, device=cuda_device)
+    plan.run_cfl_(U0.clone(), 1, t, te)
+    assert abs(t.item() - dt) < 1e-5 * dt

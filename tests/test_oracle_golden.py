@@ -244,3 +244,53 @@ def test_rk2_scheme_matches_reference():
     for _ in range(3):
         W = sm.step(W, 2e-3)
     assert rel_l2(W, z["ot_U"]) < 1e-12
+
+
+def test_mhd_resistivity_viscosity_match_reference():
+    """2D MHD with explicit resistivity and viscosity (the spectral Laplacian
+    with mask and filter, Nyquist modes included when dealiasing is off) and
+    the parabolic CFL limit, against the reference's own runs."""
+    from oracle import mhd as M
+    z = golden("mhd_diffusion.npz")
+    for tag, (nx, ny), fp, dealias, eta, nu in (("a", (32, 32), {"enabled": True, "p": 8, "alpha": 36.0}, True,
+                                                  0.02, 0.01),
+                                                 ("b", (32, 16), None, False, 0.2, 0.0)):
+        s = M.MHDSolver2D(nx, ny, filter_params=fp, dealias=dealias, cfl=0.3, resistivity=eta, viscosity=nu,
+                          cfl_diff=0.8)
+        U0 = z[f"{tag}_U0"]
+        assert rel_l2(s.rhs(U0), z[f"{tag}_rhs0"]) < 1e-12, tag
+        assert abs(s.compute_dt(U0) - float(z[f"{tag}_dt"])) < 1e-12 * float(z[f"{tag}_dt"]), tag
+        U = U0.copy()
+        for _ in range(3):
+            U = s.step(U, 1e-3)
+        assert rel_l2(U, z[f"{tag}_U"]) < 1e-12, tag
+
+
+def test_mhd1d_matches_reference():
+    """1D MHD (SpectralSolverMHD1D): right-hand side, the 1D projection
+    (Bx -> mean, thermal pressure held), ideal RK4 and resistive/viscous RK2
+    steps, the CFL dt with the exact fast speed and the parabolic limit, and
+    the CFL run, against the reference."""
+    from oracle import mhd as M
+    z = golden("mhd1d.npz")
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    U0 = z["U0"]
+    for tag, kw, scheme in (("ideal", {}, "rk4"), ("diff", {"resistivity": 0.01, "viscosity": 0.005}, "rk2")):
+        s = M.MHDSolver1D(128, 1.0, filter_params=fp, cfl=0.4, scheme=scheme, **kw)
+        assert rel_l2(s.rhs(U0), z[f"{tag}_rhs0"]) < 1e-12, tag
+        assert rel_l2(s.project(U0), z[f"{tag}_P0"]) < 1e-14, tag
+        assert abs(s.compute_dt(U0) - float(z[f"{tag}_dt0"])) < 1e-12 * float(z[f"{tag}_dt0"]), tag
+        U = U0.copy()
+        for _ in range(4):
+            U = s.step(U, 1e-3)
+        assert rel_l2(U, z[f"{tag}_U"]) < 1e-12, tag
+    s = M.MHDSolver1D(128, 1.0, filter_params=fp, cfl=0.4)
+    U = s.project(U0)
+    t, dts = 0.0, []
+    while t < 0.05 - 1e-12:
+        dt = min(s.compute_dt(U), 0.05 - t)
+        U = s.step(U, dt)
+        t += dt
+        dts.append(dt)
+    np.testing.assert_allclose(dts, z["cfl_dts"], rtol=1e-12)
+    assert rel_l2(U, z["cfl_U"]) < 1e-12
