@@ -92,6 +92,12 @@ typedef struct {
    * solver.py:878-880): dt <= mhd_cfl_diff / (max(eta, nu) k^2_max).
    * Default 1. */
   double mhd_cfl_diff;
+  /* 1D Legendre grids: boundary codes per side (left, right) and variable
+   * (density, momentum, energy), index side * 3 + variable: 0 copy the
+   * neighbouring interior value (Neumann), 1 set to zero (the momentum of a
+   * wall), 2 leave unchanged (Grid1D.apply_boundary_conditions,
+   * grid.py:620-735).  Default: walls, {0, 1, 0, 0, 1, 0}. */
+  int lgl_bc1d[6];
 } ps_plan_desc;
 
 #define PS_SCHEME_RK4 0

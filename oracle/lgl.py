@@ -165,3 +165,146 @@ class LGLSolver2D:
         s = float(np.max(np.abs(vel[0]) + np.sqrt(self.gamma * p / rho)))
         h = min(float(np.min(np.diff(self.ax.x))), float(np.min(np.diff(self.ay.x))))
         return 1e-6 if s <= 0 else self.cfl * h / s
+
+
+# wall / neumann boundary codes per (boundary, variable): 0 copy the
+# neighbouring interior value, 1 set to zero, 2 leave unchanged
+BC_COPY, BC_ZERO, BC_NONE = 0, 1, 2
+
+
+def bc_codes_1d(bc) -> np.ndarray:
+    """Resolve Grid1D's boundary configuration (a string, a per-variable or a
+    per-boundary dict; grid.py:184-246) into codes [boundary (left, right)]
+    [variable (density, momentum, energy)] following apply_boundary_conditions
+    (grid.py:620-735): "wall" (aliases reflective, dirichlet) zeroes the
+    momentum and copies the interior value into density and energy;
+    "neumann" (alias open) copies for every variable."""
+    def norm_bc(v):
+        n = str(v).strip().lower()
+        return "wall" if n in ("reflective", "dirichlet", "wall") else "neumann" if n in ("neumann", "open") else n
+
+    def norm_var(v):
+        n = str(v).strip().lower()
+        if n in ("rho", "density"):
+            return "density"
+        if n in ("p", "pressure"):
+            return "pressure"
+        if n in ("u", "velocity", "mom", "momentum", "momentum_x"):
+            return "momentum"
+        return n
+
+    def norm_side(b):
+        n = str(b).strip().lower()
+        return "left" if n in ("left", "x0", "x_min", "start") else "right" if n in ("right", "x1", "x_max", "end") else n
+
+    g, var_map, side_map = None, None, None
+    if isinstance(bc, dict):
+        if any(str(k).lower() in ("left", "right", "x0", "x1", "x_min", "x_max", "start", "end") for k in bc):
+            side_map = {}
+            for bk, vd in bc.items():
+                side = norm_side(bk)
+                if isinstance(vd, dict):
+                    side_map[side] = {norm_var(k): norm_bc(v) for k, v in vd.items()}
+                else:
+                    side_map[side] = {v: norm_bc(vd) for v in ("density", "momentum", "pressure")}
+        else:
+            var_map = {norm_var(k): norm_bc(v) for k, v in bc.items()}
+    elif isinstance(bc, str) and bc:
+        g = norm_bc(bc)
+
+    def get(var, side):
+        if side_map is not None and side in side_map:
+            return side_map[side].get(var, g or "wall")
+        if var_map is not None:
+            return var_map.get(var, g or "wall")
+        gg = g or "wall"
+        if gg == "wall":
+            return "wall" if var == "momentum" else "neumann"
+        return gg
+
+    codes = np.full((2, 3), BC_NONE, dtype=np.int32)
+    for si, side in enumerate(("left", "right")):
+        for vi, var in enumerate(("density", "momentum", "pressure")):
+            b = get(var, side)
+            if var == "momentum":
+                codes[si, vi] = BC_ZERO if b in ("wall", "reflective") else BC_COPY if b in ("neumann", "open") else BC_NONE
+            else:
+                codes[si, vi] = BC_COPY if b in ("neumann", "open", "wall") else BC_NONE
+    return codes
+
+
+def apply_bc_1d(U: np.ndarray, codes: np.ndarray) -> np.ndarray:
+    """In place; variables in the order density, momentum, energy and, per
+    variable, left then right (grid.py:702-735)."""
+    for vi in range(3):
+        for si, (dst, src) in enumerate(((0, 1), (-1, -2))):
+            c = codes[si, vi]
+            if c == BC_COPY:
+                U[vi, dst] = U[vi, src]
+            elif c == BC_ZERO:
+                U[vi, dst] = 0.0
+    return U
+
+
+class LGLSolver1D:
+    """SpectralSolver1D on a Legendre grid (solver.py:62-132, 259-269): the
+    boundary conditions applied in place to every stage input, flux, rhs =
+    -D F (plus constant gravity), 1D clamp after every stage, and after the
+    step the nodal filter (if enabled) with the boundary conditions, inside
+    the step and again at the filter cadence (_apply_physical_filters)."""
+
+    def __init__(self, n: int, length: float = 1.0, gamma: float = 1.4, filter_params: Optional[dict] = None,
+                 cfl: float = 0.4, bc="wall", gravity: Optional[float] = None, scheme: str = "rk4"):
+        self.ax = LGLAxis(n, length)
+        self.gamma, self.cfl, self.gravity, self.scheme = gamma, cfl, gravity, scheme
+        fp = filter_params or {}
+        self.filter = bool(fp.get("enabled", False))
+        self.F = self.ax.nodal_filter(int(fp.get("p", 8)), float(fp.get("alpha", 36.0))) if self.filter else None
+        self.interval = max(1, int(fp.get("interval", 1) or 1))
+        self.codes = bc_codes_1d(bc)
+        self.step_counter = 0
+
+    def rhs(self, U: np.ndarray) -> np.ndarray:
+        apply_bc_1d(U, self.codes)
+        rho, vel, p = primitive(U, self.gamma)
+        u = vel[0]
+        F = np.array([rho * u, rho * u * u + p, (U[2] + p) * u])
+        r = -(F @ self.ax.D.T)
+        if self.gravity is not None:
+            r[1] += rho * self.gravity
+            r[2] += rho * self.gravity * u
+        return r
+
+    def clamp(self, U):
+        return positivity_clamp(U, self.gamma, 1e-10, 1e-12)
+
+    def filt(self, U):
+        if self.filter:
+            U = U @ self.F.T
+        return apply_bc_1d(U, self.codes)
+
+    def step(self, U: np.ndarray, dt: float) -> np.ndarray:
+        k1 = self.rhs(U)
+        if self.scheme == "rk2":
+            U1 = self.clamp(U + dt * 0.5 * k1)
+            Un = self.clamp(U + dt * self.rhs(U1))
+        else:
+            U2 = self.clamp(U + 0.5 * dt * k1)
+            k2 = self.rhs(U2)
+            U3 = self.clamp(U + 0.5 * dt * k2)
+            k3 = self.rhs(U3)
+            U4 = self.clamp(U + dt * k3)
+            k4 = self.rhs(U4)
+            Un = self.clamp(U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4))
+        Un = self.filt(Un)  # inside the step
+        if self.step_counter % self.interval == 0:
+            Un = self.filt(Un)  # cadence
+        self.step_counter += 1
+        return Un
+
+    def compute_dt(self, U: np.ndarray) -> float:
+        rho, vel, p = primitive(U, self.gamma)
+        s = float(np.max(np.abs(vel[0]) + np.sqrt(self.gamma * p / rho)))
+        if s <= 0.0:
+            return 1e-6
+        return self.cfl * float(np.min(np.diff(self.ax.x))) / s

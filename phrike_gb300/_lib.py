@@ -64,6 +64,7 @@ class PlanDesc(C.Structure):
         ("av_weight", C.c_double * 5),
         ("scheme", C.c_int),
         ("mhd_cfl_diff", C.c_double),
+        ("lgl_bc1d", C.c_int * 6),
     ]
 
 

@@ -1,0 +1,280 @@
+// 1D Legendre-Gauss-Lobatto (LGL) collocation: whole RK steps of the Euler
+// equations in one launch, one CTA per solve (SpectralSolver1D on a Grid1D
+// with basis "legendre": solver.py:62-132, 259-269; grid.py:276-300,
+// 620-735; basis/legendre.py:681-859).
+//
+// Per stage: the boundary conditions in place on the stage input (codes per
+// boundary and variable: copy the neighbouring interior value, set to zero,
+// or leave), the flux in shared memory, k = -D F with the differentiation
+// matrix read column by column from L2 (D^T, coalesced across the CTA's
+// threads), constant gravity, the RK update and the 1D positivity clamp.
+// After the step: the nodal filter (if enabled) with the boundary conditions,
+// inside the step and again at the filter cadence.  The energy slot holds
+// E' = E - E_ref (the energy of the first node), an exact rewrite that keeps
+// float32 rounding relative to the field's variation.
+#include <cuda_runtime.h>
+
+#include "lgl1d.cuh"
+#include "pass_common.cuh"
+
+namespace ps {
+
+namespace {
+
+__device__ __forceinline__ void bc_apply(float* u, int N, const int* codes, int i) {
+  // codes[side * 3 + var]; thread i handles (side, var) = (i / 3, i % 3)
+  if (i >= 6) return;
+  const int side = i / 3, var = i % 3;
+  const int c = codes[i];
+  const int dst = side == 0 ? 0 : N - 1, src = side == 0 ? 1 : N - 2;
+  if (c == 0) u[var * N + dst] = u[var * N + src];
+  else if (c == 1) u[var * N + dst] = 0.0f;
+}
+
+template <typename REAL>
+__global__ void __launch_bounds__(256) k_lgl1d(Lgl1DArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = a.n;
+  const int sol = blockIdx.x;
+  if (a.active != nullptr && !a.active[sol]) return;
+  REAL* F = reinterpret_cast<REAL*>(smem_raw);          // [3][N]
+  float* us = reinterpret_cast<float*>(F + 3 * N);       // [3][N]
+  float* un = us + 3 * N;                                 // [3][N]
+  float* acc = un + 3 * N;                                // [3][N]
+  __shared__ float red[32];
+  __shared__ int codes[6];
+  const REAL* DT = static_cast<const REAL*>(a.DT);
+  const REAL* FT = static_cast<const REAL*>(a.FT);
+  float* U = a.U + (long)sol * a.solve_stride;
+  if (threadIdx.x < 6) codes[threadIdx.x] = a.bc.c[threadIdx.x];
+  const float er = U[2 * N];
+  for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+    float v = U[i];
+    if (i >= 2 * N) v -= er;
+    un[i] = v;
+    us[i] = v;
+  }
+  __syncthreads();
+  const float g1 = a.gamma - 1.0f;
+  const float href = a.gamma * er;
+  const float pmin_shift = a.p_min - g1 * er;
+
+  // k = -D F(us) (+ gravity) for the node i, after flux() and a barrier
+  auto flux = [&]() {
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const float rho = us[j], m = us[N + j], E = us[2 * N + j];
+      const float u = m / rho;
+      const float p = g1 * (E - 0.5f * rho * u * u);  // p' (E holds E')
+      F[j] = (REAL)m;
+      F[N + j] = (REAL)(m * u + p);
+      F[2 * N + j] = (REAL)(((E + p) + href) * u);
+    }
+  };
+  // (D F)_i = sum_j D_ij (F_j - F_i): D annihilates constants, and the large
+  // entries of D (near the diagonal at the ends, O(N^2)) then multiply small
+  // differences, so the rounding of D and F stays relative to F's variation
+  auto deriv = [&](int i, float (&k)[3]) {
+    REAL s0 = 0, s1 = 0, s2 = 0;
+    const REAL f0 = F[i], f1 = F[N + i], f2 = F[2 * N + i];
+    for (int j = 0; j < N; ++j) {
+      const REAL d = DT[(long)j * N + i];
+      s0 += d * (F[j] - f0);
+      s1 += d * (F[N + j] - f1);
+      s2 += d * (F[2 * N + j] - f2);
+    }
+    k[0] = -(float)s0;
+    k[1] = -(float)s1;
+    k[2] = -(float)s2;
+    if (a.gx != 0.0f) {  // gravity source (solver.py:82-91)
+      const float rho = us[i], u = us[N + i] / rho;
+      k[1] += rho * a.gx;
+      k[2] += rho * a.gx * u;
+    }
+  };
+  // nodal filter of us (if enabled) and the boundary conditions; the filter
+  // keeps constants (rows sum to 1), so it is summed as
+  // u_i + sum_j F_ij (u_j - u_i) with rounding relative to the variation
+  auto filter_bc = [&]() {
+    if (FT != nullptr) {
+      for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) F[i] = (REAL)us[i];
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        REAL s0 = 0, s1 = 0, s2 = 0;
+        const REAL f0 = F[i], f1 = F[N + i], f2 = F[2 * N + i];
+        for (int j = 0; j < N; ++j) {
+          const REAL f = FT[(long)j * N + i];
+          s0 += f * (F[j] - f0);
+          s1 += f * (F[N + j] - f1);
+          s2 += f * (F[2 * N + j] - f2);
+        }
+        us[i] = (float)(f0 + s0);
+        us[N + i] = (float)(f1 + s1);
+        us[2 * N + i] = (float)(f2 + s2);
+      }
+      __syncthreads();
+    }
+    bc_apply(us, N, codes, threadIdx.x);
+    __syncthreads();
+  };
+
+  if (a.rhs_out != nullptr) {  // rhs only (the boundary conditions act on the copy in shared memory)
+    bc_apply(us, N, codes, threadIdx.x);
+    __syncthreads();
+    flux();
+    __syncthreads();
+    float* R = a.rhs_out + (long)sol * a.solve_stride;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      float k[3];
+      deriv(i, k);
+      R[i] = k[0];
+      R[N + i] = k[1];
+      R[2 * N + i] = k[2];
+    }
+    return;
+  }
+
+  float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
+  double tl = (a.t != nullptr) ? a.t[sol] : 0.0;
+  const double te = (a.tend != nullptr) ? a.tend[sol] : 0.0;
+  int taken = 0;
+  const int cad0 = (a.steps_done != nullptr) ? a.steps_done[sol] : a.step_counter0;
+#pragma unroll 1
+  for (int step = 0; step < a.nsteps; ++step) {
+    double dtd = dt;
+    if (a.t != nullptr) {  // CFL step size from the state as given (solver.py:235-240)
+      if (tl >= te - 1e-12) break;
+      float sm = 0.0f;
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float rho = un[i], u = un[N + i] / rho;
+        const float pp = g1 * (un[2 * N + i] - 0.5f * rho * u * u) + g1 * er;
+        sm = fmaxf(sm, fabsf(u) + sqrtf(a.gamma * pp / rho));
+      }
+      sm = block_max(sm, red);
+      if (threadIdx.x == 0) red[0] = sm;
+      __syncthreads();
+      const double spd = (double)red[0];
+      __syncthreads();
+      dtd = (spd <= 0.0) ? 1e-6 : (double)a.cfl * (double)a.hmin / spd;
+      dtd = fmin(dtd, te - tl);
+      dt = (float)dtd;
+    }
+#pragma unroll 1
+    for (int stage = 0; stage < 4; ++stage) {
+      if (a.rk2 && (stage == 1 || stage == 2)) continue;
+      const RKCoef rc = rk_coef(stage, dt, a.rk2);
+      // the boundary conditions act on the stage input (and so on U^n at stage 0)
+      bc_apply(us, N, codes, threadIdx.x);
+      __syncthreads();
+      if (stage == 0) {
+        for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) un[i] = us[i];
+        __syncthreads();
+      }
+      flux();
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        float k[3];
+        deriv(i, k);
+        float u3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int s = c * N + i;
+          if (stage == 3) {
+            u3[c] = fmaf(rc.wacc, k[c], acc[s]);
+          } else {
+            const float v = un[s];
+            acc[s] = fmaf(rc.wacc, k[c], (stage == 0) ? v : acc[s]);
+            u3[c] = fmaf(rc.wnext, k[c], v);
+          }
+        }
+        clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
+        us[i] = u3[0];
+        us[N + i] = u3[1];
+        us[2 * N + i] = u3[2];
+      }
+      __syncthreads();
+    }
+    filter_bc();  // inside the step (_rk4_step -> _apply_physical_filters)
+    if (((cad0 + step) % a.filter_interval) == 0) filter_bc();  // cadence
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) un[i] = us[i];
+    __syncthreads();
+    tl += dtd;
+    ++taken;
+  }
+  if (threadIdx.x == 0) {
+    if (a.t != nullptr) a.t[sol] = tl;
+    if (a.steps_done != nullptr) a.steps_done[sol] += taken;
+  }
+  for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) U[i] = un[i] + (i >= 2 * N ? er : 0.0f);
+}
+
+// out[f][i] = sum_j M[i][j] in[f][j] for nf fields per solve (MT = M^T),
+// summed as sum_j M[i][j] (in[f][j] - in[f][i]) + c in[f][i] with c the row
+// sum of M (0 for D, 1 for the filter) so rounding follows the variation
+template <typename REAL>
+__global__ void k_lgl1d_apply(const REAL* MT, const float* in, float* out, int n, int nf, long ss, float rowsum) {
+  const int f = blockIdx.y % nf, sol = blockIdx.y / nf;
+  const float* x = in + (long)sol * ss + (long)f * n;
+  float* y = out + (long)sol * ss + (long)f * n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const REAL xi = (REAL)x[i];
+    REAL s = 0;
+    for (int j = 0; j < n; ++j) s += MT[(long)j * n + i] * ((REAL)x[j] - xi);
+    y[i] = (float)(s + (REAL)rowsum * xi);
+  }
+}
+
+template <typename REAL>
+__global__ void k_transpose(const REAL* in, REAL* out, int n) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x) {
+    const long i = e / n, j = e % n;
+    out[j * n + i] = in[e];
+  }
+}
+
+__global__ void k_lgl1d_bc(float* U, int n, long ss, Bc1D bc, const int* active) {
+  if (active != nullptr && !active[blockIdx.x]) return;
+  bc_apply(U + (long)blockIdx.x * ss, n, bc.c, threadIdx.x);
+}
+
+}  // namespace
+
+size_t lgl1d_smem(int n, bool fp64) { return (size_t)3 * n * (fp64 ? 8 : 4) + (size_t)9 * n * 4; }
+
+cudaError_t launch_lgl1d(const Lgl1DArgs& a, bool fp64, int nsolve, cudaStream_t s) {
+  const size_t sm = lgl1d_smem(a.n, fp64);
+  cudaError_t e;
+  if (fp64) {
+    if ((e = cudaFuncSetAttribute(k_lgl1d<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+      return e;
+    k_lgl1d<double><<<nsolve, 256, sm, s>>>(a);
+  } else {
+    if ((e = cudaFuncSetAttribute(k_lgl1d<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+      return e;
+    k_lgl1d<float><<<nsolve, 256, sm, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lgl1d_apply(const void* MT, bool fp64, const float* in, float* out, int n, int nf, int nsolve,
+                               long ss, float rowsum, cudaStream_t s) {
+  const dim3 grid((n + 255) / 256, nf * nsolve);
+  if (fp64) k_lgl1d_apply<double><<<grid, 256, 0, s>>>(static_cast<const double*>(MT), in, out, n, nf, ss, rowsum);
+  else k_lgl1d_apply<float><<<grid, 256, 0, s>>>(static_cast<const float*>(MT), in, out, n, nf, ss, rowsum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const void* in, void* out, int n, bool fp64, cudaStream_t s) {
+  const long total = (long)n * n;
+  const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  if (fp64) k_transpose<double><<<blocks, 256, 0, s>>>(static_cast<const double*>(in), static_cast<double*>(out), n);
+  else k_transpose<float><<<blocks, 256, 0, s>>>(static_cast<const float*>(in), static_cast<float*>(out), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lgl1d_bc(float* U, int n, long ss, int nsolve, const Bc1D& bc, const int* active,
+                            cudaStream_t s) {
+  k_lgl1d_bc<<<nsolve, 32, 0, s>>>(U, n, ss, bc, active);
+  return cudaGetLastError();
+}
+
+}  // namespace ps

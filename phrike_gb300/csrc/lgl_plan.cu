@@ -15,6 +15,7 @@
 
 #include "lgl.cuh"
 #include "lgl_tc.cuh"
+#include "lgl1d.cuh"
 #include "plan.cuh"
 #include "reduce.cuh"
 
@@ -249,7 +250,21 @@ int filter_state(ps_plan p, float* U, const int* act, cudaStream_t s) {
 }  // namespace
 
 int lgl_validate(const ps_plan_desc* d) {
-  if (d->ndim != 2) return errorf(PS_ERR_UNSUPPORTED, "the Legendre basis is supported on 2D grids only");
+  if (d->ndim == 1) {  // Grid1D(basis="legendre") with SpectralSolver1D
+    if (d->equations != PS_EQ_EULER) return errorf(PS_ERR_UNSUPPORTED, "1D Legendre grids carry the Euler equations");
+    if (d->n[0] < 3 || d->n[0] > 2048) return errorf(PS_ERR_UNSUPPORTED, "1D LGL grids need 3..2048 nodes");
+    if (!(d->length[0] > 0.0)) return errorf(PS_ERR_INVALID, "length must be positive");
+    if (!(d->gamma > 1.0)) return errorf(PS_ERR_INVALID, "gamma must exceed 1");
+    if (d->filter_interval < 1) return errorf(PS_ERR_INVALID, "filter_interval must be >= 1");
+    if (d->av_mode != PS_AV_OFF)
+      return errorf(PS_ERR_UNSUPPORTED, "artificial viscosity is not implemented for LGL grids");
+    if (d->gemm_precision != PS_GEMM_FP32 && d->gemm_precision != PS_GEMM_FP64)
+      return errorf(PS_ERR_UNSUPPORTED, "1D LGL contractions run in float32 or float64");
+    for (int i = 0; i < 6; ++i)
+      if (d->lgl_bc1d[i] < 0 || d->lgl_bc1d[i] > 2) return errorf(PS_ERR_INVALID, "boundary codes are 0, 1 or 2");
+    return PS_OK;
+  }
+  if (d->ndim != 2) return errorf(PS_ERR_UNSUPPORTED, "the Legendre basis is supported on 1D and 2D grids only");
   if (d->basis[0] != PS_BASIS_LEGENDRE || d->basis[1] != PS_BASIS_LEGENDRE)
     return errorf(PS_ERR_UNSUPPORTED, "mixed Fourier x Legendre grids are not supported (LGL on both axes only)");
   if (d->equations != PS_EQ_EULER) return errorf(PS_ERR_UNSUPPORTED, "equation set %d not supported", d->equations);
@@ -270,6 +285,10 @@ int lgl_validate(const ps_plan_desc* d) {
 
 size_t lgl_scratch_bytes(const ps_plan_desc* d, int nsolve) {
   size_t b = 0;
+  if (d->ndim == 1) {
+    const size_t n = (size_t)d->n[0];
+    return 16 * n + 20 * n * n + (d->filter_enabled ? 20 * n * n : 0);  // D, F (float64, float32, transposed)
+  }
   for (int a = 0; a < 2; ++a) {
     const size_t n = (size_t)d->n[a];
     b += 16 * n + 12 * n * n;                 // nodes, weights, D in float64 and float32
@@ -288,7 +307,7 @@ int lgl_setup(ps_plan p) {
   p->lgl = true;
   p->gemm = p->desc.gemm_precision;
   double hmin = 1e300;
-  for (int a = 0; a < 2; ++a) {
+  for (int a = 0; a < p->nd; ++a) {
     const int n = p->n[a];
     if ((rc = plan_alloc(p, &p->lgl_x[a], n)) != PS_OK) return rc;
     if ((rc = plan_alloc(p, &p->lgl_w[a], n)) != PS_OK) return rc;
@@ -308,6 +327,24 @@ int lgl_setup(ps_plan p) {
     for (int j = 0; j + 1 < n; ++j) hmin = fmin(hmin, x[j + 1] - x[j]);  // grid.py:826-832
   }
   p->lgl_hmin = hmin;
+  if (p->nd == 1) {  // transposed matrices for the column-by-column contractions of k_lgl1d
+    const int n = p->n[0];
+    const bool fp64 = p->gemm == PS_GEMM_FP64;
+    const size_t esz = fp64 ? sizeof(double) : sizeof(float);
+    unsigned char* dt = nullptr;
+    if ((rc = plan_alloc(p, &dt, esz * n * n)) != PS_OK) return rc;
+    LGL_CU(launch_transpose(fp64 ? (const void*)p->D64[0] : (const void*)p->D32[0], dt, n, fp64, 0), "D transpose");
+    p->lgl_DT = dt;
+    if (p->desc.filter_enabled) {
+      unsigned char* ft = nullptr;
+      if ((rc = plan_alloc(p, &ft, esz * n * n)) != PS_OK) return rc;
+      LGL_CU(launch_transpose(fp64 ? (const void*)p->F64[0] : (const void*)p->F32[0], ft, n, fp64, 0),
+             "filter transpose");
+      p->lgl_FT = ft;
+    }
+    LGL_CU(cudaDeviceSynchronize(), "1D LGL tables");
+    return PS_OK;
+  }
   if (p->gemm == PS_GEMM_BF16X3) {
     const int nx = p->n[0], ny = p->n[1];
     p->pitch[0] = (nx + 7) / 8 * 8;
@@ -344,7 +381,59 @@ int lgl_setup(ps_plan p) {
   return PS_OK;
 }
 
+// 1D: whole steps (or the right-hand side) in k_lgl1d
+int lgl1d_run(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+              float* rhs_out, cudaStream_t s) {
+  Lgl1DArgs a{};
+  a.U = U;
+  a.solve_stride = p->ss(3);
+  a.n = p->n[0];
+  a.DT = p->lgl_DT;
+  a.FT = p->lgl_FT;
+  for (int i = 0; i < 6; ++i) a.bc.c[i] = p->desc.lgl_bc1d[i];
+  a.nsteps = nsteps;
+  a.dt_dev = d_dt;
+  a.dt = dt;
+  a.gamma = (float)p->desc.gamma;
+  a.rho_min = 1e-10f;  // 1D clamp floors (solver.py:32-59)
+  a.p_min = 1e-12f;
+  a.gx = (float)p->desc.gravity[0];
+  a.filter_interval = p->desc.filter_interval;
+  a.step_counter0 = (int)(p->step_counter % p->desc.filter_interval);
+  a.t = d_t;
+  a.tend = d_tend;
+  a.cfl = (float)p->desc.cfl;
+  a.hmin = (float)p->lgl_hmin;
+  a.steps_done = (d_t != nullptr) ? p->steps_done : nullptr;
+  a.rhs_out = rhs_out;
+  a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+  ProfScope prof(p, s, PS_KIND_STEP1D, 4.0 * p->cells * p->nsolve * 3 * 2);
+  LGL_CU(launch_lgl1d(a, p->gemm == PS_GEMM_FP64, p->nsolve, s), "1D LGL kernel");
+  if (rhs_out == nullptr && d_t == nullptr) p->step_counter += nsteps;
+  return PS_OK;
+}
+
+// out = M f for nf fields (M^T given), through the 3-field scratch when in place
+int lgl1d_apply(ps_plan p, const void* MT, float rowsum, const float* f, float* out, int nf, cudaStream_t s) {
+  const bool fp64 = p->gemm == PS_GEMM_FP64;
+  const int n = p->n[0];
+  if (f != out) {
+    LGL_CU(launch_lgl1d_apply(MT, fp64, f, out, n, nf, p->nsolve, (long)nf * n, rowsum, s), "1D LGL contraction");
+    return PS_OK;
+  }
+  for (int f0 = 0; f0 < nf; ++f0) {  // field by field through F1 (one field of every solve)
+    for (int z = 0; z < p->nsolve; ++z) {
+      const float* src = f + ((long)z * nf + f0) * n;
+      LGL_CU(launch_lgl1d_apply(MT, fp64, src, p->F1, n, 1, 1, n, rowsum, s), "1D LGL contraction");
+      LGL_CU(cudaMemcpyAsync(out + ((long)z * nf + f0) * n, p->F1, sizeof(float) * n, cudaMemcpyDeviceToDevice, s),
+             "contraction copy");
+    }
+  }
+  return PS_OK;
+}
+
 int lgl_rhs(ps_plan p, const float* U, float* rhs, cudaStream_t s) {
+  if (p->nd == 1) return lgl1d_run(p, const_cast<float*>(U), 0, 0.0, nullptr, nullptr, nullptr, rhs, s);
   // the reference applies the walls to U in place before the fluxes; here to
   // a copy, so U is left as given
   const size_t bytes = sizeof(float) * p->ss(4) * p->nsolve;
@@ -358,6 +447,7 @@ int lgl_rhs(ps_plan p, const float* U, float* rhs, cudaStream_t s) {
 int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
               cudaStream_t s) {
   int rc;
+  if (p->nd == 1) return lgl1d_run(p, U, nsteps, dt, d_dt, d_t, d_tend, nullptr, s);
   const bool cfl = d_t != nullptr;
   const int* act = cfl ? p->active : nullptr;
   const double* dtp = cfl ? p->dt : d_dt;
@@ -394,6 +484,7 @@ int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
 }
 
 int lgl_derivative(ps_plan p, int axis, const float* f, float* out, int nf, cudaStream_t s) {
+  if (p->nd == 1) return lgl1d_apply(p, p->lgl_DT, 0.0f, f, out, nf, s);
   const long Z = (long)nf * p->nsolve;
   if (f != out) return contract(p, axis, false, f, out, Z, nullptr, 1, s);
   // in place: through the scratch G (8 nsolve fields) in chunks
@@ -417,6 +508,7 @@ int lgl_filter(ps_plan p, const float* f, float* out, int nf, cudaStream_t s) {
              "filter copy");
     return PS_OK;
   }
+  if (p->nd == 1) return lgl1d_apply(p, p->lgl_FT, 1.0f, f, out, nf, s);
   const long Z = (long)nf * p->nsolve;
   const long cap = 8L * p->nsolve;
   int rc;

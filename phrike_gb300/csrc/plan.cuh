@@ -66,6 +66,8 @@ struct ps_plan_s {
   double* F64[2] = {nullptr, nullptr};    // nodal filter matrices (filter on)
   float* F32[2] = {nullptr, nullptr};
   double lgl_hmin = 0.0;                  // smallest node spacing (CFL)
+  void* lgl_DT = nullptr;                 // 1D: D^T and the nodal filter transposed (float or double)
+  void* lgl_FT = nullptr;
   // artificial viscosity (1D in the step kernel; 2D through av_buf, 21 fields per solve)
   ps::AVParams av{};
   float* av_buf = nullptr;

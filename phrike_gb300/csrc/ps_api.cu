@@ -17,6 +17,7 @@
 #include "av.cuh"
 #include "launch.cuh"
 #include "lgl.cuh"
+#include "lgl1d.cuh"
 #include "plan.cuh"
 #include "reduce.cuh"
 
@@ -1003,6 +1004,8 @@ int ps_plan_desc_init(ps_plan_desc* d, int ndim) {
   d->mhd_rho_min = 1e-10;
   d->mhd_p_min = 1e-12;
   d->mhd_cfl_diff = 1.0;
+  const int walls[6] = {0, 1, 0, 0, 1, 0};  // density copy, momentum zero, energy copy
+  for (int i = 0; i < 6; ++i) d->lgl_bc1d[i] = walls[i];
   d->mhd_project_substages = 1;
   d->mhd_divergence_clean = 1;
   return PS_OK;
@@ -1222,6 +1225,13 @@ int ps_lgl_build(int n, double length, double* d_nodes, double* d_weights, doubl
 int ps_apply_boundary_conditions(ps_plan p, float* U, void* stream) {
   if (!p || !U) return fail(PS_ERR_INVALID, "null argument");
   if (!p->lgl) return PS_OK;  // periodic Fourier grids have none
+  if (p->nd == 1) {
+    ps::Bc1D bc;
+    for (int i = 0; i < 6; ++i) bc.c[i] = p->desc.lgl_bc1d[i];
+    PS_CU(ps::launch_lgl1d_bc(U, p->n[0], p->ss(3), p->nsolve, bc, nullptr, (cudaStream_t)stream),
+          "1D boundary conditions");
+    return PS_OK;
+  }
   PS_CU(ps::launch_lgl_bc(U, p->n[0], p->n[1], p->ss(4), p->nsolve, nullptr, (cudaStream_t)stream), "LGL walls");
   return PS_OK;
 }

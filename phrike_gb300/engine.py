@@ -53,7 +53,7 @@ class Plan:
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
                  gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None,
-                 av_config: Optional[Dict] = None, scheme: str = "rk4"):
+                 av_config: Optional[Dict] = None, scheme: str = "rk4", lgl_bc1d: Optional[Sequence[int]] = None):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -117,6 +117,9 @@ class Plan:
             wts = av_config.get("variable_weights", None) or {}
             for c in range(5):
                 desc.av_weight[c] = float(wts.get(names[c], 1.0))
+        if lgl_bc1d is not None:  # 1D Legendre boundary codes (ps_plan_desc.lgl_bc1d)
+            for i, c in enumerate(lgl_bc1d):
+                desc.lgl_bc1d[i] = int(c)
         scheme = str(scheme).lower()
         if scheme not in ("rk4", "rk2"):
             raise ValueError(f"fixed-step scheme must be 'rk4' or 'rk2' (got {scheme!r})")

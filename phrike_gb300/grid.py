@@ -46,6 +46,63 @@ def _check_backend(backend: str, basis: str = "fourier") -> None:
         raise ValueError(f"Unknown or unsupported basis for the gb300 Fourier grids: {basis!r}")
 
 
+def _bc_codes_1d(bc: Any) -> list:
+    """Boundary codes of a 1D Legendre grid, [side (left, right)] x [variable
+    (density, momentum, energy)] flattened: 0 copy the neighbouring interior
+    value, 1 zero, 2 leave.  Resolves a string, a per-variable or a
+    per-boundary dict like Grid1D (grid.py:184-246, 620-735): "wall" (aliases
+    reflective, dirichlet) zeroes the momentum and copies density and energy;
+    "neumann" (alias open) copies every variable."""
+    def norm_bc(v):
+        n = str(v).strip().lower()
+        return "wall" if n in ("reflective", "dirichlet", "wall") else "neumann" if n in ("neumann", "open") else n
+
+    def norm_var(v):
+        n = str(v).strip().lower()
+        return {"rho": "density", "density": "density", "p": "pressure", "pressure": "pressure", "u": "momentum",
+                "velocity": "momentum", "mom": "momentum", "momentum": "momentum",
+                "momentum_x": "momentum"}.get(n, n)
+
+    def norm_side(b):
+        n = str(b).strip().lower()
+        return "left" if n in ("left", "x0", "x_min", "start") else "right" if n in ("right", "x1", "x_max", "end") \
+            else n
+
+    glob, var_map, side_map = None, None, None
+    if isinstance(bc, dict):
+        if any(str(k).lower() in ("left", "right", "x0", "x1", "x_min", "x_max", "start", "end") for k in bc):
+            side_map = {}
+            for bk, vd in bc.items():
+                if isinstance(vd, dict):
+                    side_map[norm_side(bk)] = {norm_var(k): norm_bc(v) for k, v in vd.items()}
+                else:
+                    side_map[norm_side(bk)] = {v: norm_bc(vd) for v in ("density", "momentum", "pressure")}
+        else:
+            var_map = {norm_var(k): norm_bc(v) for k, v in bc.items()}
+    elif isinstance(bc, str) and bc:
+        glob = norm_bc(bc)
+
+    def get(var, side):
+        if side_map is not None and side in side_map:
+            return side_map[side].get(var, glob or "wall")
+        if var_map is not None:
+            return var_map.get(var, glob or "wall")
+        g = glob or "wall"
+        if g == "wall":
+            return "wall" if var == "momentum" else "neumann"
+        return g
+
+    codes = []
+    for side in ("left", "right"):
+        for var in ("density", "momentum", "pressure"):
+            b = get(var, side)
+            if var == "momentum":
+                codes.append(1 if b in ("wall", "reflective") else 0 if b in ("neumann", "open") else 2)
+            else:
+                codes.append(0 if b in ("neumann", "open", "wall") else 2)
+    return codes
+
+
 def _is_lgl2d(basis_x: str, basis_y: str) -> bool:
     bx, by = str(basis_x).lower(), str(basis_y).lower()
     if bx == "legendre" and by == "legendre":
@@ -89,7 +146,7 @@ class _FourierGridBase:
         if g not in self._plans:
             self._plans[g] = Plan(self._shape, self._lengths, gamma=g, dealias=self.dealias,
                                   filter_params=self.filter_params, device=self.device, basis=self._basis,
-                                  gemm_precision=self.gemm_precision)
+                                  gemm_precision=self.gemm_precision, lgl_bc1d=getattr(self, "_bc_codes", None))
         return self._plans[g]
 
     def to_device(self, f: Any) -> torch.Tensor:
@@ -127,17 +184,34 @@ class _FourierGridBase:
 
 
 class Grid1D(_FourierGridBase):
-    """1D periodic Fourier grid (reference: phrike/grid.py:144-735)."""
+    """1D grid: periodic Fourier, or Legendre-Gauss-Lobatto nodes with boundary
+    conditions (reference: phrike/grid.py:144-735)."""
 
-    def __init__(self, N: int, Lx: float, basis: str = "fourier", bc: Optional[str] = None,
+    def __init__(self, N: int, Lx: float, basis: str = "fourier", bc: Optional[Any] = None,
                  dealias: bool = True, filter_params: Optional[Dict[str, float]] = None, fft_workers: int = 1,
                  backend: str = "gb300", torch_device: Optional[str] = None, precision: str = "single",
-                 debug: bool = False, problem_config: Optional[Dict[str, Any]] = None):
-        _check_backend(backend, basis)
+                 debug: bool = False, problem_config: Optional[Dict[str, Any]] = None, gemm_precision: str = "fp32"):
         self.N, self.Lx, self.basis, self.bc = int(N), float(Lx), basis, bc
         self.fft_workers, self.backend, self.debug, self.problem_config = fft_workers, backend, debug, problem_config
         self._shape = (self.N,)
         self._lengths = (self.Lx,)
+        self.mhd_config: Optional[Dict[str, Any]] = None  # set by MHD problems (grid.mhd_config)
+        if str(basis).lower() == "legendre":
+            # LGL nodes on [0, Lx] (grid.py:276-300, basis/legendre.py:681-729); no
+            # Fourier masks; bc as in apply_boundary_conditions (grid.py:620-735)
+            if str(backend).lower() != "gb300":
+                raise ValueError(f"phrike_gb300 grids implement backend 'gb300' only (got {backend!r})")
+            self._basis = "legendre"
+            self.gemm_precision = str(gemm_precision).lower()
+            self._bc_codes = _bc_codes_1d(bc if bc is not None else "dirichlet")
+            self._init_plan(dealias, filter_params, torch_device, precision)
+            self.x, self.w, self.D = lgl_build(self.N, self.Lx, self.device)
+            self.dx = float(torch.min(torch.diff(self.x)).item())
+            self.dealias_mask = torch.ones(self.N, dtype=torch.float64, device=self.device)
+            self.filter_sigma = torch.ones(self.N, dtype=torch.float64, device=self.device)
+            self.k = self.ik = None
+            return
+        _check_backend(backend, basis)
         self.dx = self.Lx / self.N
         self._init_plan(dealias, filter_params, torch_device, precision)
         self.x = torch.linspace(0.0, self.Lx, self.N + 1, dtype=torch.float64)[:-1].to(self.device)
@@ -145,7 +219,6 @@ class Grid1D(_FourierGridBase):
         self.ik = 1j * self.k
         self.dealias_mask = torch.as_tensor(_mask_1d(self.N, dealias), device=self.device)
         self.filter_sigma = torch.as_tensor(_sigma_1d(self.N, filter_params), device=self.device)
-        self.mhd_config: Optional[Dict[str, Any]] = None  # set by MHD problems (grid.mhd_config)
 
     def dx1(self, f: Any) -> torch.Tensor:
         return self._op(f, 0)

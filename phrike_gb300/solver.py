@@ -73,7 +73,8 @@ class _SpectralSolverBase:
                          basis=getattr(grid, "_basis", "fourier"),
                          gemm_precision=getattr(grid, "gemm_precision", "fp32"), equations=self._equations,
                          mhd_config=getattr(grid, "mhd_config", None), av_config=av,
-                         scheme="rk2" if self.scheme == "rk2" else "rk4")
+                         scheme="rk2" if self.scheme == "rk2" else "rk4",
+                         lgl_bc1d=getattr(grid, "_bc_codes", None))
         self._ark = Plan.adaptive_desc(adaptive) if adaptive is not None else None
 
     # -- reference interface -----------------------------------------------

@@ -53,6 +53,8 @@ def main(ref_path: str, only: str = "") -> None:
         return mhd_diffusion_fixtures(grid, equations, solver, problems)
     if only == "mhd1d":
         return mhd1d_fixtures(grid, equations, solver, problems)
+    if only == "lgl1d":
+        return lgl1d_fixtures(grid, equations, solver, problems)
 
     out = {}
 
@@ -207,6 +209,36 @@ def source_fixtures(grid, equations, solver, problems) -> None:
         out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
                                                            None)
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+def lgl1d_fixtures(grid, equations, solver, problems) -> None:
+    """1D Legendre (LGL) grid with SpectralSolver1D: nodes, D, a Gaussian
+    density/pressure pulse with a velocity bump between walls; rhs, RK4 steps
+    with the nodal filter (cadence 2), a per-boundary/per-variable bc map
+    with RK2, gravity, and the CFL dt."""
+    out = {}
+    for tag, n, fp, bc, scheme, grav in (
+            ("wall", 33, {"enabled": True, "p": 8, "alpha": 36.0, "interval": 2}, None, "rk4", None),
+            ("mixed", 41, None, {"left": {"density": "neumann", "momentum": "wall", "pressure": "open"},
+                                 "right": "neumann"}, "rk2", -1.5)):
+        g = grid.Grid1D(N=n, Lx=2.0, basis="legendre", bc=bc, filter_params=fp)
+        x = np.asarray(g.x)
+        rho = 1.0 + 0.2 * np.exp(-((x - 0.8) ** 2) / 0.02)
+        p = rho ** 1.4 / 1.4
+        u = 0.1 * np.sin(np.pi * x / 2.0) ** 2
+        U0 = np.stack([rho, rho * u, p / 0.4 + 0.5 * rho * u * u])
+        gc = {"enabled": True, "gx": grav} if grav is not None else None
+        s = solver.SpectralSolver1D(g, equations.EulerEquations1D(gamma=1.4), scheme=scheme, cfl=0.4,
+                                    gravity_config=gc)
+        out[f"{tag}_x"] = x
+        out[f"{tag}_U0"] = U0
+        out[f"{tag}_rhs0"] = solver._compute_rhs(g, s.equations, U0.copy(), None, gc)
+        out[f"{tag}_dt0"] = s.compute_dt(U0)
+        U = U0.copy()
+        for _ in range(5):
+            U = s.step(U, 2e-4)
+        out[f"{tag}_U"] = U
+    np.savez_compressed(os.path.join(HERE, "lgl1d.npz"), **out)
+
 
 def mhd1d_fixtures(grid, equations, solver, problems) -> None:
     """1D MHD (SpectralSolverMHD1D): the circularly polarized Alfven wave with

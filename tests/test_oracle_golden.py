@@ -120,6 +120,51 @@ def test_lgl_oracle_matches_reference(nx, ny):
     assert abs(s.compute_dt(U0) - float(z["dt_cfl0"])) <= 1e-14 * float(z["dt_cfl0"])
 
 
+@pytest.mark.parametrize("tag", ["wall", "mixed"])
+def test_lgl1d_oracle_matches_reference(tag):
+    """1D Legendre grid: nodes, the rhs with the boundary codes applied first,
+    five steps (RK4 with the filter at cadence 2; RK2 with a per-boundary,
+    per-variable bc map and gravity) and the CFL dt against the reference."""
+    from lgl1d_cases import CASES, DT, LENGTH, NSTEPS, initial_state
+    from oracle import lgl as L
+    c = CASES[tag]
+    z = golden("lgl1d.npz")
+    s = L.LGLSolver1D(c["n"], LENGTH, gamma=1.4, filter_params=c["filter_params"], cfl=0.4,
+                      bc=c["bc"] if c["bc"] is not None else "dirichlet", gravity=c["gravity"], scheme=c["scheme"])
+    np.testing.assert_allclose(s.ax.x, z[f"{tag}_x"], rtol=0, atol=1e-14)
+    U0 = initial_state(s.ax.x)
+    np.testing.assert_allclose(U0, z[f"{tag}_U0"], rtol=0, atol=1e-14)
+    assert rel_l2(s.rhs(U0.copy()), z[f"{tag}_rhs0"]) < 1e-12
+    U = U0.copy()
+    for _ in range(NSTEPS):
+        U = s.step(U, DT)
+    for k in range(3):
+        assert rel_l2(U[k], z[f"{tag}_U"][k]) < 1e-13, k
+    assert abs(s.compute_dt(U0) - float(z[f"{tag}_dt0"])) <= 1e-13 * float(z[f"{tag}_dt0"])
+
+
+def test_lgl1d_bc_codes():
+    """Boundary resolution: walls zero the momentum and copy the rest; a
+    per-boundary map with a bare string applies to every variable."""
+    from oracle import lgl as L
+    np.testing.assert_array_equal(L.bc_codes_1d("dirichlet"), [[L.BC_COPY, L.BC_ZERO, L.BC_COPY]] * 2)
+    np.testing.assert_array_equal(L.bc_codes_1d("open"), [[L.BC_COPY] * 3] * 2)
+    np.testing.assert_array_equal(L.bc_codes_1d({"left": "wall", "right": {"rho": "neumann", "u": "periodic"}}),
+                                  [[L.BC_COPY, L.BC_ZERO, L.BC_COPY], [L.BC_COPY, L.BC_NONE, L.BC_COPY]])
+
+
+@pytest.mark.parametrize("bc", [None, "wall", "reflective", "neumann", "open", "periodic",
+                                {"density": "open", "momentum": "dirichlet"},
+                                {"x0": "open", "x_max": {"pressure": "periodic", "mom": "open"}}])
+def test_lgl1d_grid_bc_codes_match_oracle(bc):
+    """The grid's boundary resolver (host code handed to the plan descriptor)
+    agrees with the oracle's for every form of the configuration."""
+    from oracle import lgl as L
+    from phrike_gb300.grid import _bc_codes_1d
+    want = L.bc_codes_1d(bc if bc is not None else "dirichlet").reshape(-1).tolist()
+    assert _bc_codes_1d(bc if bc is not None else "dirichlet") == want
+
+
 def test_lgl_filter_preserves_low_modes():
     """The nodal filter keeps constants and linear functions (sigma_0 = 1,
     sigma_1 = exp(-alpha/(n-1)^p) ~ 1) and damps the top mode by e^-alpha."""
