@@ -688,7 +688,7 @@ def run_serving(args):
         "metric": "served solves/s and latency (continuous batching) vs plain one-at-a-time", "value":
         stats["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
         "data": "synthetic (seeded Poisson stream, analytic initial conditions)",
-        "config": {"workload": f"{args.requests} requests at 200/s: sod1d, khi2d, ot2d, tgv3d, lgl2d; "
+        "config": {"workload": f"{args.requests} requests at 200/s: sod1d, khi2d, ot2d, tgv3d, lgl2d, lgl1d; "
                                "t_end ~ U[0.1, 1.0]", "chunk_steps_per_graph": args.chunk},
         "latency_s": {"p50": stats["latency_p50"], "p95": stats["latency_p95"], "p99": stats["latency_p99"]},
         "seconds": stats["seconds"], "max_live_slots": stats["max_live_slots"], "groups": stats["groups"],

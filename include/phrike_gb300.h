@@ -261,6 +261,31 @@ int ps_project_solenoidal(ps_plan plan, float* Bx, float* By, void* stream);
  * recomputed with the thermal pressure held fixed. */
 int ps_project_state(ps_plan plan, float* U, void* stream);
 
+/* Spectral interpolation of Fourier fields at arbitrary points:
+ *   out[c][p] = Re( sum_k c_k F_k exp(i k . x_p) ) / N_total,  F = FFT(f_c),
+ * c_k the plan's dealias mask x filter, k = 2 pi fftfreq(N)/L per axis, i.e.
+ * the exact trigonometric interpolant the reference evaluates without finufft
+ * (and to its eps = 1e-6 with it).  f holds nf (1..3) fields of the plan's
+ * grid (solve 0), points is [ndim][npoints] float64 (x row, then y, z), out
+ * [nf][npoints] float32.  Cost O(npoints x cells).  Fourier plans only.
+ * Replaces Grid1D.evaluate_fourier_at_points_1d (grid.py:581-618),
+ * Grid2D.evaluate_fourier_at_points (grid.py:1180-1222) and the 3D single
+ * and batched forms (grid.py:1520-1632). */
+int ps_eval_points(ps_plan plan, const float* f, int nf, const double* points, int npoints, float* out,
+                   void* stream);
+
+/* One leap-frog step of tracer particles in the velocity u_a = U[1+a]/U[0]
+ * of the state U (solve 0), interpolated as in ps_eval_points:
+ *   first != 0: prev = pos; pos += dt u        (Euler start)
+ *   otherwise:  pos, prev = prev + 2 dt u, pos
+ * then pos = pos mod L per axis (numpy's rule, result in [0, L)).  pos and
+ * prev are [ndim][npoints] float64, updated in place; velocity_out
+ * ([ndim][npoints] float32) receives the interpolated velocity when not
+ * null.  Replaces FourierTracers1D/2D/3D.step (tracers.py:50-79, 103-148,
+ * 178-236). */
+int ps_tracers_step(ps_plan plan, const float* U, double* pos, double* prev, int npoints, int first, double dt,
+                    float* velocity_out, void* stream);
+
 /* Device status word of a plan, read synchronously: 0 = healthy; bit
  * PS_STATUS_TMA_TIMEOUT = a kernel gave up waiting for a tile load (bounded
  * wait) and its results are invalid.  No reference counterpart: the

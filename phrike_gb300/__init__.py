@@ -143,10 +143,14 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
         raise ValueError(f"unknown problem {problem_name!r} "
                          "(available: sod, tgv3d, khi2d, orszag_tang2d, alfven1d)")
     dt = integ.get("dt", None)
+    # tracer particles from the ``tracers`` block (problems/base.py:961-1021, 1082-1102)
+    from .tracers import tracers_from_config
+    tracers = tracers_from_config(grid, cfg.get("tracers", {}) or {})
     history = solver.run(U0, float(integ.get("t0", 0.0)), float(integ.get("t_end", 0.01)),
                          output_interval=float(integ.get("output_interval", 0.1)),
                          checkpoint_interval=float(integ.get("checkpoint_interval", 0.0)), outdir=outdir,
-                         dt=float(dt) if dt is not None else None)
+                         tracers=tracers, dt=float(dt) if dt is not None else None)
+    solver.tracers = tracers
     return solver, history
 
 
@@ -162,4 +166,7 @@ def __getattr__(name: str):
                 "SpectralSolverMHD2D"):
         from . import solver
         return getattr(solver, name)
+    if name in ("FourierTracers1D", "FourierTracers2D", "FourierTracers3D"):
+        from . import tracers
+        return getattr(tracers, name)
     raise AttributeError(name)

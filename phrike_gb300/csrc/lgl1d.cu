@@ -1,5 +1,5 @@
 // 1D Legendre-Gauss-Lobatto (LGL) collocation: whole RK steps of the Euler
-// equations in one launch, one CTA per solve (SpectralSolver1D on a Grid1D
+// equations in one launch, one CTA per solve (one thread per node up to 1024) (SpectralSolver1D on a Grid1D
 // with basis "legendre": solver.py:62-132, 259-269; grid.py:276-300,
 // 620-735; basis/legendre.py:681-859).
 //
@@ -31,14 +31,20 @@ __device__ __forceinline__ void bc_apply(float* u, int N, const int* codes, int 
   else if (c == 1) u[var * N + dst] = 0.0f;
 }
 
+// the three flux (or state) values of one node, one vector load per node
 template <typename REAL>
-__global__ void __launch_bounds__(256) k_lgl1d(Lgl1DArgs a) {
+struct alignas(4 * sizeof(REAL)) Node4 {
+  REAL v0, v1, v2, pad;
+};
+
+template <typename REAL>
+__global__ void __launch_bounds__(1024) k_lgl1d(Lgl1DArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = a.n;
   const int sol = blockIdx.x;
   if (a.active != nullptr && !a.active[sol]) return;
-  REAL* F = reinterpret_cast<REAL*>(smem_raw);          // [3][N]
-  float* us = reinterpret_cast<float*>(F + 3 * N);       // [3][N]
+  Node4<REAL>* F = reinterpret_cast<Node4<REAL>*>(smem_raw);  // [N] nodes x (3 + pad)
+  float* us = reinterpret_cast<float*>(F + N);           // [3][N]
   float* un = us + 3 * N;                                 // [3][N]
   float* acc = un + 3 * N;                                // [3][N]
   __shared__ float red[32];
@@ -65,9 +71,7 @@ __global__ void __launch_bounds__(256) k_lgl1d(Lgl1DArgs a) {
       const float rho = us[j], m = us[N + j], E = us[2 * N + j];
       const float u = m / rho;
       const float p = g1 * (E - 0.5f * rho * u * u);  // p' (E holds E')
-      F[j] = (REAL)m;
-      F[N + j] = (REAL)(m * u + p);
-      F[2 * N + j] = (REAL)(((E + p) + href) * u);
+      F[j] = Node4<REAL>{(REAL)m, (REAL)(m * u + p), (REAL)(((E + p) + href) * u), (REAL)0};
     }
   };
   // (D F)_i = sum_j D_ij (F_j - F_i): D annihilates constants, and the large
@@ -75,12 +79,14 @@ __global__ void __launch_bounds__(256) k_lgl1d(Lgl1DArgs a) {
   // differences, so the rounding of D and F stays relative to F's variation
   auto deriv = [&](int i, float (&k)[3]) {
     REAL s0 = 0, s1 = 0, s2 = 0;
-    const REAL f0 = F[i], f1 = F[N + i], f2 = F[2 * N + i];
+    const Node4<REAL> fi = F[i];
+#pragma unroll 4
     for (int j = 0; j < N; ++j) {
       const REAL d = DT[(long)j * N + i];
-      s0 += d * (F[j] - f0);
-      s1 += d * (F[N + j] - f1);
-      s2 += d * (F[2 * N + j] - f2);
+      const Node4<REAL> fj = F[j];
+      s0 += d * (fj.v0 - fi.v0);
+      s1 += d * (fj.v1 - fi.v1);
+      s2 += d * (fj.v2 - fi.v2);
     }
     k[0] = -(float)s0;
     k[1] = -(float)s1;
@@ -96,20 +102,23 @@ __global__ void __launch_bounds__(256) k_lgl1d(Lgl1DArgs a) {
   // u_i + sum_j F_ij (u_j - u_i) with rounding relative to the variation
   auto filter_bc = [&]() {
     if (FT != nullptr) {
-      for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) F[i] = (REAL)us[i];
+      for (int i = threadIdx.x; i < N; i += blockDim.x)
+        F[i] = Node4<REAL>{(REAL)us[i], (REAL)us[N + i], (REAL)us[2 * N + i], (REAL)0};
       __syncthreads();
       for (int i = threadIdx.x; i < N; i += blockDim.x) {
         REAL s0 = 0, s1 = 0, s2 = 0;
-        const REAL f0 = F[i], f1 = F[N + i], f2 = F[2 * N + i];
+        const Node4<REAL> fi = F[i];
+#pragma unroll 4
         for (int j = 0; j < N; ++j) {
           const REAL f = FT[(long)j * N + i];
-          s0 += f * (F[j] - f0);
-          s1 += f * (F[N + j] - f1);
-          s2 += f * (F[2 * N + j] - f2);
+          const Node4<REAL> fj = F[j];
+          s0 += f * (fj.v0 - fi.v0);
+          s1 += f * (fj.v1 - fi.v1);
+          s2 += f * (fj.v2 - fi.v2);
         }
-        us[i] = (float)(f0 + s0);
-        us[N + i] = (float)(f1 + s1);
-        us[2 * N + i] = (float)(f2 + s2);
+        us[i] = (float)(fi.v0 + s0);
+        us[N + i] = (float)(fi.v1 + s1);
+        us[2 * N + i] = (float)(fi.v2 + s2);
       }
       __syncthreads();
     }
@@ -238,7 +247,11 @@ __global__ void k_lgl1d_bc(float* U, int n, long ss, Bc1D bc, const int* active)
 
 }  // namespace
 
-size_t lgl1d_smem(int n, bool fp64) { return (size_t)3 * n * (fp64 ? 8 : 4) + (size_t)9 * n * 4; }
+size_t lgl1d_smem(int n, bool fp64) { return (size_t)4 * n * (fp64 ? 8 : 4) + (size_t)9 * n * 4; }
+
+// one thread per node up to 1024 (whole warps), so the contraction rows are
+// spread evenly and the column loads of D^T have many warps in flight
+static int lgl1d_threads(int n) { return n >= 1024 ? 1024 : ((n + 31) / 32) * 32; }
 
 cudaError_t launch_lgl1d(const Lgl1DArgs& a, bool fp64, int nsolve, cudaStream_t s) {
   const size_t sm = lgl1d_smem(a.n, fp64);
@@ -246,11 +259,11 @@ cudaError_t launch_lgl1d(const Lgl1DArgs& a, bool fp64, int nsolve, cudaStream_t
   if (fp64) {
     if ((e = cudaFuncSetAttribute(k_lgl1d<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
       return e;
-    k_lgl1d<double><<<nsolve, 256, sm, s>>>(a);
+    k_lgl1d<double><<<nsolve, lgl1d_threads(a.n), sm, s>>>(a);
   } else {
     if ((e = cudaFuncSetAttribute(k_lgl1d<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
       return e;
-    k_lgl1d<float><<<nsolve, 256, sm, s>>>(a);
+    k_lgl1d<float><<<nsolve, lgl1d_threads(a.n), sm, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -7,6 +7,7 @@ component-first, C-contiguous, shape (ncomp, [Nz,] [Ny,] Nx).
 from __future__ import annotations
 
 import ctypes as C
+import math
 from typing import Dict, Optional, Sequence
 
 import torch
@@ -284,6 +285,49 @@ class Plan:
         self._check_state(U)
         _lib.check(self._lib.ps_project_state(self._handle, _ptr(U), _stream(self.device)))
         return U
+
+    def _points(self, pts: torch.Tensor, n: Optional[int] = None) -> int:
+        if not (isinstance(pts, torch.Tensor) and pts.device == self.device and pts.dtype == torch.float64
+                and pts.is_contiguous() and pts.dim() == 2 and pts.shape[0] == self.ndim):
+            raise RuntimeError(f"points must be a contiguous float64 ({self.ndim}, P) tensor on {self.device}")
+        if n is not None and pts.shape[1] != n:
+            raise RuntimeError("position arrays differ in length")
+        return int(pts.shape[1])
+
+    def eval_points(self, f: torch.Tensor, points: torch.Tensor, out: Optional[torch.Tensor] = None
+                    ) -> torch.Tensor:
+        """Spectral interpolant of the fields f (nf, *shape) (nf <= 3, one
+        solve) at points (ndim, P) float64: out (nf, P) float32."""
+        if not (f.device == self.device and f.dtype == torch.float32 and f.is_contiguous()):
+            raise RuntimeError(f"expected contiguous float32 fields on {self.device}")
+        nf = f.numel() // math.prod(self.shape)
+        if f.numel() != nf * math.prod(self.shape) or not 1 <= nf <= 3:
+            raise RuntimeError(f"expected 1..3 fields of {self.shape}, got {tuple(f.shape)}")
+        npts = self._points(points)
+        if out is None:
+            out = torch.empty((nf, npts), dtype=torch.float32, device=self.device)
+        _lib.check(self._lib.ps_eval_points(self._handle, _ptr(f), nf, _ptr(points), npts, _ptr(out),
+                                            _stream(self.device)))
+        return out
+
+    def tracers_step_(self, U: torch.Tensor, pos: torch.Tensor, prev: torch.Tensor, first: bool, dt: float,
+                      velocity_out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """One leap-frog step of tracers in the velocity of U (solve 0):
+        pos and prev (ndim, P) float64 updated in place."""
+        if not (U.device == self.device and U.dtype == torch.float32 and U.is_contiguous()
+                and U.numel() >= self.ncomp * math.prod(self.shape)):
+            raise RuntimeError(f"expected a contiguous float32 state of {self.ncomp} x {self.shape}")
+        npts = self._points(pos)
+        self._points(prev, npts)
+        vp = 0
+        if velocity_out is not None:
+            if not (velocity_out.device == self.device and velocity_out.dtype == torch.float32
+                    and velocity_out.is_contiguous() and velocity_out.numel() == self.ndim * npts):
+                raise RuntimeError("velocity_out must be a contiguous float32 (ndim, P) tensor")
+            vp = _ptr(velocity_out)
+        _lib.check(self._lib.ps_tracers_step(self._handle, _ptr(U), _ptr(pos), _ptr(prev), npts, 1 if first else 0,
+                                             float(dt), vp, _stream(self.device)))
+        return pos
 
     def project_solenoidal_(self, Bx: torch.Tensor, By: torch.Tensor):
         """Helmholtz projection of (Bx, By) in place (one field per solve each)."""

@@ -168,6 +168,15 @@ class _FourierGridBase:
         shape = t.shape
         return self.plan.filter(t.reshape((-1,) + self._shape)).reshape(shape)
 
+    def _eval_points(self, fields: list, coords: list) -> torch.Tensor:
+        """Spectral interpolant (mask x filter) of 1..3 fields at points
+        (ps_eval_points); returns (len(fields), P) float32."""
+        if self._basis != "fourier":
+            raise ValueError("point evaluation requires a Fourier basis")
+        f = torch.stack([self.to_device(v).reshape(self._shape) for v in fields]).contiguous()
+        pts = torch.stack([torch.as_tensor(c, dtype=torch.float64).reshape(-1).to(self.device) for c in coords])
+        return self.plan.eval_points(f, pts.contiguous())
+
     def apply_boundary_conditions(self, U: Any, equations: Any = None) -> Any:
         """Periodic Fourier grids have no boundary conditions (grid.py:631-632,
         1087-1089); an LGL x LGL grid applies its solid walls in place to a
@@ -226,6 +235,11 @@ class Grid1D(_FourierGridBase):
     def divergence_x(self, Bx: Any) -> torch.Tensor:
         """d(Bx)/dx with the masked derivative (grid.py:550-552)."""
         return self.dx1(Bx)
+
+    def evaluate_fourier_at_points_1d(self, f: Any, xp: Any) -> torch.Tensor:
+        """f at arbitrary points through its masked, filtered Fourier series
+        (grid.py:581-618)."""
+        return self._eval_points([f], [xp])[0]
 
     def project_solenoidal_x(self, Bx: Any) -> torch.Tensor:
         """The 1D Leray projection keeps only the mean of Bx (grid.py:554-567)."""
@@ -313,6 +327,11 @@ class Grid2D(_FourierGridBase):
         self._mhd_plan.project_solenoidal_(bx, by)
         return bx, by
 
+    def evaluate_fourier_at_points(self, f: Any, xp: Any, yp: Any) -> torch.Tensor:
+        """f (Ny, Nx) at points (xp, yp) through its masked, filtered Fourier
+        series (grid.py:1180-1222)."""
+        return self._eval_points([f], [xp, yp])[0]
+
     def xy_mesh(self) -> Tuple[torch.Tensor, torch.Tensor]:
         Y, X = torch.meshgrid(self.y, self.x, indexing="ij")
         return X, Y
@@ -357,6 +376,16 @@ class Grid3D(_FourierGridBase):
 
     def dz1(self, f: Any) -> torch.Tensor:
         return self._op(f, 2)
+
+    def evaluate_fourier_at_points(self, f: Any, xp: Any, yp: Any, zp: Any) -> torch.Tensor:
+        """f (Nz, Ny, Nx) at points (xp, yp, zp) (grid.py:1520-1567)."""
+        return self._eval_points([f], [xp, yp, zp])[0]
+
+    def evaluate_fourier_at_points_batched_3d(self, fx: Any, fy: Any, fz: Any, xp: Any, yp: Any, zp: Any
+                                              ) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        """Three fields at the same points in one sweep (grid.py:1569-1632)."""
+        v = self._eval_points([fx, fy, fz], [xp, yp, zp])
+        return v[0], v[1], v[2]
 
     def xyz_mesh(self) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
         Z, Y, X = torch.meshgrid(self.z, self.y, self.x, indexing="ij")

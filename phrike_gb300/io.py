@@ -46,9 +46,9 @@ def _primitives(U: np.ndarray, gamma: float) -> Dict[str, np.ndarray]:
 
 def save_solution_snapshot(outdir: str, t: float, U: Any, grid: Any, equations: Any, tag: Optional[str] = None,
                            tracers: Any = None) -> str:
-    """Write one snapshot (phrike/io.py:103-236) and return its path."""
-    if tracers is not None:
-        raise NotImplementedError("backend 'gb300': tracers are not implemented")
+    """Write one snapshot (phrike/io.py:103-236) and return its path; with
+    tracers, their positions and mass as tracer_x/y/z and tracer_mass
+    (io.py:86-100)."""
     os.makedirs(outdir, exist_ok=True)
     ts = f"t{t:.6f}"
     if tag:
@@ -77,6 +77,13 @@ def save_solution_snapshot(outdir: str, t: float, U: Any, grid: Any, equations: 
                 extra["div_b"] = _host(grid.divergence(U[5], U[6]))
             except Exception:
                 pass
+    if tracers is not None:
+        extra["tracer_x"] = _host(tracers.x)
+        for k in ("y", "z"):
+            if hasattr(tracers, k):
+                extra[f"tracer_{k}"] = _host(getattr(tracers, k))
+        if hasattr(tracers, "mass"):
+            extra["tracer_mass"] = np.asarray(tracers.mass)
     np.savez(path, t=t, U=Uh, meta=meta, created=str(datetime.now(timezone.utc).replace(tzinfo=None)),
              **coords, **prim, **extra)
     return path
@@ -94,6 +101,9 @@ def load_checkpoint(checkpoint_path: str) -> Dict[str, Any]:
         if k in data:
             out[k] = data[k]
     out["primitive_vars"] = {k: data[k] for k in ("rho", "u", "ux", "uy", "uz", "p") if k in data}
+    for k in ("tracer_x", "tracer_y", "tracer_z", "tracer_mass"):
+        if k in data:
+            out[k] = data[k]
     return out
 
 

@@ -118,6 +118,15 @@ def alfven_cp_1d(N: int, L: float = 1.0, t: float = 0.0, rho0: float = 1.0, p0: 
     return np.stack([rho, rho * ux, rho * uy, rho * uz, E, Bx, By, Bz])
 
 
+def acoustic_pulse_lgl_1d(x: np.ndarray, gamma: float = 1.4, amp: float = 0.01, width2: float = 0.01,
+                          center: float = 0.0) -> np.ndarray:
+    """rho = 1 + amp exp(-(x - center)^2/width2), p = rho^gamma/gamma, u = 0
+    on the given node coordinates (domain [-1, 1])."""
+    rho = 1.0 + amp * np.exp(-((np.asarray(x) - center) ** 2) / width2)
+    p = rho ** gamma / gamma
+    return _euler_conservative(rho, [np.zeros_like(rho)], p, gamma)
+
+
 def acoustic_pulse_lgl_2d(x: np.ndarray, y: np.ndarray, gamma: float = 1.4,
                           amp: float = 0.01, width2: float = 0.01,
                           center: Tuple[float, float] = (0.0, 0.0)) -> np.ndarray:

@@ -52,6 +52,7 @@ FAMILIES: Dict[str, dict] = {
                  equations="mhd"),
     "tgv3d": dict(ndim=3, gamma=1.4, cfl=0.25, filter=None),
     "lgl2d": dict(ndim=2, gamma=1.4, cfl=0.3, filter=None, basis="legendre", gemm_precision="bf16x3"),
+    "lgl1d": dict(ndim=1, gamma=1.4, cfl=0.3, filter=None, basis="legendre", gemm_precision="fp32"),
 }
 
 
@@ -111,6 +112,10 @@ class Request:
             from .engine import lgl_build
             x = (lgl_build(n, 2.0)[0] - 1.0).cpu().numpy()
             U = problems.acoustic_pulse_lgl_2d(x, x, amp=p.get("amp", 0.01), width2=p.get("width2", 0.01))
+        elif f == "lgl1d":
+            from .engine import lgl_build
+            x = (lgl_build(n, 2.0)[0] - 1.0).cpu().numpy()
+            U = problems.acoustic_pulse_lgl_1d(x, amp=p.get("amp", 0.01), width2=p.get("width2", 0.01))
         else:
             raise ValueError(f"unknown family {f!r}")
         self.U0 = U
@@ -416,10 +421,10 @@ def make_plan_bytes(family: str, n: int, slots: int) -> int:
 def request_stream(count: int, rate: float = 200.0, seed: int = 20261203,
                    t_end_range: Tuple[float, float] = (0.1, 1.0), families: Optional[Dict[str, List[int]]] = None
                    ) -> List[Request]:
-    """Seeded Poisson stream mixing the five families with uniform size draws
+    """Seeded Poisson stream mixing the six families with uniform size draws
     and t_end ~ U[t_end_range]."""
     fam = families or {"sod1d": [256, 512, 1024, 2048, 4096], "khi2d": [128, 256, 512, 1024], "ot2d": [128, 256, 512],
-                       "tgv3d": [32, 64, 128], "lgl2d": [65, 129, 257, 513]}
+                       "tgv3d": [32, 64, 128], "lgl2d": [65, 129, 257, 513], "lgl1d": [65, 129, 257, 513]}
     names = sorted(fam)
     rng = np.random.default_rng(seed)
     t = 0.0

@@ -115,9 +115,8 @@ class _SpectralSolverBase:
             dt: Optional[float] = None) -> Dict[str, List[float]]:
         """CFL-driven loop of the reference (solver.py:338-422); with ``dt``
         given, fixed steps of that size instead."""
-        if tracers is not None:
-            raise NotImplementedError("backend 'gb300': tracers are not implemented")
         self.U = self.grid.to_device(U0).clone()
+        self._tracers = tracers
         self.t = float(t0)
         next_output = self.t + output_interval
         # snapshots every checkpoint_interval into outdir (solver.py:357-361, 408-417)
@@ -139,6 +138,8 @@ class _SpectralSolverBase:
             self.t += h
             if on_step is not None:
                 on_step(step_count, h, self.U)
+            if tracers is not None:  # after every step with its dt (solver.py:398-399)
+                tracers.step(self.grid, self.equations, self.U, h)
             step_count += 1
             if dt is None:
                 step_dt = self.compute_dt(self.U)
@@ -157,7 +158,8 @@ class _SpectralSolverBase:
     def _checkpoint(self) -> None:
         if self._outdir and self.t + 1e-12 >= self._next_ckpt:
             from .io import save_solution_snapshot
-            save_solution_snapshot(self._outdir, self.t, self.U, self.grid, self.equations)
+            save_solution_snapshot(self._outdir, self.t, self.U, self.grid, self.equations,
+                                   tracers=getattr(self, "_tracers", None))
             self._next_ckpt += self._ckpt_interval
 
     def _run_adaptive(self, history, dt0, t_end, output_interval, next_output, on_output, on_step,
@@ -167,7 +169,9 @@ class _SpectralSolverBase:
         the next output time, so outputs are recorded after the same attempts
         as in the reference.  With on_step every attempt is a separate call
         and on_step sees each accepted attempt (step_count counts attempts,
-        rejected ones included)."""
+        rejected ones included).  Tracers, like on_step, take one attempt per
+        call and move after every attempt with its attempted dt, rejected
+        attempts included, as the reference's loop does (solver.py:384-399)."""
         dev = self.plan.device
         f64 = dict(dtype=torch.float64, device=dev)
         t = torch.full((1,), self.t, **f64)
@@ -179,13 +183,16 @@ class _SpectralSolverBase:
         while self.t < t_end - 1e-12:
             # an output or a checkpoint is still due after this attempt
             behind = self.t + 1e-12 >= min(next_output, self._next_ckpt)
-            if on_step is not None or behind:
+            tracers = getattr(self, "_tracers", None)
+            if on_step is not None or tracers is not None or behind:
                 dt_used = min(float(dtv.item()), t_end - self.t)
                 before = counts[0, 0].item()
                 self.plan.run_adaptive_(self.U, 1, self._ark, t, te, dtv, None, counts)
                 self.t = float(t.item())
                 if counts[0, 0].item() > before and on_step is not None:
                     on_step(step_count, dt_used, self.U)
+                if tracers is not None:
+                    tracers.step(self.grid, self.equations, self.U, dt_used)
                 step_count += 1
             else:
                 tout.fill_(min(next_output, self._next_ckpt))

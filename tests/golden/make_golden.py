@@ -53,6 +53,8 @@ def main(ref_path: str, only: str = "") -> None:
         return mhd_diffusion_fixtures(grid, equations, solver, problems)
     if only == "mhd1d":
         return mhd1d_fixtures(grid, equations, solver, problems)
+    if only == "tracers":
+        return tracer_fixtures(grid, equations, solver, problems)
     if only == "lgl1d":
         return lgl1d_fixtures(grid, equations, solver, problems)
 
@@ -209,6 +211,67 @@ def source_fixtures(grid, equations, solver, problems) -> None:
         out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
                                                            None)
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+def tracer_fixtures(grid, equations, solver, problems) -> None:
+    """Tracers (tracers.py) and point evaluation (grid.py evaluate_fourier_at_*)
+    on the cases of tests/tracer_cases.py: a random field and the velocity
+    at the initial tracer positions, the tracer positions after STEPS
+    leap-frog steps in the fixed state, and a KHI 32^2 run (CFL 0.4,
+    t_end 0.02) with 30 tracers through SpectralSolver2D.run."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import tracer_cases as TC
+    from phrike import tracers as T
+    out = {}
+    for name, (shape, lengths, dealias, filt, _) in TC.CASES.items():
+        nd = len(shape)
+        fp = dict(filt) if filt else None
+        if nd == 1:
+            g = grid.Grid1D(N=shape[0], Lx=lengths[0], dealias=dealias, filter_params=fp)
+            eq = equations.EulerEquations1D(gamma=TC.GAMMA)
+        elif nd == 2:
+            g = grid.Grid2D(Nx=shape[1], Ny=shape[0], Lx=lengths[1], Ly=lengths[0], dealias=dealias,
+                            filter_params=fp)
+            eq = equations.EulerEquations2D(gamma=TC.GAMMA)
+        else:
+            g = grid.Grid3D(Nx=shape[2], Ny=shape[1], Nz=shape[0], Lx=lengths[2], Ly=lengths[1], Lz=lengths[0],
+                            dealias=dealias, filter_params=fp)
+            eq = equations.EulerEquations3D(gamma=TC.GAMMA)
+        U = TC.state(name)
+        f = TC.field(name)
+        pos = TC.tracer_positions(name)
+        prim = eq.primitive(U)
+        vel = [prim[1 + a] for a in range(nd)]
+        if nd == 1:
+            fv = g.evaluate_fourier_at_points_1d(f, pos[0])
+            vv = [g.evaluate_fourier_at_points_1d(vel[0], pos[0])]
+            tr = T.FourierTracers1D(pos[0])
+        elif nd == 2:
+            fv = g.evaluate_fourier_at_points(f, pos[0], pos[1])
+            vv = [g.evaluate_fourier_at_points(v, pos[0], pos[1]) for v in vel]
+            tr = T.FourierTracers2D(pos[0], pos[1])
+        else:
+            fv = g.evaluate_fourier_at_points(f, pos[0], pos[1], pos[2])
+            vv = list(g.evaluate_fourier_at_points_batched_3d(vel[0], vel[1], vel[2], pos[0], pos[1], pos[2]))
+            tr = T.FourierTracers3D(pos[0], pos[1], pos[2])
+        for _ in range(TC.STEPS):
+            tr.step(g, eq, U.copy(), TC.DT)
+        out[f"{name}_f"] = np.asarray(fv)
+        out[f"{name}_vel"] = np.stack(vv)
+        out[f"{name}_pos"] = np.stack([tr.x] + ([tr.y] if nd > 1 else []) + ([tr.z] if nd > 2 else []))
+    # a solver run with tracers (problems/base.py:1082-1102 -> solver.run(..., tracers=))
+    g = grid.Grid2D(Nx=32, Ny=32, Lx=1.0, Ly=1.0, dealias=True)
+    eq = equations.EulerEquations2D(gamma=1.4)
+    s = solver.SpectralSolver2D(g, eq, scheme="rk4", cfl=0.4)
+    U0 = problems.kelvin_helmholtz_2d(32, 32, U0=1.0, A=0.01)
+    rng = np.random.default_rng(99)
+    x0, y0 = rng.uniform(0, 1, 30), rng.uniform(0, 1, 30)
+    tr = T.FourierTracers2D(x0, y0)
+    s.run(U0.copy(), 0.0, 0.02, output_interval=1.0, tracers=tr)
+    out["khi_x0"], out["khi_y0"] = x0, y0
+    out["khi_pos"] = np.stack([tr.x, tr.y])
+    out["khi_U"] = s.U
+    np.savez_compressed(os.path.join(HERE, "tracers.npz"), **out)
+
 
 def lgl1d_fixtures(grid, equations, solver, problems) -> None:
     """1D Legendre (LGL) grid with SpectralSolver1D: nodes, D, a Gaussian

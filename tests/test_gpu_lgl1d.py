@@ -171,7 +171,7 @@ def test_lgl1d_batch_matches_alone(cuda_device):
 
 
 def test_lgl1d_large_grid_properties(cuda_device):
-    """2048 nodes (the kernel's largest, float64 contractions: about 120 KB of
+    """2048 nodes (the kernel's largest, float64 contractions: about 136 KB of
     shared memory per CTA): mass is conserved to quadrature accuracy, walls
     hold and nothing becomes non-finite over 20 steps."""
     from phrike_gb300.engine import Plan

@@ -1,5 +1,5 @@
 """The serving loop: continuous batching of a mixed request stream (Sod 1D,
-KHI 2D, Orszag-Tang MHD, TGV 3D, LGL acoustic) on one GPU.  Requests arrive
+KHI 2D, Orszag-Tang MHD, TGV 3D, 1D and 2D LGL acoustic) on one GPU.  Requests arrive
 while others are running, are admitted into free slots of resident batched
 plans, overlap on the device and retire at their end times.  Every result
 must equal the same solve run alone (same kernels and arithmetic per slot):
@@ -9,7 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SMALL = {"sod1d": [256, 512], "khi2d": [32, 64], "ot2d": [32, 64], "tgv3d": [16, 32], "lgl2d": [17, 33]}
+SMALL = {"sod1d": [256, 512], "khi2d": [32, 64], "ot2d": [32, 64], "tgv3d": [16, 32], "lgl2d": [17, 33], "lgl1d": [17, 33]}
 
 
 def _stream(count, seed=7, rate=400.0):

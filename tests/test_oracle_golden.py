@@ -339,3 +339,42 @@ def test_mhd1d_matches_reference():
         dts.append(dt)
     np.testing.assert_allclose(dts, z["cfl_dts"], rtol=1e-12)
     assert rel_l2(U, z["cfl_U"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["d1", "d1_nyq", "d2", "d2_nyq", "d3", "d3_nyq"])
+def test_tracer_oracle_matches_reference(name):
+    """Point evaluation of a random field and of the velocity, and tracer
+    positions after leap-frog steps, against the reference's grids and
+    tracer classes (dealias on with the filter, and off: Nyquist modes)."""
+    import tracer_cases as TC
+    from oracle import tracers as OT
+    z = golden("tracers.npz")
+    shape, lengths, dealias, filt, _ = TC.CASES[name]
+    lxyz = list(reversed(lengths))
+    pos = TC.tracer_positions(name)
+    f = OT.eval_points(TC.field(name), pos, lxyz, dealias, filt)
+    assert np.abs(f - z[f"{name}_f"]).max() <= 1e-12 * np.abs(z[f"{name}_f"]).max()
+    U = TC.state(name)
+    tr = OT.Tracers(*pos)
+    v = tr.velocity(U, lxyz, dealias, filt)
+    assert np.abs(v - z[f"{name}_vel"]).max() <= 1e-12 * np.abs(z[f"{name}_vel"]).max()
+    for _ in range(TC.STEPS):
+        tr.step(U, TC.DT, lxyz, dealias, filt)
+    assert np.abs(np.stack(tr.pos) - z[f"{name}_pos"]).max() < 1e-13
+
+
+def test_tracer_config_layouts():
+    """tracers_from_config draws the reference's seeded random and uniform
+    layouts (problems/base.py:961-1021), without a device."""
+    from phrike_gb300.tracers import tracers_from_config
+
+    class G:  # a stand-in 3D Fourier grid: only shape and lengths are read
+        _shape, _basis, Lx, Ly, Lz = (4, 4, 4), "fourier", 1.0, 2.0, 3.0
+
+    t = tracers_from_config(G, {"enabled": True, "num": 5, "seed": 42})
+    rng = np.random.default_rng(42)
+    want = [rng.uniform(0.0, L, size=5) for L in (1.0, 2.0, 3.0)]
+    np.testing.assert_array_equal(np.stack([t.x, t.y, t.z]), np.stack(want))
+    u = tracers_from_config(G, {"enabled": True, "num": 8, "layout": "uniform"})
+    assert len(u.x) == 8 and float(np.max(u.z)) < 3.0
+    assert tracers_from_config(G, {"enabled": False}) is None
