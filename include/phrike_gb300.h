@@ -34,9 +34,10 @@ extern "C" {
 
 /* equation sets */
 #define PS_EQ_EULER 0
-#define PS_EQ_MHD 1 /* 2D (2.5D) ideal MHD, 8 components [rho, rho u (3), E, B (3)],
-                       periodic Fourier grids (equations.py:770-907,
-                       SpectralSolverMHD, solver.py:840-1049)            */
+#define PS_EQ_MHD 1 /* 1D, 2D (2.5D) and 3D ideal/resistive MHD, 8 components
+                       [rho, rho u (3), E, B (3)], periodic Fourier grids
+                       (equations.py:659-1100, SpectralSolverMHD,
+                       solver.py:840-1049, 1165-1174); 3D: 8..256 points per axis */
 
 /* arithmetic of the LGL differentiation-matrix contractions */
 #define PS_GEMM_FP32 0   /* float32 operands, float32 accumulate                 */
@@ -255,6 +256,11 @@ int ps_apply_boundary_conditions(ps_plan plan, float* U, void* stream);
  * plan's 2D Fourier grid.  Replaces Grid2D.project_solenoidal
  * (grid.py:1297-1327). */
 int ps_project_solenoidal(ps_plan plan, float* Bx, float* By, void* stream);
+
+/* The 3D projection of (Bx, By, Bz) in place for a 3D MHD plan: Nyquist
+ * planes zeroed, B_hat -= k (k . B_hat)/|k|^2.  Replaces
+ * Grid3D.project_solenoidal (grid.py:1649-1684). */
+int ps_project_solenoidal_3d(ps_plan plan, float* Bx, float* By, float* Bz, void* stream);
 
 /* The MHD state projection of SpectralSolverMHD._project_B
  * (solver.py:966-986) in place on U (PS_EQ_MHD plans): B projected, E

@@ -235,3 +235,96 @@ class MHDSolver1D(MHDSolver2D):
 
     def max_div_b(self, U: np.ndarray) -> float:
         return float(np.max(np.abs(self.box.deriv(U[5], 0))))
+
+
+def fluxes_3d(U: np.ndarray, gamma: float):
+    """Fx, Fy, Fz of MHDEquations3D.flux (equations.py:946-1038)."""
+    Fx, Fy = fluxes(U, gamma)
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    E = U[4]
+    uB = ux * Bx + uy * By + uz * Bz
+    ps = p + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+    mz = rho * uz
+    Fz = np.array([mz, mz * ux - Bz * Bx, mz * uy - Bz * By, mz * uz + ps - Bz * Bz,
+                   (E + ps) * uz - Bz * uB, uz * Bx - ux * Bz, uz * By - uy * Bz, np.zeros_like(rho)])
+    return Fx, Fy, Fz
+
+
+def max_wave_speed_3d(U: np.ndarray, gamma: float) -> float:
+    """max(|ux|, |uy|, |uz|) + sqrt(a^2 + b^2) (equations.py:1040-1061)."""
+    rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, gamma)
+    a2 = gamma * p / rho
+    b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+    um = np.maximum(np.maximum(np.abs(ux), np.abs(uy)), np.abs(uz))
+    return float(np.max(um + np.sqrt(np.maximum(a2 + b2, 0.0))))
+
+
+def project_solenoidal_3d(box: FourierBox, Bx: np.ndarray, By: np.ndarray, Bz: np.ndarray):
+    """Grid3D.project_solenoidal (grid.py:1649-1684): Nyquist planes zeroed,
+    B_hat -= k (k . B_hat) / k^2 (k = 0 kept)."""
+    nz, ny, nx = box.shape
+    F = [fftn(B, (-3, -2, -1)) for B in (Bx, By, Bz)]
+    for G in F:
+        if nx % 2 == 0:
+            G[..., :, :, nx // 2] = 0
+        if ny % 2 == 0:
+            G[..., :, ny // 2, :] = 0
+        if nz % 2 == 0:
+            G[..., nz // 2, :, :] = 0
+    kx = box.k[2][None, None, :]
+    ky = box.k[1][None, :, None]
+    kz = box.k[0][:, None, None]
+    k2 = kx * kx + ky * ky + kz * kz
+    k2s = np.where(k2 == 0.0, 1.0, k2)
+    coef = (kx * F[0] + ky * F[1] + kz * F[2]) / k2s
+    return tuple(ifftn(G - k * coef, (-3, -2, -1)).real for G, k in zip(F, (kx, ky, kz)))
+
+
+class MHDSolver3D(MHDSolver2D):
+    """SpectralSolverMHD3D (solver.py:840-1049, 1173-1174): rhs =
+    -(dx1 Fx + dy1 Fy + dz1 Fz) + eta lap B + nu lap(rho u); clamp and 3D
+    projection after every stage, filter then projection at the cadence;
+    CFL dt = cfl min(dx, dy, dz) / max speed, parabolic limit with
+    k^2_max = max(kx^2 + ky^2 + kz^2)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, lx: float = 1.0, ly: float = 1.0, lz: float = 1.0, **kw):
+        super().__init__(nx, ny, lx, ly, **kw)
+        fp = kw.get("filter_params") or {}
+        self.box = FourierBox((nz, ny, nx), (lz, ly, lx), dealias=kw.get("dealias", True),
+                              filter_enabled=bool(fp.get("enabled", False)), filter_p=int(fp.get("p", 8)),
+                              filter_alpha=float(fp.get("alpha", 36.0)))
+
+    def rhs(self, U: np.ndarray) -> np.ndarray:
+        Fx, Fy, Fz = fluxes_3d(U, self.gamma)
+        r = -(self.box.deriv(Fx, 2) + self.box.deriv(Fy, 1) + self.box.deriv(Fz, 0))
+        if self.resistivity != 0.0:
+            for c in (5, 6, 7):
+                r[c] = r[c] + self.resistivity * self.box.laplacian(U[c])
+        if self.viscosity != 0.0:
+            for c in (1, 2, 3):
+                r[c] = r[c] + self.viscosity * self.box.laplacian(U[c])
+        return r
+
+    def project(self, U: np.ndarray) -> np.ndarray:
+        if self.divergence_clean == "none":
+            return U
+        rho, ux, uy, uz, p, Bx, By, Bz = primitive(U, self.gamma)
+        Bx, By, Bz = project_solenoidal_3d(self.box, U[5], U[6], U[7])
+        V = U.copy()
+        V[5], V[6], V[7] = Bx, By, Bz
+        V[4] = p / (self.gamma - 1.0) + 0.5 * rho * (ux * ux + uy * uy + uz * uz) + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+        return V
+
+    def compute_dt(self, U: np.ndarray) -> float:
+        s = max_wave_speed_3d(U, self.gamma)
+        if s <= 0.0:
+            return 1e-6
+        dt = self.cfl * min(self.box.spacing) / s
+        dif = max(self.resistivity, self.viscosity)
+        if dif > 0.0:
+            k2max = sum(float(np.max(k * k)) for k in self.box.k)
+            dt = min(dt, self.cfl_diff / (dif * k2max))
+        return dt
+
+    def max_div_b(self, U: np.ndarray) -> float:
+        return float(np.max(np.abs(self.box.deriv(U[5], 2) + self.box.deriv(U[6], 1) + self.box.deriv(U[7], 0))))

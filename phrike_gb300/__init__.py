@@ -139,9 +139,21 @@ def run_simulation(problem_name: str, config_path: Optional[str] = None, config:
                             int(ic.get("direction", 1)), gamma)
         solver = S.SpectralSolverMHD1D(grid, eqs, scheme=integ.get("scheme", "rk4"),
                                        cfl=float(integ.get("cfl", 0.4)), **opts)
+    elif name == "alfven3d":
+        Nx, Ny, Nz = int(g.get("Nx", 64)), int(g.get("Ny", 8)), int(g.get("Nz", 8))
+        Lx = float(g.get("Lx", 1.0))
+        gamma = float(phys.get("gamma", 5.0 / 3.0))
+        grid = G.Grid3D(Nx=Nx, Ny=Ny, Nz=Nz, Lx=Lx, Ly=float(g.get("Ly", 1.0)), Lz=float(g.get("Lz", 1.0)), **kw)
+        grid.mhd_config = (phys.get("mhd", {}) or {})
+        eqs = E.MHDEquations3D(gamma=gamma)
+        U0 = P.alfven_cp_3d(Nx, Ny, Nz, Lx, 0.0, float(ic.get("rho0", 1.0)), float(ic.get("p0", 0.1)),
+                            float(ic.get("B0", 1.0)), float(ic.get("b1", 0.1)), int(ic.get("m", 1)),
+                            int(ic.get("direction", 1)), gamma)
+        solver = S.SpectralSolverMHD3D(grid, eqs, scheme=integ.get("scheme", "rk4"),
+                                       cfl=float(integ.get("cfl", 0.3)), **opts)
     else:
         raise ValueError(f"unknown problem {problem_name!r} "
-                         "(available: sod, tgv3d, khi2d, orszag_tang2d, alfven1d)")
+                         "(available: sod, tgv3d, khi2d, orszag_tang2d, alfven1d, alfven3d)")
     dt = integ.get("dt", None)
     # tracer particles from the ``tracers`` block (problems/base.py:961-1021, 1082-1102)
     from .tracers import tracers_from_config
@@ -159,11 +171,12 @@ def __getattr__(name: str):
     if name in ("Grid1D", "Grid2D", "Grid3D"):
         from . import grid
         return getattr(grid, name)
-    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D", "MHDEquations1D", "MHDEquations2D"):
+    if name in ("EulerEquations1D", "EulerEquations2D", "EulerEquations3D", "MHDEquations1D", "MHDEquations2D",
+                "MHDEquations3D"):
         from . import equations
         return getattr(equations, name)
     if name in ("SpectralSolver1D", "SpectralSolver2D", "SpectralSolver3D", "SpectralSolverMHD1D",
-                "SpectralSolverMHD2D"):
+                "SpectralSolverMHD2D", "SpectralSolverMHD3D"):
         from . import solver
         return getattr(solver, name)
     if name in ("FourierTracers1D", "FourierTracers2D", "FourierTracers3D"):

@@ -117,6 +117,7 @@ _SIGNATURES = [
     ("ps_apply_boundary_conditions", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_project_solenoidal", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_project_state", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_project_solenoidal_3d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_eval_points", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_tracers_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                   C.c_void_p, C.c_void_p]),

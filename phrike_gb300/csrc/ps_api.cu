@@ -18,6 +18,7 @@
 #include "launch.cuh"
 #include "lgl.cuh"
 #include "lgl1d.cuh"
+#include "mhd3d.cuh"
 #include "plan.cuh"
 #include "reduce.cuh"
 
@@ -83,7 +84,10 @@ int validate(const ps_plan_desc* d) {
     return fail(PS_ERR_INVALID, "scheme must be PS_SCHEME_RK4 or PS_SCHEME_RK2 (got %d)", d->scheme);
   if (is_lgl(d)) return ps::lgl_validate(d);
   if (d->equations == PS_EQ_MHD) {
-    if (d->ndim == 3) return fail(PS_ERR_UNSUPPORTED, "MHD plans are 1D or 2D (got ndim 3)");
+    if (d->ndim == 3)
+      for (int a = 0; a < 3; ++a)
+        if (!ps::mhd3_supported_n(d->n[a]))
+          return fail(PS_ERR_UNSUPPORTED, "3D MHD axis %d: N=%d not supported (powers of two 8..256)", a, d->n[a]);
     if (d->ndim == 1 && d->n[0] > 2048)
       return fail(PS_ERR_UNSUPPORTED, "1D MHD pencils are limited to 2048 points (got %d)", d->n[0]);
     if (!(d->mhd_resistivity >= 0.0) || !(d->mhd_viscosity >= 0.0) || !(d->mhd_cfl_diff > 0.0))
@@ -132,8 +136,10 @@ ps::AVParams av_params(const ps_plan_desc* d) {
 }
 
 size_t scratch_fields(int nd, bool mhd = false) {
-  // G + AB + acc + Us (+ 1D flux); MHD: G (16) + acc + Us + half spectra (~2)
+  // G + AB + acc + Us (+ 1D flux); MHD: G (16) + acc + Us + half spectra (~2);
+  // 3D MHD: three 8-field flux blocks + acc + Us + 3 half spectra (~3)
   if (nd == 1) return 3;
+  if (mhd && nd == 3) return 24 + 8 + 8 + 4;
   if (mhd) return 16 + 8 + 8 + 3;
   if (nd == 2) return 8 + 4 + 4;
   return 15 + 10 + 5 + 5;
@@ -641,8 +647,46 @@ int project(ps_plan p, float* Bx, float* By, float* E, long ss, const int* activ
   return PS_OK;
 }
 
+// 3D Helmholtz projection of (Bx, By, Bz) in place (solve stride ss); E
+// (nullable) updated at fixed thermal pressure (grid.py:1649-1684,
+// solver.py:966-986)
+int project3(ps_plan p, float* Bx, float* By, float* Bz, float* E, long ss, const int* active, cudaStream_t s) {
+  ps::Proj3Args a{};
+  a.B[0] = Bx;
+  a.B[1] = By;
+  a.B[2] = Bz;
+  a.E = E;
+  a.ss = ss;
+  a.H = p->H;
+  a.nx = p->n[0];
+  a.ny = p->n[1];
+  a.nz = p->n[2];
+  a.hx = p->n[0] / 2 + 1;
+  a.nsolve = p->nsolve;
+  a.k0x = (float)(2.0 * M_PI / p->desc.length[0]);
+  a.k0y = (float)(2.0 * M_PI / p->desc.length[1]);
+  a.k0z = (float)(2.0 * M_PI / p->desc.length[2]);
+  a.active = active;
+  // bytes: read B (3), write/read/write/read/write/read the half spectra (~3 each), write B (+E)
+  ProfScope prof(p, s, PS_KIND_OP, 4.0 * p->cells * p->nsolve * (3 + 6 * 3 + 3 + (E ? 2 : 0)));
+  cudaError_t e;
+  a.ax = p->ax(0);
+  if ((e = ps::launch_proj3_xf(p->n[0], a, s)) != cudaSuccess) return cuda_fail(e, "3D projection x forward");
+  a.ax = p->ax(1);
+  if ((e = ps::launch_proj3_y(p->n[1], false, a, s)) != cudaSuccess) return cuda_fail(e, "3D projection y forward");
+  a.ax = p->ax(2);
+  if ((e = ps::launch_proj3_z(p->n[2], a, s)) != cudaSuccess) return cuda_fail(e, "3D projection z");
+  a.ax = p->ax(1);
+  if ((e = ps::launch_proj3_y(p->n[1], true, a, s)) != cudaSuccess) return cuda_fail(e, "3D projection y inverse");
+  a.ax = p->ax(0);
+  if ((e = ps::launch_proj3_xi(p->n[0], a, s)) != cudaSuccess) return cuda_fail(e, "3D projection x inverse");
+  return PS_OK;
+}
+
 int project_state(ps_plan p, float* U, const int* active, cudaStream_t s) {
   if (!p->desc.mhd_divergence_clean) return PS_OK;  // divergence_clean "none"
+  if (p->nd == 3)
+    return project3(p, U + 5 * p->cells, U + 6 * p->cells, U + 7 * p->cells, U + 4 * p->cells, p->ss(8), active, s);
   if (p->nd == 1) {
     PS_CU(ps::launch_project_mhd1d(U, p->cells, p->ss(8), p->nsolve, active, s), "1D projection");
     return PS_OK;
@@ -689,6 +733,67 @@ int mhd1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double
   return PS_OK;
 }
 
+// 3D MHD stage: the flux kernel (with the CFL speed on request), the nine
+// operator passes dx1 Fx, dy1 Fy, dz1 Fz (and the nine of the three
+// Laplacian blocks with explicit diffusion), then the update kernel: stage
+// < 0 writes the right-hand side to out, else the RK stage with the clamp.
+// control: after the flux kernel, the device CFL step control (solver.py:1018-1034).
+int mhd3_stage(ps_plan p, const float* src, int stage, const float* Un, float* out, double dt, const double* dtp,
+               float* speed, bool control, double* d_t, const double* d_tend, cudaStream_t s, const int* act) {
+  int rc;
+  const bool dif = p->dif_buf != nullptr;
+  ps::Mhd3FluxArgs f{};
+  f.U = src;
+  f.F = p->G;
+  f.dif = dif ? p->dif_buf : nullptr;
+  f.cells = p->cells;
+  f.nsolve = p->nsolve;
+  f.gamma = (float)p->desc.gamma;
+  f.speed = speed;
+  f.active = act;
+  {
+    ProfScope prof(p, s, PS_KIND_X, 4.0 * p->cells * p->nsolve * (8 + 24 + (dif ? 18 : 0)));
+    PS_CU(ps::launch_mhd3_flux(f, s), "3D MHD flux");
+  }
+  if (control)
+    PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s,
+                                  p->dt_diff()),
+          "step control");
+  const long c = p->cells * p->nsolve;
+  for (int d = 0; d < 3; ++d) {  // block d: the flux along axis d, D on axis d and P on the others
+    float* F = p->G + (long)d * 8 * c;
+    for (int ax = 0; ax < 3; ++ax)
+      if ((rc = apply_op(p, ax, F, F, 8, ax == d ? 1 : 0, 1.0f, s, false, act)) != PS_OK) return rc;
+  }
+  if (dif)
+    for (int d = 0; d < 3; ++d) {  // L on axis d (-k^2 m s, Nyquist kept) and P on the others
+      float* D = p->dif_buf + (long)d * 6 * c;
+      for (int ax = 0; ax < 3; ++ax)
+        if ((rc = apply_op(p, ax, D, D, 6, ax == d ? 2 : 0, 1.0f, s, false, act)) != PS_OK) return rc;
+    }
+  ps::Mhd3UpdateArgs u{};
+  u.F = p->G;
+  u.dif = dif ? p->dif_buf : nullptr;
+  u.eta = (float)p->desc.mhd_resistivity;
+  u.nu = (float)p->desc.mhd_viscosity;
+  u.Un = Un;
+  u.acc = p->acc;
+  u.out = out;
+  u.cells = p->cells;
+  u.nsolve = p->nsolve;
+  u.stage = stage;
+  u.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+  u.dt_dev = dtp;
+  u.dt = dt;
+  u.gamma = (float)p->desc.gamma;
+  u.rho_min = (float)p->desc.mhd_rho_min;
+  u.p_min = (float)p->desc.mhd_p_min;
+  u.active = act;
+  ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * p->nsolve * (24 + (dif ? 18 : 0) + (stage < 0 ? 8 : 32)));
+  PS_CU(ps::launch_mhd3_update(u, s), "3D MHD update");
+  return PS_OK;
+}
+
 int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
               cudaStream_t s) {
   int rc;
@@ -706,6 +811,14 @@ int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
       if (p->desc.scheme == PS_SCHEME_RK2 && (stage == 1 || stage == 2)) continue;  // midpoint RK2
       const float* src = (stage == 0) ? U : p->Us;
       float* out = (stage < 3) ? p->Us : U;
+      if (p->nd == 3) {
+        const bool ctl = cfl && stage == 0;
+        if ((rc = mhd3_stage(p, src, stage, U, out, dt, dtp, ctl ? p->speed : nullptr, ctl, d_t, d_tend, s, act)) !=
+            PS_OK)
+          return rc;
+        if (p->desc.mhd_project_substages && (rc = project_state(p, out, act, s)) != PS_OK) return rc;
+        continue;
+      }
       if ((rc = xfirst_mhd(p, src, (cfl && stage == 0) ? p->speed : nullptr, s, act)) != PS_OK) return rc;
       if (cfl && stage == 0)
         PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s,
@@ -715,8 +828,8 @@ int steps_mhd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
       if (p->desc.mhd_project_substages && (rc = project_state(p, out, act, s)) != PS_OK) return rc;
     }
     if (due) {
-      if ((rc = apply_op(p, 0, U, U, 8, 0, 1.0f, s, true, act)) != PS_OK) return rc;
-      if ((rc = apply_op(p, 1, U, U, 8, 0, 1.0f, s, true, act)) != PS_OK) return rc;
+      for (int ax = 0; ax < p->nd; ++ax)
+        if ((rc = apply_op(p, ax, U, U, 8, 0, 1.0f, s, true, act)) != PS_OK) return rc;
       if ((rc = project_state(p, U, act, s)) != PS_OK) return rc;
     }
     if (cfl)
@@ -779,6 +892,7 @@ void ark_final_combs(const ps::ArkTableau& t, ps::ArkComb* high, ps::ArkComb* di
 // flux divergence
 int ark_rhs(ps_plan p, const float* src, float* k, const int* act, cudaStream_t s) {
   int rc;
+  if (p->mhd && p->nd == 3) return mhd3_stage(p, src, -1, src, k, 0.0, nullptr, nullptr, false, nullptr, nullptr, s, act);
   if (p->mhd) {
     if ((rc = xfirst_mhd(p, src, nullptr, s, act)) != PS_OK) return rc;
   } else {
@@ -912,14 +1026,15 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     // 1D MHD from 2048 points: U^n and the accumulator in global scratch
     if (p->mhd && p->n[0] >= 2048 && (rc = dalloc(p, &p->acc, 16 * c)) != PS_OK) return cleanup(rc);
   } else {
-    const int ng = p->mhd ? 16 : (p->nd == 3) ? 15 : 8;
+    const bool mhd3 = p->mhd && p->nd == 3;
+    const int ng = mhd3 ? 24 : p->mhd ? 16 : (p->nd == 3) ? 15 : 8;
     if ((rc = dalloc(p, &p->G, ng * c)) != PS_OK) return cleanup(rc);
-    if (p->mhd && (rc = dalloc(p, &p->H, (size_t)2 * nsolve * p->n[1] * (p->n[0] / 2 + 1))) != PS_OK)
-      return cleanup(rc);
+    const size_t hplanes = mhd3 ? (size_t)3 * p->n[2] * p->n[1] : (size_t)2 * p->n[1];
+    if (p->mhd && (rc = dalloc(p, &p->H, hplanes * nsolve * (p->n[0] / 2 + 1))) != PS_OK) return cleanup(rc);
     if (p->mhd && (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0) &&
-        (rc = dalloc(p, &p->dif_buf, 12 * c)) != PS_OK)
+        (rc = dalloc(p, &p->dif_buf, (mhd3 ? 18 : 12) * c)) != PS_OK)
       return cleanup(rc);
-    if (p->nd == 3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
+    if (p->nd == 3 && !mhd3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
   }
@@ -959,7 +1074,7 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
   if (lgl) {
     if ((rc = ps::lgl_setup(p)) != PS_OK) return cleanup(rc);
-  } else if (p->nd >= 2) {
+  } else if (p->nd >= 2 && !(p->mhd && p->nd == 3)) {
     if ((rc = make_map(&p->map_G_y, p->G, p, p->mhd ? 16 : (p->nd == 3) ? 15 : 8, 1)) != PS_OK)
       return cleanup(rc);
     if (p->nd == 3 && (rc = make_map(&p->map_AB_z, p->AB, p, 10, 2)) != PS_OK) return cleanup(rc);
@@ -1027,6 +1142,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
   if (d->ndim == 1 && mhd && d->n[0] >= 2048) fields += 16;
   if (mhd && d->ndim == 2 && (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0)) fields += 12;
+  if (mhd && d->ndim == 3 && (d->mhd_resistivity != 0.0 || d->mhd_viscosity != 0.0)) fields += 18;
   *bytes = fields * (size_t)cells * sizeof(float) * nsolve + tables + 64 + 32 * (size_t)nsolve;
   return PS_OK;
 }
@@ -1104,6 +1220,7 @@ int ps_rhs(ps_plan p, const float* U, float* rhs, void* stream) {
   if (p->lgl) return ps::lgl_rhs(p, U, rhs, s);
   if (p->mhd) {
     if (p->nd == 1) return mhd1d(p, const_cast<float*>(U), 0, 0.0, nullptr, nullptr, nullptr, rhs, s);
+    if (p->nd == 3) return mhd3_stage(p, U, -1, U, rhs, 0.0, nullptr, nullptr, false, nullptr, nullptr, s, nullptr);
     if ((rc = xfirst_mhd(p, U, nullptr, s, nullptr)) != PS_OK) return rc;
     return last(p, -1, U, rhs, 0.0, nullptr, false, s, nullptr);
   }
@@ -1236,6 +1353,13 @@ int ps_apply_boundary_conditions(ps_plan p, float* U, void* stream) {
   return PS_OK;
 }
 
+int ps_project_solenoidal_3d(ps_plan p, float* Bx, float* By, float* Bz, void* stream) {
+  if (!p || !Bx || !By || !Bz) return fail(PS_ERR_INVALID, "null argument");
+  if (p->lgl || p->nd != 3 || p->H == nullptr)
+    return fail(PS_ERR_UNSUPPORTED, "the 3D Helmholtz projection needs a 3D Fourier MHD plan");
+  return project3(p, Bx, By, Bz, nullptr, p->cells, nullptr, (cudaStream_t)stream);
+}
+
 int ps_project_solenoidal(ps_plan p, float* Bx, float* By, void* stream) {
   if (!p || !Bx || !By) return fail(PS_ERR_INVALID, "null argument");
   if (p->lgl || p->nd != 2 || p->H == nullptr)
@@ -1255,6 +1379,10 @@ int ps_max_wave_speed(ps_plan p, const float* U, float* d_out, void* stream) {
     if (p->nd == 1)
       PS_CU(ps::launch_speed_mhd1d(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out,
                                    (cudaStream_t)stream),
+            "max wave speed");
+    else if (p->nd == 3)
+      PS_CU(ps::launch_speed_mhd3(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out,
+                                  (cudaStream_t)stream),
             "max wave speed");
     else
       PS_CU(ps::launch_speed_mhd(U, p->cells, p->ss(8), p->nsolve, (float)p->desc.gamma, d_out,

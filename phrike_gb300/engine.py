@@ -329,6 +329,14 @@ class Plan:
                                              float(dt), vp, _stream(self.device)))
         return pos
 
+    def project_solenoidal_3d_(self, Bx: torch.Tensor, By: torch.Tensor, Bz: torch.Tensor):
+        """3D Helmholtz projection of (Bx, By, Bz) in place (one field per solve each)."""
+        for b in (Bx, By, Bz):
+            self._check_state(b, 1)
+        _lib.check(self._lib.ps_project_solenoidal_3d(self._handle, _ptr(Bx), _ptr(By), _ptr(Bz),
+                                                      _stream(self.device)))
+        return Bx, By, Bz
+
     def project_solenoidal_(self, Bx: torch.Tensor, By: torch.Tensor):
         """Helmholtz projection of (Bx, By) in place (one field per solve each)."""
         self._check_state(Bx, 1)

@@ -202,6 +202,35 @@ class MHDEquations2D:
 
 
 @dataclass
+class MHDEquations3D(MHDEquations2D):
+    """Ideal compressible MHD in 3D, state (8, Nz, Ny, Nx)
+    (phrike/equations.py:911-1100): fluxes Fx, Fy, Fz and the isotropic CFL
+    bound max(|ux|, |uy|, |uz|) + sqrt(a^2 + b^2)."""
+
+    gamma: float = 5.0 / 3.0
+
+    def flux(self, U):
+        U = _t(U)
+        Fx, Fy = super().flux(U)
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        ps = p + 0.5 * (Bx * Bx + By * By + Bz * Bz)
+        mz = rho * uz
+        uB = ux * Bx + uy * By + uz * Bz
+        Fz = torch.stack([mz, mz * ux - Bz * Bx, mz * uy - Bz * By, mz * uz + ps - Bz * Bz,
+                          (U[4] + ps) * uz - Bz * uB, uz * Bx - ux * Bz, uz * By - uy * Bz,
+                          torch.zeros_like(rho)], dim=0)
+        return Fx, Fy, Fz
+
+    def max_wave_speed(self, U) -> float:
+        rho, ux, uy, uz, p, Bx, By, Bz = self.primitive(U)
+        a2 = self.gamma * p / rho
+        b2 = (Bx * Bx + By * By + Bz * Bz) / rho
+        fast = torch.sqrt(torch.clamp(a2 + b2, min=0.0))
+        um = torch.maximum(torch.maximum(torch.abs(ux), torch.abs(uy)), torch.abs(uz))
+        return float(torch.max(um + fast).item())
+
+
+@dataclass
 class MHDEquations1D(MHDEquations2D):
     """Ideal compressible MHD varying along x only (phrike/equations.py:659-767):
     the same 8-component state, the x flux alone (its Bx row is zero, so Bx

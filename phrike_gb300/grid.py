@@ -351,6 +351,8 @@ class Grid3D(_FourierGridBase):
         self._shape = (self.Nz, self.Ny, self.Nx)
         self._lengths = (self.Lz, self.Ly, self.Lx)
         self.dx, self.dy, self.dz = self.Lx / self.Nx, self.Ly / self.Ny, self.Lz / self.Nz
+        self.mhd_config: Optional[Dict[str, Any]] = None  # set by MHD problems (grid.mhd_config)
+        self._mhd_plan: Optional[Plan] = None
         self._init_plan(dealias, filter_params, torch_device, precision)
         self.x = torch.as_tensor(np.linspace(0.0, self.Lx, self.Nx, endpoint=False), device=self.device)
         self.y = torch.as_tensor(np.linspace(0.0, self.Ly, self.Ny, endpoint=False), device=self.device)
@@ -376,6 +378,21 @@ class Grid3D(_FourierGridBase):
 
     def dz1(self, f: Any) -> torch.Tensor:
         return self._op(f, 2)
+
+    # --- MHD solenoidal helpers (grid.py:1635-1703) ---
+    def divergence(self, Vx: Any, Vy: Any, Vz: Any) -> torch.Tensor:
+        """dx1(Vx) + dy1(Vy) + dz1(Vz) with the masked derivative operators."""
+        return self.dx1(Vx) + self.dy1(Vy) + self.dz1(Vz)
+
+    def project_solenoidal(self, Vx: Any, Vy: Any, Vz: Any) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        """Helmholtz (Leray) projection of (Vx, Vy, Vz); returns new tensors
+        (ps_project_solenoidal_3d)."""
+        if self._mhd_plan is None:
+            self._mhd_plan = Plan(self._shape, self._lengths, dealias=self.dealias, filter_params=self.filter_params,
+                                  device=self.device, equations="mhd")
+        v = [self.to_device(V).clone() for V in (Vx, Vy, Vz)]
+        self._mhd_plan.project_solenoidal_3d_(*v)
+        return v[0], v[1], v[2]
 
     def evaluate_fourier_at_points(self, f: Any, xp: Any, yp: Any, zp: Any) -> torch.Tensor:
         """f (Nz, Ny, Nx) at points (xp, yp, zp) (grid.py:1520-1567)."""

@@ -118,6 +118,16 @@ def alfven_cp_1d(N: int, L: float = 1.0, t: float = 0.0, rho0: float = 1.0, p0: 
     return np.stack([rho, rho * ux, rho * uy, rho * uz, E, Bx, By, Bz])
 
 
+def alfven_cp_3d(Nx: int, Ny: int, Nz: int, Lx: float = 1.0, t: float = 0.0, rho0: float = 1.0, p0: float = 0.1,
+                 B0: float = 1.0, b1: float = 0.1, m: int = 1, direction: int = 1,
+                 gamma: float = 5.0 / 3.0) -> np.ndarray:
+    """The circularly polarized Alfven wave along x in a 3D box (the
+    reference's alfven3d problem, problems/problem_list/alfven3d.py:23-50):
+    the 1D profile repeated over (z, y); shape (8, Nz, Ny, Nx)."""
+    U1 = alfven_cp_1d(Nx, Lx, t, rho0, p0, B0, b1, m, direction, gamma)
+    return np.ascontiguousarray(np.broadcast_to(U1[:, None, None, :], (8, Nz, Ny, Nx)))
+
+
 def acoustic_pulse_lgl_1d(x: np.ndarray, gamma: float = 1.4, amp: float = 0.01, width2: float = 0.01,
                           center: float = 0.0) -> np.ndarray:
     """rho = 1 + amp exp(-(x - center)^2/width2), p = rho^gamma/gamma, u = 0

@@ -333,6 +333,27 @@ class SpectralSolverMHD2D(_SpectralSolverBase):
                            on_output, on_step, tracers, dt)
 
 
+class SpectralSolverMHD3D(SpectralSolverMHD2D):
+    """3D ideal/resistive MHD (phrike/solver.py:840-1049, 1173-1174): the
+    same stage structure as 2D with the 3D fluxes, the 3D projection after
+    every stage and the filter then projection at the cadence; CFL dt =
+    cfl * min(dx, dy, dz) / max(max(|ux|, |uy|, |uz|) + sqrt(a^2 + b^2)),
+    capped by cfl_diff / (max(eta, nu) k^2_max) with diffusion."""
+
+    _ndim = 3
+
+    def _spacing(self) -> float:
+        return min(self.grid.dx, self.grid.dy, self.grid.dz)
+
+    def _k2_max(self) -> float:
+        g = self.grid
+        return sum((math.pi * n / L) ** 2 for n, L in ((g.Nx, g.Lx), (g.Ny, g.Ly), (g.Nz, g.Lz)))
+
+    def max_div_b(self, U: Any) -> float:
+        t = self.grid.to_device(U)
+        return float(torch.max(torch.abs(self.grid.divergence(t[5], t[6], t[7]))).item())
+
+
 class SpectralSolverMHD1D(SpectralSolverMHD2D):
     """1D MHD (phrike/solver.py:840-1049, 1165-1166): the x flux of
     MHDEquations1D, every RK stage clamped and (project_each_substage)

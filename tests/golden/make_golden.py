@@ -53,6 +53,8 @@ def main(ref_path: str, only: str = "") -> None:
         return mhd_diffusion_fixtures(grid, equations, solver, problems)
     if only == "mhd1d":
         return mhd1d_fixtures(grid, equations, solver, problems)
+    if only == "mhd3d":
+        return mhd3d_fixtures(grid, equations, solver, problems)
     if only == "tracers":
         return tracer_fixtures(grid, equations, solver, problems)
     if only == "lgl1d":
@@ -211,6 +213,42 @@ def source_fixtures(grid, equations, solver, problems) -> None:
         out[f"av2d_{mode}_rhs0"] = solver._compute_rhs_2d(g2b, s2b.equations, U0.copy(), s2b.artificial_viscosity,
                                                            None)
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+def mhd3d_fixtures(grid, equations, solver, problems) -> None:
+    """3D MHD (SpectralSolverMHD3D) on the cases of tests/mhd3d_cases.py:
+    rhs, the projected state, fixed-dt steps, the CFL dt, div B and the
+    conserved sums; plus a short CFL run of the Alfven case."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import mhd3d_cases as MC
+    out = {}
+    for name, (nx, ny, nz, lx, ly, lz, filt, cfg, scheme, dt, nsteps) in MC.CASES.items():
+        g = grid.Grid3D(Nx=nx, Ny=ny, Nz=nz, Lx=lx, Ly=ly, Lz=lz, dealias=True,
+                        filter_params=dict(filt) if filt else None)
+        g.mhd_config = dict(cfg)
+        eq = equations.MHDEquations3D(gamma=MC.GAMMA)
+        s = solver.SpectralSolverMHD3D(g, eq, scheme=scheme, cfl=0.3)
+        U0 = MC.initial_state(name)
+        out[f"{name}_U0"] = U0
+        out[f"{name}_rhs0"] = s._compute_rhs(U0.copy())
+        out[f"{name}_P0"] = s._project_B(U0.copy())
+        U = U0.copy()
+        for _ in range(nsteps):
+            U = s.step(U, dt)
+        out[f"{name}_U"] = U
+        out[f"{name}_dt0"] = s.compute_dt(U0)
+        out[f"{name}_divb_U"] = s.max_div_b(U)
+        c = eq.conserved_quantities(U)
+        out[f"{name}_cons"] = np.array([c[k] for k in ("mass", "momentum_x", "momentum_y", "momentum_z", "energy",
+                                                        "magnetic_energy", "cross_helicity")])
+    nx, ny, nz, lx, ly, lz, filt = MC.CASES["alfven"][:7]
+    g = grid.Grid3D(Nx=nx, Ny=ny, Nz=nz, Lx=lx, Ly=ly, Lz=lz, dealias=True, filter_params=dict(filt))
+    g.mhd_config = {}
+    s = solver.SpectralSolverMHD3D(g, equations.MHDEquations3D(gamma=MC.GAMMA), cfl=0.3)
+    seen = []
+    s.run(MC.initial_state("alfven"), 0.0, 0.05, output_interval=0.05, on_step=lambda n, dt, U: seen.append(dt))
+    out["cfl_U"], out["cfl_t"], out["cfl_dts"] = np.asarray(s.U), s.t, np.asarray(seen)
+    np.savez_compressed(os.path.join(HERE, "mhd3d.npz"), **out)
+
 
 def tracer_fixtures(grid, equations, solver, problems) -> None:
     """Tracers (tracers.py) and point evaluation (grid.py evaluate_fourier_at_*)

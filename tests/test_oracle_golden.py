@@ -378,3 +378,31 @@ def test_tracer_config_layouts():
     u = tracers_from_config(G, {"enabled": True, "num": 8, "layout": "uniform"})
     assert len(u.x) == 8 and float(np.max(u.z)) < 3.0
     assert tracers_from_config(G, {"enabled": False}) is None
+
+
+@pytest.mark.parametrize("name", ["alfven", "turb"])
+def test_mhd3d_oracle_matches_reference(name):
+    """3D MHD: rhs (with resistivity and viscosity in the turb case), the
+    projected state, fixed-dt steps (RK4 with the filter; RK2), the CFL dt,
+    div B and the conserved sums against SpectralSolverMHD3D."""
+    import mhd3d_cases as MC
+    from oracle import mhd as M
+    z = golden("mhd3d.npz")
+    nx, ny, nz, lx, ly, lz, filt, cfg, scheme, dt, nsteps = MC.CASES[name]
+    s = M.MHDSolver3D(nx, ny, nz, lx, ly, lz, gamma=MC.GAMMA, filter_params=filt, cfl=0.3, scheme=scheme,
+                      resistivity=cfg.get("resistivity", 0.0), viscosity=cfg.get("viscosity", 0.0))
+    U0 = MC.initial_state(name)
+    np.testing.assert_allclose(U0, z[f"{name}_U0"], rtol=0, atol=1e-15)
+    assert rel_l2(s.rhs(U0.copy()), z[f"{name}_rhs0"]) < 1e-12
+    assert rel_l2(s.project(U0.copy()), z[f"{name}_P0"]) < 1e-13
+    U = U0.copy()
+    for _ in range(nsteps):
+        U = s.step(U, dt)
+    for c in range(8):
+        assert rel_l2(U[c], z[f"{name}_U"][c]) < 1e-12 or np.abs(U[c] - z[f"{name}_U"][c]).max() < 1e-13, c
+    assert abs(s.compute_dt(U0) - float(z[f"{name}_dt0"])) <= 1e-13 * float(z[f"{name}_dt0"])
+    assert s.max_div_b(U) < 1e-12
+    cons = M.conserved_quantities(U, MC.GAMMA)
+    np.testing.assert_allclose([cons[k] for k in ("mass", "momentum_x", "momentum_y", "momentum_z", "energy",
+                                                  "magnetic_energy", "cross_helicity")], z[f"{name}_cons"],
+                               rtol=1e-12, atol=1e-10)
