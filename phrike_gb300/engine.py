@@ -103,6 +103,11 @@ class Plan:
             var = av_config.get("sensor_variable", "density")
             if var not in sensors:
                 raise ValueError(f"Unknown sensor variable: {var}")
+            if var == "velocity_magnitude" and mode == "sensor" and self.ndim == 2:
+                # the reference's 2D sensor unpacks primitive() as (rho, u, p, _), takes
+                # sqrt(u[0]^2 + u[1]^2) of the first two rows of u_x (a 1D array) and
+                # its 2D FFT raises (artificial_viscosity.py:133-139, 169-190)
+                raise ValueError("velocity_magnitude sensor on a 2D grid: axes exceeds dimensionality of input")
             desc.av_sensor = sensors[var]
             nu_c = float(av_config.get("nu_constant", 0.0))
             if mode == "constant" and nu_c < 0:

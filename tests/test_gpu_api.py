@@ -98,3 +98,14 @@ def test_run_writes_reference_snapshots(cuda_device, tmp_path):
     assert d["U"].shape == (4, 32, 32) and set(d["primitive_vars"]) == {"rho", "ux", "uy", "p"}
     assert d["meta"]["Nx"] == 32 and abs(d["meta"]["gamma"] - 1.4) < 1e-12
     assert np.isfinite(d["U"]).all() and d["t"] in times
+
+
+def test_2d_velocity_magnitude_sensor_raises_like_the_reference(cuda_device):
+    """The reference's 2D velocity-magnitude AV sensor raises ValueError
+    (its q is a 1D array); plans asking for it raise the same error, while
+    the 1D form is accepted."""
+    from phrike_gb300.engine import Plan
+    av = {"enabled": True, "sensor_variable": "velocity_magnitude"}
+    with pytest.raises(ValueError):
+        Plan((16, 16), (1.0, 1.0), av_config=av)
+    Plan((64,), (1.0,), av_config=av)
