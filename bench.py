@@ -531,6 +531,71 @@ def run_ot(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mhd3d(args):
+    """3D ideal MHD: the circularly polarized Alfven wave along x (the
+    reference's alfven3d problem) on --mhd3d-n^3, gamma = 5/3, filter p = 8,
+    alpha = 36, fixed dt = 1e-3 RK4 with per-stage clamp and 3D projection:
+    cell-updates/s, per-kind launch times against the measured HBM peak, and
+    one float64 oracle step on the host cores as the CPU baseline."""
+    import torch
+    from oracle import mhd as M
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.engine import Plan
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    n = args.mhd3d_n
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    U0 = problems.alfven_cp_3d(n, n, n, 1.0)
+    plan = Plan((n, n, n), (1.0, 1.0, 1.0), gamma=5.0 / 3.0, filter_params=fp, device=device, equations="mhd")
+    U = torch.as_tensor(U0, dtype=torch.float32, device=device).contiguous()
+    plan.project_state_(U)
+    plan.run_(U, args.warmup, 1e-3)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    st = torch.cuda.current_stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(1, min(args.steps, 50))
+    e0.record(st)
+    plan.run_(U, steps, 1e-3)
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / steps
+    plan.profile(True)
+    plan.run_(U, 2, 1e-3)
+    prof = plan.collect_profile()
+    plan.profile(False)
+    peak, src = hbm_peak()
+    kinds, total_bytes = {}, 0.0
+    for k, v in prof.items():
+        per = v["ms"] / v["launches"]
+        total_bytes += v["bytes"] / 2
+        kinds[k] = {"launches_per_step": v["launches"] / 2, "us_per_launch": per * 1e3,
+                    "gbs": v["bytes"] / v["launches"] / (per * 1e-3) / 1e9,
+                    "frac_of_peak": v["bytes"] / v["launches"] / (per * 1e-3) / 1e9 / peak}
+    cn = min(n, 64)  # CPU baseline: one float64 oracle step at a bounded size
+    s = M.MHDSolver3D(cn, cn, cn, 1.0, 1.0, 1.0, gamma=5.0 / 3.0, filter_params=fp)
+    R = s.project(problems.alfven_cp_3d(cn, cn, cn, 1.0))
+    t0 = time.perf_counter()
+    R = s.step(R, 1e-3)
+    cpu_s = time.perf_counter() - t0
+    G = U.cpu().numpy()
+    line = {
+        "metric": "3D ideal MHD Alfven wave: cell-updates/s (RK4, per-stage 3D projection)",
+        "value": n ** 3 / (ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (analytic circularly polarized Alfven wave)",
+        "config": {"workload": f"Alfven 3D {n}^3, gamma 5/3, filter p=8 alpha=36, RK4 dt=1e-3"},
+        "passes": kinds, "step_GBps": total_bytes / (ms * 1e-3) / 1e9, "peak_gbs": peak, "peak_source": src,
+        "cpu_baseline": {"value": cn ** 3 / cpu_s, "unit": "cell-updates/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"1 RK4 step of the float64 oracle at {cn}^3"},
+        "state_finite": bool(np.isfinite(G).all()), "status": plan.status(), "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_adaptive(args):
     """Adaptive embedded RK45 with the reference's shipped settings.
     (a) configs/sod.yaml: 1D Sod N=1024, rk45, rtol 1e-6, atol 1e-8,
@@ -705,7 +770,8 @@ def run_serving(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive"], default="tgv")
+    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive", "mhd3d"],
+                    default="tgv")
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
@@ -719,6 +785,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--ot-n", type=int, default=512)
+    ap.add_argument("--mhd3d-n", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -746,6 +813,9 @@ def main():
         elif args.workload == "adaptive":
             if rank == 0:
                 run_adaptive(args)
+        elif args.workload == "mhd3d":
+            if rank == 0:
+                run_mhd3d(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
