@@ -596,6 +596,54 @@ def run_mhd3d(args):
     print(json.dumps(line), flush=True)
 
 
+def run_tracers(args):
+    """Tracer advection (FourierTracers3D.step) with the reference's turb3d
+    tracer block: 262,144 tracers (64^3 uniform layout) on a 64^3 TGV state,
+    one leap-frog step per call with the spectral interpolation of the
+    velocity: tracer-steps/s, against the float64 oracle's evaluation of a
+    bounded sample of the tracers on the host cores."""
+    import torch
+    from oracle import tracers as OT
+    from phrike_gb300 import _build, problems
+    from phrike_gb300.grid import Grid3D
+    from phrike_gb300.tracers import tracers_from_config
+
+    _build.build()
+    n, num = args.tracer_n, args.tracer_num
+    L = 2 * np.pi
+    g = Grid3D(Nx=n, Ny=n, Nz=n, Lx=L, Ly=L, Lz=L)
+    U0 = problems.taylor_green_3d(n)
+    U = torch.as_tensor(U0, dtype=torch.float32, device="cuda").contiguous()
+    tr = tracers_from_config(g, {"enabled": True, "num": num, "layout": "uniform", "seed": 42})
+    for _ in range(args.warmup):
+        tr.step(g, None, U, 1e-3)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 20))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        tr.step(g, None, U, 1e-3)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # CPU: the oracle's interpolation of 64 tracers' velocities (3 components)
+    sample = 64
+    pos = [tr.x[:sample].cpu().numpy(), tr.y[:sample].cpu().numpy(), tr.z[:sample].cpu().numpy()]
+    t0 = time.perf_counter()
+    for a in range(3):
+        OT.eval_points(U0[1 + a] / U0[0], pos, (L, L, L), True, None)
+    cpu_s = time.perf_counter() - t0
+    line = {
+        "metric": "tracer steps/s (spectral velocity interpolation + leap-frog)", "value": num / (ms * 1e-3),
+        "unit": "tracer-steps/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f32 fields, f64 positions", "data": "synthetic (TGV state, uniform tracers)",
+        "config": {"workload": f"{num} tracers on a {n}^3 TGV state (turb3d tracer block)"},
+        "cpu_baseline": {"value": sample / cpu_s, "unit": "tracer-steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"velocity of {sample} tracers by the float64 oracle (exact interpolant)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_adaptive(args):
     """Adaptive embedded RK45 with the reference's shipped settings.
     (a) configs/sod.yaml: 1D Sod N=1024, rk45, rtol 1e-6, atol 1e-8,
@@ -770,8 +818,8 @@ def run_serving(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive", "mhd3d"],
-                    default="tgv")
+    ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive", "mhd3d",
+                                           "tracers"], default="tgv")
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
@@ -786,6 +834,8 @@ def main():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--ot-n", type=int, default=512)
     ap.add_argument("--mhd3d-n", type=int, default=128)
+    ap.add_argument("--tracer-n", type=int, default=64)
+    ap.add_argument("--tracer-num", type=int, default=262144)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -816,6 +866,9 @@ def main():
         elif args.workload == "mhd3d":
             if rank == 0:
                 run_mhd3d(args)
+        elif args.workload == "tracers":
+            if rank == 0:
+                run_tracers(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
