@@ -761,7 +761,9 @@ def run_serving(args):
     The plain form serves the same stream one solve at a time, first come
     first served, each solve alone on its own plan; its service times come
     from one alone run per (family, size) to t_end = --plain-t-end, scaled
-    linearly with each request's t_end (CFL steps of near-constant size)."""
+    linearly with each request's t_end (CFL steps of near-constant size).
+    The served run gives groups whose solves cost at least 5 s per unit time
+    alone a high-priority stream."""
     import torch
     from phrike_gb300 import _build
     from phrike_gb300.serving import Request, Server, request_stream, run_alone
@@ -775,18 +777,19 @@ def run_serving(args):
     Server(device, chunk=args.chunk).serve([Request(-1 - i, f, n, 1e-4) for i, (f, n) in enumerate(keys)],
                                           realtime=False)
     torch.cuda.synchronize()
-    srv = Server(device, chunk=args.chunk)
-    sampler = ClockSampler(0)
-    sampler.start()
-    stats = srv.serve(reqs, realtime=True)
-    clocks = sampler.stop()
-    # plain service times
+    # plain service times, one alone run per (family, size); they also give the
+    # server its cost model (long solves on high-priority streams)
     rate = {}
     for key in sorted({(r.family, r.n) for r in reqs}):
         probe = Request(-1, key[0], key[1], args.plain_t_end)
         run_alone(probe, device, chunk=args.chunk)  # warm-up (plan, kernels)
         _, sec = run_alone(probe, device, chunk=args.chunk)
         rate[key] = sec / args.plain_t_end
+    srv = Server(device, chunk=args.chunk, cost=lambda f, n: rate[(f, n)])
+    sampler = ClockSampler(0)
+    sampler.start()
+    stats = srv.serve(reqs, realtime=True)
+    clocks = sampler.stop()
     done, lat = 0.0, []
     for r in sorted(reqs, key=lambda q: q.arrival):
         start = max(r.arrival, done)

@@ -188,11 +188,13 @@ class Server:
 
     ``budget_bytes``: HBM the groups may hold (plan scratch + states); default
     half of the free device memory.  ``slots``: callable (family, n) -> slots
-    per group.  ``chunk``: CFL steps per captured chunk.
+    per group.  ``chunk``: CFL steps per captured chunk.  ``cost``: callable
+    (family, n) -> seconds per unit of simulated time of one solve alone;
+    groups costing at least ``priority_seconds`` get a high-priority stream.
     """
 
     def __init__(self, device=None, budget_bytes: Optional[int] = None, chunk: int = 20, slots=None,
-                 use_graphs: bool = True):
+                 use_graphs: bool = True, cost=None, priority_seconds: float = 5.0):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
@@ -201,6 +203,12 @@ class Server:
         self.chunk = int(chunk)
         self.slots_for = slots or self._default_slots
         self.use_graphs = use_graphs
+        # cost(family, n) -> seconds of one solve alone per unit of simulated
+        # time (e.g. measured by run_alone); groups at or above priority_seconds
+        # run on a high-priority stream, so that the long solves that set the
+        # stream's makespan are slowed least by the short ones around them
+        self.cost = cost
+        self.priority_seconds = float(priority_seconds)
         self.groups: List[_Group] = []
         self.used = 0
         self.projectors: Dict[int, Plan] = {}
@@ -241,7 +249,9 @@ class Server:
         U = torch.as_tensor(np.stack([ben] * slots), dtype=torch.float32, device=self.device).contiguous()
         t = torch.zeros(slots, dtype=torch.float64, device=self.device)
         te = torch.zeros(slots, dtype=torch.float64, device=self.device)  # t >= t_end: free
-        g = _Group(family, n, plan, U, t, te, torch.cuda.Stream(self.device), [None] * slots, need)
+        high = self.cost is not None and float(self.cost(family, n)) >= self.priority_seconds
+        stream = torch.cuda.Stream(self.device, priority=-1) if high else torch.cuda.Stream(self.device)
+        g = _Group(family, n, plan, U, t, te, stream, [None] * slots, need)
         if self.use_graphs:
             # warm up (kernel attributes, module loading) and capture the chunk
             # while every slot is free, so that a slot's chunk boundaries fall
