@@ -644,6 +644,91 @@ def run_tracers(args):
     print(json.dumps(line), flush=True)
 
 
+def validation_report(device, tgv_n=64, tgv_steps=50, drift_n=256, drift_steps=200):
+    """Accuracy figures of the plain form against the float64 oracle:
+    (1) relative L2 error per conserved field of the 3D TGV after fixed-dt
+        RK4 steps (both from the float32-rounded initial state);
+    (2) mass / momentum / energy drift of the 256^3 TGV over 200 steps (the
+        reference's plain sums);
+    (3) spectral convergence: the masked derivative of f = 1/(1.5 + cos 2 pi x)
+        (Fourier coefficients ~ 0.382^|k|) at N = 8..128, with the slope of
+        ln(error) per grid point from N = 16 to 32 (the 2/3 mask keeps
+        |k| <= N/3: asymptotic slope ln(0.382)/3 = -0.321);
+    (4) RK4 temporal order: the circularly polarized Alfven wave (m = 2,
+        N = 32, t = 1, filter off) through the 1D MHD kernel at dt = 0.02,
+        0.01, 0.005 against the exact solution."""
+    import torch
+    from oracle import mhd as M
+    from oracle import spectral as O
+    from phrike_gb300 import problems
+    from phrike_gb300.engine import Plan
+
+    def rl(a, b):
+        return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+    out = {}
+    n = tgv_n
+    U0 = problems.taylor_green_3d(n).astype(np.float32).astype(np.float64)
+    plan = Plan((n, n, n), (2 * np.pi,) * 3, device=device)
+    U = torch.as_tensor(U0, dtype=torch.float32, device=device)
+    plan.run_(U, tgv_steps, 1e-3)
+    s = O.EulerSolver(O.FourierBox((n, n, n), (2 * np.pi,) * 3, dealias=True), cfl=0.25)
+    R = U0.copy()
+    for _ in range(tgv_steps):
+        R = s.step(R, 1e-3)
+    G = U.double().cpu().numpy()
+    out["tgv_rel_l2"] = {"n": n, "steps": tgv_steps, "dt": 1e-3, "rho": rl(G[0], R[0]), "mom": rl(G[1:4], R[1:4]),
+                         "E": rl(G[4], R[4])}
+    n = drift_n
+    plan = Plan((n, n, n), (2 * np.pi,) * 3, device=device)
+    U = torch.as_tensor(problems.taylor_green_3d(n), dtype=torch.float32, device=device)
+    c0 = plan.conserved(U).double().cpu().numpy().reshape(-1)
+    plan.run_(U, drift_steps, 1e-3)
+    c1 = plan.conserved(U).double().cpu().numpy().reshape(-1)
+    scale = [abs(c0[0]), float(np.linalg.norm(c0[1:4])) + abs(c0[0]), abs(c0[4])]
+    out["tgv_drift"] = {"n": n, "steps": drift_steps, "mass": abs(c1[0] - c0[0]) / scale[0],
+                        "momentum": float(np.linalg.norm(c1[1:4] - c0[1:4])) / scale[1],
+                        "energy": abs(c1[4] - c0[4]) / scale[2]}
+    conv = {}
+    for N in (8, 16, 32, 64, 128):
+        x = np.arange(N) / N
+        f = 1.0 / (1.5 + np.cos(2 * np.pi * x))
+        df = 2 * np.pi * np.sin(2 * np.pi * x) / (1.5 + np.cos(2 * np.pi * x)) ** 2
+        p1 = Plan((N,), (1.0,), device=device)
+        d = p1.derivative(torch.as_tensor(f, dtype=torch.float32, device=device).reshape(1, N), 0)
+        ref = O.FourierBox((N,), (1.0,), dealias=True).deriv(f, 0)
+        conv[N] = {"gpu": rl(d.double().cpu().numpy().reshape(-1), df), "oracle": rl(ref, df)}
+    slope = {k: float(np.log(conv[32][k] / conv[16][k]) / 16.0) for k in ("gpu", "oracle")}
+    out["spectral_convergence"] = {"errors": conv, "slope_16_32": slope, "asymptotic_slope": float(np.log(1.5 - np.sqrt(1.25)) / 3)}
+    errs = []
+    for dt in (0.02, 0.01, 0.005):
+        p1 = Plan((32,), (1.0,), gamma=5.0 / 3.0, device=device, equations="mhd")
+        V = torch.as_tensor(problems.alfven_cp_1d(32, m=2), dtype=torch.float32, device=device).contiguous()
+        p1.project_state_(V)
+        p1.run_(V, int(round(1.0 / dt)), dt)
+        ex = problems.alfven_cp_1d(32, t=1.0, m=2)
+        errs.append(rl(V.double().cpu().numpy()[6:8], ex[6:8]))
+    so = M.MHDSolver1D(32, 1.0, gamma=5.0 / 3.0)
+    oerr = []
+    for dt in (0.02, 0.01):
+        W = so.project(problems.alfven_cp_1d(32, m=2))
+        for _ in range(int(round(1.0 / dt))):
+            W = so.step(W, dt)
+        oerr.append(rl(W[6:8], problems.alfven_cp_1d(32, t=1.0, m=2)[6:8]))
+    out["rk4_order"] = {"dt": [0.02, 0.01, 0.005], "gpu_errors": errs,
+                        "gpu_orders": [float(np.log2(errs[i] / errs[i + 1])) for i in range(2)],
+                        "oracle_errors": oerr, "oracle_order": float(np.log2(oerr[0] / oerr[1]))}
+    return out
+
+
+def run_validation(args):
+    import torch
+    from phrike_gb300 import _build
+    _build.build()
+    rep = validation_report(torch.device("cuda", 0))
+    print(json.dumps({"metric": "accuracy of the plain form against the float64 oracle", **rep}), flush=True)
+
+
 def run_adaptive(args):
     """Adaptive embedded RK45 with the reference's shipped settings.
     (a) configs/sod.yaml: 1D Sod N=1024, rk45, rtol 1e-6, atol 1e-8,
@@ -822,7 +907,7 @@ def run_serving(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", choices=["tgv", "ensemble", "lgl", "serving", "ot", "adaptive", "mhd3d",
-                                           "tracers"], default="tgv")
+                                           "tracers", "validation"], default="tgv")
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
@@ -872,6 +957,9 @@ def main():
         elif args.workload == "tracers":
             if rank == 0:
                 run_tracers(args)
+        elif args.workload == "validation":
+            if rank == 0:
+                run_validation(args)
         elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
