@@ -201,6 +201,44 @@ class Plan:
         _lib.check(self._lib.ps_step_rk4(self._handle, _ptr(U), float(dt), dptr, _stream(self.device)))
         return U
 
+    def step_host_stream(self, inputs: Sequence[torch.Tensor], outputs: Sequence[torch.Tensor], dt: float,
+                         nsteps: int = 1) -> None:
+        """Advance a stream of independent states held in pinned host memory:
+        output i = input i after ``nsteps`` RK4 steps of ``dt``.  The copy of
+        state i + 1 to the device and of state i - 1 back to the host overlap
+        the steps of state i (two device buffers, one copy stream per
+        direction; the steps themselves stay on the current stream, in order,
+        since they share the plan's scratch).  Returns when every output has
+        landed.  Inputs and outputs may repeat the same host tensors."""
+        if len(inputs) != len(outputs):
+            raise ValueError("inputs and outputs differ in length")
+        comp = torch.cuda.current_stream(self.device)
+        h2d, d2h = torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)
+        bufs, freed = [], [None, None]
+        for i, (hi, ho) in enumerate(zip(inputs, outputs)):
+            if not (hi.is_pinned() and ho.is_pinned()):
+                raise ValueError("host states must be in pinned memory")
+            b = i % 2
+            if len(bufs) <= b:
+                bufs.append(torch.empty(hi.shape, dtype=torch.float32, device=self.device))
+            with torch.cuda.stream(h2d):
+                if freed[b] is not None:
+                    h2d.wait_event(freed[b])
+                bufs[b].copy_(hi, non_blocking=True)
+                loaded = torch.cuda.Event()
+                loaded.record(h2d)
+            comp.wait_event(loaded)
+            self.run_(bufs[b], nsteps, dt) if nsteps > 1 else self.step_(bufs[b], dt)
+            stepped = torch.cuda.Event()
+            stepped.record(comp)
+            with torch.cuda.stream(d2h):
+                d2h.wait_event(stepped)
+                ho.copy_(bufs[b], non_blocking=True)
+                freed[b] = torch.cuda.Event()
+                freed[b].record(d2h)
+        d2h.synchronize()
+        comp.wait_stream(d2h)
+
     def run_(self, U: torch.Tensor, nsteps: int, dt: float = 0.0,
              dt_dev: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._check_state(U)

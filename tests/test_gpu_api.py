@@ -109,3 +109,20 @@ def test_2d_velocity_magnitude_sensor_raises_like_the_reference(cuda_device):
     with pytest.raises(ValueError):
         Plan((16, 16), (1.0, 1.0), av_config=av)
     Plan((64,), (1.0,), av_config=av)
+
+
+def test_step_host_stream_matches_steps(cuda_device):
+    """Pinned host states through step_host_stream equal each state stepped
+    on the device by step_ (same kernels, copies overlapped)."""
+    from phrike_gb300.engine import Plan
+    N = 32
+    plan = Plan((N, N, N), (2 * np.pi,) * 3, device=cuda_device)
+    rng = np.random.default_rng(4)
+    states = [problems.taylor_green_3d(N) * (1.0 + 0.05 * rng.random()) for _ in range(5)]
+    hin = [torch.as_tensor(s, dtype=torch.float32).pin_memory() for s in states]
+    hout = [torch.empty_like(h).pin_memory() for h in hin]
+    plan.step_host_stream(hin, hout, 1e-3, nsteps=2)
+    for h, o in zip(hin, hout):
+        U = h.to(cuda_device)
+        plan.run_(U, 2, 1e-3)
+        assert torch.equal(U.cpu(), o)
