@@ -12,10 +12,12 @@
 // per-axis weights K_a in shared memory (an N-point DFT of g_q = (c_q/N)
 // exp(2 pi i k_q x_p / L) per axis and tracer, phases reduced in float64),
 // then sweeps the field once, each warp over (row, segment) units with lanes
-// along x (coalesced), and accumulates Re(K_x K_y K_z f) for all its tracers.
+// along x (coalesced; a lane's points of a unit are loaded together), and
+// accumulates Re(K_x K_y K_z f) for all its tracers.
 // K_a is complex only through the unpaired Nyquist term (even N, dealias
 // off); K_x's imaginary part is carried only then (NYQX).  Partial sums are
-// float32 over one unit and float64 across units.
+// float32 over TR_FLUSH units, then summed across the warp and added to
+// float64 accumulators in shared memory.
 //
 // The velocity mode evaluates u_a = U[1+a] / U[0] on the fly (the primitive
 // velocity of equations.primitive) and, with pos/prev given, advances the
@@ -33,8 +35,7 @@ namespace {
 
 constexpr int TR_THREADS = 256;
 constexpr int TR_WARPS = TR_THREADS / 32;
-constexpr int TR_UNIT = 256;      // x points per (row, segment) unit
-constexpr int TR_FLUSH = 16;      // units summed in float32 before the float64 accumulator
+constexpr int TR_FLUSH = 16;      // units summed in float32 before the float64 accumulators
 constexpr int TR_MAXN = 8192;     // points per axis
 
 struct TracerArgs {
@@ -62,7 +63,7 @@ __device__ __forceinline__ double np_mod(double a, double b) {
   return r;
 }
 
-template <int TPC, bool NYQX>
+template <int TPC, bool NYQX, int MX>
 __global__ void __launch_bounds__(TR_THREADS) k_tracers(TracerArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
@@ -134,89 +135,84 @@ __global__ void __launch_bounds__(TR_THREADS) k_tracers(TracerArgs a) {
   }
   __syncthreads();  // the unit weights of missing axes
 
-  // ---- the sweep over the field
+  // ---- the sweep over the field: each warp takes (row, segment) units of up
+  // to 32 * MX points along x; lanes hold MX points each, loaded together
   const int rows = n1 * n2;
-  const int ux = min(n0, TR_UNIT);
+  const int ux = min(n0, 32 * MX);
   const int segs = (n0 + ux - 1) / ux;
-  const long units = (long)rows * segs;
+  const int units = rows * segs;
+  for (int i = tid; i < TR_WARPS * TPC * 3; i += blockDim.x) red[i] = 0.0;
+  __syncthreads();
   float sf[TPC][3];
-  double sd[TPC][3];
 #pragma unroll
   for (int t = 0; t < TPC; ++t)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      sf[t][c] = 0.0f;
-      sd[t][c] = 0.0;
-    }
-  int since = 0;
-  for (long u = warp; u < units; u += TR_WARPS) {
-    const int row = (int)(u / segs), seg = (int)(u - (long)row * segs);
-    const int jy = row % n1, jz = row / n1;
-    float pr[TPC][3], pi[TPC][3];
+    for (int c = 0; c < 3; ++c) sf[t][c] = 0.0f;
+  // float partials of TR_FLUSH units are summed across the warp's lanes and
+  // added to the warp's float64 accumulators in shared memory
+  auto flush = [&]() {
 #pragma unroll
     for (int t = 0; t < TPC; ++t)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        pr[t][c] = 0.0f;
-        pi[t][c] = 0.0f;
-      }
-#pragma unroll 1
-    for (int m = 0; m < (ux + 31) / 32; ++m) {
-      const int jx = seg * ux + 32 * m + lane;
-      if (jx >= n0 || jx >= (seg + 1) * ux) continue;
-      const long cell = (long)row * n0 + jx;
-      float v[3];
-      if (a.velocity) {
-        const float rinv = 1.0f / a.f[cell];
+        float v = sf[t][c];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) v[c] = (c < a.nf) ? a.f[(1 + c) * a.cells + cell] * rinv : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp * TPC * 3 + t * 3 + c] += (double)v;
+        sf[t][c] = 0.0f;
+      }
+  };
+  int since = 0;
+  for (int u = warp; u < units; u += TR_WARPS) {
+    const int row = (segs == 1) ? u : u / segs, seg = u - row * segs;
+    const int jz = row / n1, jy = row - jz * n1;
+    float v[MX][3];
+    int jxs[MX];
+#pragma unroll
+    for (int m = 0; m < MX; ++m) {
+      const int jx = seg * ux + 32 * m + lane;
+      const bool ok = jx < n0 && 32 * m + lane < ux;
+      jxs[m] = ok ? jx : -1;
+      const long cell = (long)row * n0 + (ok ? jx : 0);
+      if (a.velocity) {
+        const float rinv = ok ? 1.0f / a.f[cell] : 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[m][c] = (ok && c < a.nf) ? a.f[(1 + c) * a.cells + cell] * rinv : 0.0f;
       } else {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) v[c] = (c < a.nf) ? a.f[c * a.cells + cell] : 0.0f;
-      }
-#pragma unroll
-      for (int t = 0; t < TPC; ++t) {
-        if (NYQX) {
-          const float kr = Kx[(t * n0 + jx) * 2], ki = Kx[(t * n0 + jx) * 2 + 1];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            pr[t][c] = fmaf(v[c], kr, pr[t][c]);
-            pi[t][c] = fmaf(v[c], ki, pi[t][c]);
-          }
-        } else {
-          const float kr = Kx[t * n0 + jx];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) pr[t][c] = fmaf(v[c], kr, pr[t][c]);
-        }
+        for (int c = 0; c < 3; ++c) v[m][c] = (ok && c < a.nf) ? a.f[c * a.cells + cell] : 0.0f;
       }
     }
 #pragma unroll
     for (int t = 0; t < TPC; ++t) {
       const float2 wy = Ky[t * n1 + jy], wz = Kz[t * n2 + jz];
       const float wr = wy.x * wz.x - wy.y * wz.y, wi = wy.x * wz.y + wy.y * wz.x;
+      float pr[3] = {0.0f, 0.0f, 0.0f}, pi[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-      for (int c = 0; c < 3; ++c) sf[t][c] = fmaf(pr[t][c], wr, fmaf(-pi[t][c], wi, sf[t][c]));
+      for (int m = 0; m < MX; ++m) {
+        if (jxs[m] < 0) continue;
+        if (NYQX) {
+          const float kr = Kx[(t * n0 + jxs[m]) * 2], ki = Kx[(t * n0 + jxs[m]) * 2 + 1];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            pr[c] = fmaf(v[m][c], kr, pr[c]);
+            pi[c] = fmaf(v[m][c], ki, pi[c]);
+          }
+        } else {
+          const float kr = Kx[t * n0 + jxs[m]];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) pr[c] = fmaf(v[m][c], kr, pr[c]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sf[t][c] = fmaf(pr[c], wr, NYQX ? fmaf(-pi[c], wi, sf[t][c]) : sf[t][c]);
     }
     if (++since == TR_FLUSH) {
       since = 0;
-#pragma unroll
-      for (int t = 0; t < TPC; ++t)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          sd[t][c] += (double)sf[t][c];
-          sf[t][c] = 0.0f;
-        }
+      flush();
     }
   }
-#pragma unroll
-  for (int t = 0; t < TPC; ++t)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double v = sd[t][c] + (double)sf[t][c];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp * TPC * 3 + t * 3 + c] = v;
-    }
+  flush();
   __syncthreads();
   if (tid < TPC * 3) {
     const int t = tid / 3, c = tid % 3;
@@ -250,22 +246,35 @@ size_t tracer_smem(const TracerArgs& a, int tpc, bool nyqx) {
   return b;
 }
 
-template <int TPC, bool NYQX>
+template <int TPC, bool NYQX, int MX>
 cudaError_t launch_tracers_t(const TracerArgs& a, cudaStream_t s) {
   const size_t sm = tracer_smem(a, TPC, NYQX);
-  cudaError_t e = cudaFuncSetAttribute(k_tracers<TPC, NYQX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_tracers<TPC, NYQX, MX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   const int blocks = (a.np + TPC - 1) / TPC;
-  k_tracers<TPC, NYQX><<<blocks, TR_THREADS, sm, s>>>(a);
+  k_tracers<TPC, NYQX, MX><<<blocks, TR_THREADS, sm, s>>>(a);
   return cudaGetLastError();
 }
 
-// 4 tracers per CTA when their tables fit in 200 KB of shared memory, else 1
+template <int TPC, bool NYQX>
+cudaError_t launch_tracers_mx(const TracerArgs& a, cudaStream_t s) {
+  const int mx = (std::min(a.n[0], 256) + 31) / 32;  // points per lane and unit
+  if (mx <= 1) return launch_tracers_t<TPC, NYQX, 1>(a, s);
+  if (mx <= 2) return launch_tracers_t<TPC, NYQX, 2>(a, s);
+  if (mx <= 4) return launch_tracers_t<TPC, NYQX, 4>(a, s);
+  return launch_tracers_t<TPC, NYQX, 8>(a, s);
+}
+
+// 16 tracers per CTA (4 with the Nyquist term of x) when their tables fit in
+// 200 KB of shared memory, else 4, else 1
 cudaError_t launch_tracers(const TracerArgs& a, bool nyqx, cudaStream_t s) {
   if (a.np <= 0) return cudaSuccess;
-  const bool four = tracer_smem(a, 4, nyqx) <= 200 * 1024;
-  if (four) return nyqx ? launch_tracers_t<4, true>(a, s) : launch_tracers_t<4, false>(a, s);
-  return nyqx ? launch_tracers_t<1, true>(a, s) : launch_tracers_t<1, false>(a, s);
+  const size_t cap = 200 * 1024;
+  if (!nyqx && tracer_smem(a, 16, false) <= cap) return launch_tracers_mx<16, false>(a, s);
+  if (tracer_smem(a, 4, nyqx) <= cap)
+    return nyqx ? launch_tracers_mx<4, true>(a, s) : launch_tracers_mx<4, false>(a, s);
+  return nyqx ? launch_tracers_mx<1, true>(a, s) : launch_tracers_mx<1, false>(a, s);
 }
 
 int tracer_args(ps_plan p, TracerArgs& a) {
