@@ -190,8 +190,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   ring_init(S.ring);
   if (threadIdx.x == 0) {
-    // A pairs (c, c+1): G_c, G_c+1, Hy_c, Hy_c+1 (last pair single), then Hz pairs
-    const int order[15] = {0, 1, 5, 6, 2, 3, 7, 8, 4, 9, 10, 11, 12, 13, 14};
+    // A pairs (c, c+1) for c = 0, 2: G_c, G_c+1, Hy_c, Hy_c+1; Hz pairs for
+    // c = 0, 2; then G_4, Hz_4, Hy_4 for the merged last job
+    const int order[15] = {0, 1, 5, 6, 2, 3, 7, 8, 10, 11, 12, 13, 4, 14, 9};
     for (int i = 0; i < 15; ++i) S.ring.sched[i] = order[i];
     S.ring.ntiles = 15;
   }
@@ -205,13 +206,11 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
   const bool valid = col < a.g.ncol;
   int ti = 0;
 #pragma unroll 1
-  for (int c = 0; c < 5; c += 2) {
-    const bool two = c + 1 < 5;
+  for (int c = 0; c < 4; c += 2) {
     float2 w[B], z2[B];
-    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);  // G_c + i G_c+1
-    const int tb = ti + (two ? 2 : 1);
-    tile_pair<N, T>(z2, rc.wait(tb), two ? rc.wait(tb + 1) : nullptr, t, p);  // Hy_c + i Hy_c+1
-    ti = tb + (two ? 2 : 1);
+    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);       // G_c + i G_c+1
+    tile_pair<N, T>(z2, rc.wait(ti + 2), rc.wait(ti + 3), t, p);  // Hy_c + i Hy_c+1
+    ti += 4;
     rc.release(ti - 1);
     pf.fwd(w);
     pf.fwd(z2);
@@ -221,17 +220,16 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
         a.out[c * a.fs + base + n2 * step] = w[n2].x;
-        if (two) a.out[(c + 1) * a.fs + base + n2 * step] = w[n2].y;
+        a.out[(c + 1) * a.fs + base + n2 * step] = w[n2].y;
       }
     }
   }
 #pragma unroll 1
-  for (int c = 0; c < 5; c += 2) {
-    const bool two = c + 1 < 5;
+  for (int c = 0; c < 4; c += 2) {  // Hz_c + i Hz_c+1
     float2 w[B];
-    tile_pair<N, T>(w, rc.wait(ti), two ? rc.wait(ti + 1) : nullptr, t, p);
-    rc.release(ti + (two ? 1 : 0));
-    ti += two ? 2 : 1;
+    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
+    rc.release(ti + 1);
+    ti += 2;
     pf.fwd(w);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
@@ -244,7 +242,26 @@ __global__ void __launch_bounds__(Shape<N>::A * T, tma_min_blocks<N, T>())
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) {
         a.out[(5 + c) * a.fs + base + n2 * step] = w[n2].x;
-        if (two) a.out[(6 + c) * a.fs + base + n2 * step] = w[n2].y;
+        a.out[(6 + c) * a.fs + base + n2 * step] = w[n2].y;
+      }
+    }
+  }
+  {  // merged last job: FFT(G_4 + i Hz_4) and FFT(Hy_4); P on the first plus D on the
+     // second gives A_4 = P_y G_4 + D_y Hy_4 (real part) and B_4 = P_y Hz_4 (imaginary)
+    float2 w[B], z2[B];
+    tile_pair<N, T>(w, rc.wait(ti), rc.wait(ti + 1), t, p);
+    tile_pair<N, T>(z2, rc.wait(ti + 2), nullptr, t, p);
+    rc.release(ti + 2);
+    ti += 3;
+    pf.fwd(w);
+    pf.fwd(z2);
+    apply_pd<N, T>(w, z2, pf, S.ax, 1.0f);
+    pf.inv(w);
+    if (valid) {
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        a.out[4 * a.fs + base + n2 * step] = w[n2].x;
+        a.out[9 * a.fs + base + n2 * step] = w[n2].y;
       }
     }
   }
