@@ -257,6 +257,17 @@ int ps_apply_boundary_conditions(ps_plan plan, float* U, void* stream);
  * (grid.py:1297-1327). */
 int ps_project_solenoidal(ps_plan plan, float* Bx, float* By, void* stream);
 
+/* One-axis spectral operator on nf fields per solve (in place allowed):
+ * PS_OP_P applies mask x filter along `axis` (0 = x), PS_OP_D the masked
+ * derivative i k m s (Nyquist term dropped), PS_OP_L the masked second
+ * derivative -k^2 m s (Nyquist kept).  Products of one-axis operators give
+ * the grids' operators: dx1 = D_x P_y P_z, laplacian = L_x P_y P_z + P_x L_y P_z
+ * + P_x P_y L_z (grid.py:569-579, 1329-1338, 1696-1703). */
+#define PS_OP_P 0
+#define PS_OP_D 1
+#define PS_OP_L 2
+int ps_axis_op(ps_plan plan, int axis, int op, const float* f, float* out, int nfields, void* stream);
+
 /* The 3D projection of (Bx, By, Bz) in place for a 3D MHD plan: Nyquist
  * planes zeroed, B_hat -= k (k . B_hat)/|k|^2.  Replaces
  * Grid3D.project_solenoidal (grid.py:1649-1684). */

@@ -21,6 +21,7 @@ PS_EQ_EULER = 0
 PS_EQ_MHD = 1
 PS_AV_OFF, PS_AV_SENSOR, PS_AV_CONSTANT = 0, 1, 2
 PS_AV_Q_DENSITY, PS_AV_Q_PRESSURE, PS_AV_Q_SPEED = 0, 1, 2
+PS_OP_P, PS_OP_D, PS_OP_L = 0, 1, 2
 PS_SCHEME_RK4, PS_SCHEME_RK2 = 0, 1
 PS_GEMM_FP32 = 0
 PS_GEMM_FP64 = 1
@@ -118,6 +119,7 @@ _SIGNATURES = [
     ("ps_project_solenoidal", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_project_state", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_project_solenoidal_3d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_axis_op", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("ps_eval_points", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_tracers_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                   C.c_void_p, C.c_void_p]),

@@ -1353,6 +1353,15 @@ int ps_apply_boundary_conditions(ps_plan p, float* U, void* stream) {
   return PS_OK;
 }
 
+int ps_axis_op(ps_plan p, int axis, int op, const float* f, float* out, int nf, void* stream) {
+  if (!p || !f || !out) return fail(PS_ERR_INVALID, "null argument");
+  if (p->lgl) return fail(PS_ERR_UNSUPPORTED, "one-axis spectral operators need a Fourier plan");
+  if (axis < 0 || axis >= p->nd) return fail(PS_ERR_INVALID, "axis %d out of range", axis);
+  if (op < PS_OP_P || op > PS_OP_L) return fail(PS_ERR_INVALID, "op must be PS_OP_P, PS_OP_D or PS_OP_L");
+  if (nf < 1) return fail(PS_ERR_INVALID, "nf must be >= 1");
+  return apply_op(p, axis, f, out, nf, op, 1.0f, (cudaStream_t)stream);
+}
+
 int ps_project_solenoidal_3d(ps_plan p, float* Bx, float* By, float* Bz, void* stream) {
   if (!p || !Bx || !By || !Bz) return fail(PS_ERR_INVALID, "null argument");
   if (p->lgl || p->nd != 3 || p->H == nullptr)

@@ -310,6 +310,27 @@ class Plan:
                                            _stream(self.device)))
         return out
 
+    def axis_op(self, f: torch.Tensor, axis: int, op: str, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """One-axis operator along ``axis`` (0 = x): op "P" (mask x filter),
+        "D" (masked derivative) or "L" (masked second derivative)."""
+        ops = {"P": _lib.PS_OP_P, "D": _lib.PS_OP_D, "L": _lib.PS_OP_L}
+        nf = f.numel() // (self.cells * self.nsolve)
+        self._check_state(f, nf)
+        out = torch.empty_like(f) if out is None else out
+        _lib.check(self._lib.ps_axis_op(self._handle, int(axis), ops[op], _ptr(f), _ptr(out), nf,
+                                        _stream(self.device)))
+        return out
+
+    def laplacian(self, f: torch.Tensor) -> torch.Tensor:
+        """Sum over axes of L on that axis and P on the others."""
+        total = None
+        for a in range(self.ndim):
+            t = f
+            for b in range(self.ndim):
+                t = self.axis_op(t, b, "L" if b == a else "P")
+            total = t if total is None else total + t
+        return total
+
     def filter(self, f: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         nf = f.numel() // (self.cells * self.nsolve)
         self._check_state(f, nf)

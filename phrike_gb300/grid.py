@@ -163,6 +163,15 @@ class _FourierGridBase:
         shape = t.shape
         return self.plan.derivative(t.reshape((-1,) + self._shape), axis).reshape(shape)
 
+    def laplacian(self, f: Any) -> torch.Tensor:
+        """Masked spectral Laplacian Re IFFT(-|k|^2 m s FFT f) (grid.py:569-579,
+        1329-1338, 1696-1703)."""
+        if self._basis != "fourier":
+            raise ValueError("laplacian requires a Fourier basis")
+        t = self.to_device(f)
+        shape = t.shape
+        return self.plan.laplacian(t.reshape((-1,) + self._shape)).reshape(shape)
+
     def apply_spectral_filter(self, f: Any) -> torch.Tensor:
         t = self.to_device(f)
         shape = t.shape
@@ -393,6 +402,10 @@ class Grid3D(_FourierGridBase):
         v = [self.to_device(V).clone() for V in (Vx, Vy, Vz)]
         self._mhd_plan.project_solenoidal_3d_(*v)
         return v[0], v[1], v[2]
+
+    def curl(self, Vx: Any, Vy: Any, Vz: Any) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        """Curl with the masked derivatives (grid.py:1686-1694)."""
+        return (self.dy1(Vz) - self.dz1(Vy), self.dz1(Vx) - self.dx1(Vz), self.dx1(Vy) - self.dy1(Vx))
 
     def evaluate_fourier_at_points(self, f: Any, xp: Any, yp: Any, zp: Any) -> torch.Tensor:
         """f (Nz, Ny, Nx) at points (xp, yp, zp) (grid.py:1520-1567)."""
