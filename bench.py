@@ -294,21 +294,28 @@ def khi_ensemble_specs(nsolve: int, seed: int = 20261203, t_end: float = 1.0):
     return specs
 
 
-def run_ensemble(args):
+def run_ensemble(args, rank: int = 0, world: int = 1):
     """Ensemble solves/s: every solve to t_end in one batched, graph-captured
     run, against the same solves run one at a time (a per-size sample,
-    extrapolated by the size counts)."""
+    extrapolated by the size counts).  With N ranks the solve list is split
+    by instance (phrike_gb300.replicas.shard, cost ~ n^3: cells x CFL steps);
+    the run's time is the slowest rank's, and the plain form is N GPUs each
+    running its share one solve at a time."""
     import torch
     from phrike_gb300 import _build
     from phrike_gb300.engine import Plan
     from phrike_gb300.ensemble import Ensemble
     from phrike_gb300.equations import EulerEquations2D
     from phrike_gb300.grid import Grid2D
+    from phrike_gb300.replicas import reduce_max, shard
     from phrike_gb300.solver import SpectralSolver2D
 
     _build.build()
-    device = torch.device("cuda", 0)
-    specs = khi_ensemble_specs(args.nsolve, t_end=args.t_end)
+    device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(device)
+    all_specs = khi_ensemble_specs(args.nsolve, t_end=args.t_end)
+    mine = shard([float(sp.shape[0]) ** 3 for sp in all_specs], rank, world)
+    specs = [all_specs[i] for i in mine]
     # warm-up: the same groups for a short time, so that lazy kernel loading
     # (about 2 s for this library on first use) stays out of the timed run
     from phrike_gb300.ensemble import SolveSpec
@@ -316,18 +323,21 @@ def run_ensemble(args):
              device=device).run(chunk=args.chunk, use_graphs=True)
     torch.cuda.synchronize()
     ens = Ensemble(specs, cfl=0.4, device=device)
-    sampler = ClockSampler(0)
+    sampler = ClockSampler(device.index)
     sampler.start()
     stats = ens.run(chunk=args.chunk, use_graphs=True)
     clocks = sampler.stop()
+    seconds = reduce_max(stats["seconds"])
+    if rank != 0:
+        return
     # plain: one solve at a time, (a) device time loop, (b) host CFL loop as the reference's run()
     counts = {}
-    for sp in specs:
+    for sp in all_specs:
         counts[sp.shape[0]] = counts.get(sp.shape[0], 0) + 1
     plain_dev, plain_host = 0.0, 0.0
     sample = {}
     for n, cnt in sorted(counts.items()):
-        sp = next(x for x in specs if x.shape[0] == n)
+        sp = next(x for x in all_specs if x.shape[0] == n)
         plan = Plan(sp.shape, sp.lengths, cfl=0.4, device=device)
         U = torch.as_tensor(sp.U0, dtype=torch.float32, device=device).contiguous()
         t = torch.zeros(1, dtype=torch.float64, device=device)
@@ -351,19 +361,22 @@ def run_ensemble(args):
         plain_dev += cnt * td
         plain_host += cnt * th
         sample[str(n)] = {"solves": cnt, "device_loop_s": td, "host_loop_s": th}
+    plain_dev /= world  # N GPUs, each running its share plainly (balanced)
+    plain_host /= world
     line = {
-        "metric": "ensemble solves/s (batched vs plain, same GPU)", "value": stats["solves_per_s"],
-        "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
-        "data": "synthetic (seeded KHI initial conditions)",
+        "metric": "ensemble solves/s (batched vs plain, same GPU)", "value": args.nsolve / seconds,
+        "unit": "solves/s", "n_gpus": world, "higher_is_better": True, "dtype": "f32",
+        "scaling": "strong", "data": "synthetic (seeded KHI initial conditions)",
         "config": {"workload": f"{args.nsolve} KHI 2D solves, N uniform on 64..512, CFL 0.4, t_end={args.t_end}",
-                   "chunk_steps_per_graph": args.chunk},
-        "seconds": stats["seconds"], "graph_capture_seconds": stats["capture_seconds"],
-        "cell_updates_per_s": stats["cell_updates_per_s"],
+                   "chunk_steps_per_graph": args.chunk,
+                   "parallelism": f"replicas x{world}, solves split by instance" if world > 1 else "one GPU"},
+        "seconds": seconds, "graph_capture_seconds": stats["capture_seconds"],
+        "cell_updates_per_s": stats["cell_updates_per_s"] * (world if world > 1 else 1),
         "status": stats["status"],
         "plain_device_loop_solves_per_s": args.nsolve / plain_dev,
         "plain_host_loop_solves_per_s": args.nsolve / plain_host,
-        "speedup_vs_plain_device_loop": plain_dev / stats["seconds"],
-        "speedup_vs_plain_host_loop": plain_host / stats["seconds"],
+        "speedup_vs_plain_device_loop": plain_dev / seconds,
+        "speedup_vs_plain_host_loop": plain_host / seconds,
         "plain_sample": sample, "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -915,7 +928,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--n", "--size", dest="n", type=int, default=256)  # --size: unambiguous under torchrun
     ap.add_argument("--ot-n", type=int, default=512)
     ap.add_argument("--mhd3d-n", type=int, default=128)
     ap.add_argument("--tracer-n", type=int, default=64)
@@ -933,8 +946,7 @@ def main():
         dist.init_process_group(backend=backend)
     try:
         if args.workload == "ensemble":
-            if rank == 0:
-                run_ensemble(args)
+            run_ensemble(args, rank, world)
         elif args.workload == "lgl":
             if rank == 0:
                 run_lgl(args)
