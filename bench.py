@@ -320,9 +320,9 @@ def run_ensemble(args, rank: int = 0, world: int = 1):
     # (about 2 s for this library on first use) stays out of the timed run
     from phrike_gb300.ensemble import SolveSpec
     Ensemble([SolveSpec(sp.shape, sp.lengths, sp.U0, 1e-4) for sp in specs], cfl=0.4,
-             device=device).run(chunk=args.chunk, use_graphs=True)
+             device=device, autotune=True).run(chunk=args.chunk, use_graphs=True)
     torch.cuda.synchronize()
-    ens = Ensemble(specs, cfl=0.4, device=device)
+    ens = Ensemble(specs, cfl=0.4, device=device, autotune=True)  # tile widths measured (cached)
     sampler = ClockSampler(device.index)
     sampler.start()
     stats = ens.run(chunk=args.chunk, use_graphs=True)
@@ -371,6 +371,7 @@ def run_ensemble(args, rank: int = 0, world: int = 1):
                    "chunk_steps_per_graph": args.chunk,
                    "parallelism": f"replicas x{world}, solves split by instance" if world > 1 else "one GPU"},
         "seconds": seconds, "graph_capture_seconds": stats["capture_seconds"],
+        "tile_cols": {f"{k[0][0]}x{k[0][1]}": v for k, v in ens.tile_cols.items()},
         "cell_updates_per_s": stats["cell_updates_per_s"] * (world if world > 1 else 1),
         "status": stats["status"],
         "plain_device_loop_solves_per_s": args.nsolve / plain_dev,
@@ -868,8 +869,8 @@ def run_serving(args):
     # warm-up: one short request per (family, size) on a separate server with
     # the same group shapes, so that lazy kernel loading stays out of the timed run
     keys = sorted({(r.family, r.n) for r in reqs})
-    Server(device, chunk=args.chunk).serve([Request(-1 - i, f, n, 1e-4) for i, (f, n) in enumerate(keys)],
-                                          realtime=False)
+    Server(device, chunk=args.chunk, autotune=True).serve(
+        [Request(-1 - i, f, n, 1e-4) for i, (f, n) in enumerate(keys)], realtime=False)
     torch.cuda.synchronize()
     # plain service times, one alone run per (family, size); they also give the
     # server its cost model (long solves on high-priority streams)
@@ -879,7 +880,7 @@ def run_serving(args):
         run_alone(probe, device, chunk=args.chunk)  # warm-up (plan, kernels)
         _, sec = run_alone(probe, device, chunk=args.chunk)
         rate[key] = sec / args.plain_t_end
-    srv = Server(device, chunk=args.chunk, cost=lambda f, n: rate[(f, n)])
+    srv = Server(device, chunk=args.chunk, cost=lambda f, n: rate[(f, n)], autotune=True)
     sampler = ClockSampler(0)
     sampler.start()
     stats = srv.serve(reqs, realtime=True)

@@ -99,6 +99,11 @@ typedef struct {
    * wall), 2 leave unchanged (Grid1D.apply_boundary_conditions,
    * grid.py:620-735).  Default: walls, {0, 1, 0, 0, 1, 0}. */
   int lgl_bc1d[6];
+  /* 2D Fourier plans: columns per tile of the strided passes, 4, 8 or 16 (at
+   * most the plan's cap: 16 up to 256-point y pencils, 8 at 256-511 (Euler),
+   * 4 beyond); 0 (default): the plan's heuristic.  The arithmetic of a pencil
+   * does not depend on it; phrike_gb300/autotune.py picks it by timing. */
+  int tile_cols;
 } ps_plan_desc;
 
 #define PS_SCHEME_RK4 0
@@ -343,6 +348,9 @@ int ps_profile_collect(ps_plan plan, int nkinds, int* launches, double* ms, doub
  * stream. */
 #define PS_RHS_STATIC_MAX_CELLS 65536
 int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rhs, void* stream);
+
+/* Columns per strided-pass tile the plan uses (2D Fourier plans; 0 otherwise). */
+int ps_plan_tile_cols(ps_plan plan);
 
 /* Number of state components (ndim + 2 for Euler). */
 int ps_plan_ncomp(ps_plan plan);

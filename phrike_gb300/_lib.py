@@ -66,6 +66,7 @@ class PlanDesc(C.Structure):
         ("scheme", C.c_int),
         ("mhd_cfl_diff", C.c_double),
         ("lgl_bc1d", C.c_int * 6),
+        ("tile_cols", C.c_int),
     ]
 
 
@@ -109,6 +110,7 @@ _SIGNATURES = [
     ("ps_max_wave_speed", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_conserved", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_plan_ncomp", C.c_int, [C.c_void_p]),
+    ("ps_plan_tile_cols", C.c_int, [C.c_void_p]),
     ("ps_plan_status", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("ps_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),

@@ -1054,6 +1054,13 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
       }
     }
     if (p->mhd && p->n[1] >= 512 && p->tcols > 8) p->tcols = 8;  // 8-component last pass: 256 threads
+    if (d->tile_cols != 0) {  // explicit choice (autotuner): 4, 8 or 16, at most the cap
+      const int maxT = (p->mhd && p->n[1] >= 512) ? 8 : (p->n[1] >= 1024) ? 8 : cap;
+      if ((d->tile_cols != 4 && d->tile_cols != 8 && d->tile_cols != 16) || d->tile_cols > maxT)
+        return cleanup(fail(PS_ERR_INVALID, "tile_cols %d not allowed here (4..%d, powers of two)", d->tile_cols,
+                            maxT));
+      p->tcols = d->tile_cols;
+    }
   }
   if (d->av_mode != PS_AV_OFF && p->nd == 2 && (rc = dalloc(p, &p->av_buf, 21 * c)) != PS_OK) return cleanup(rc);
   if ((rc = dalloc(p, &p->speed, nsolve)) != PS_OK) return cleanup(rc);
@@ -1166,6 +1173,8 @@ int ps_plan_destroy(ps_plan p) {
 }
 
 int ps_plan_ncomp(ps_plan p) { return p ? p->nc : -1; }
+
+int ps_plan_tile_cols(ps_plan p) { return (p && p->nd == 2 && !p->lgl) ? p->tcols : 0; }
 
 int ps_plan_nsolve(ps_plan p) { return p ? p->nsolve : -1; }
 

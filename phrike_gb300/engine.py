@@ -54,7 +54,8 @@ class Plan:
                  cfl: Optional[float] = None, gravity: Optional[Sequence[float]] = None,
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
                  gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None,
-                 av_config: Optional[Dict] = None, scheme: str = "rk4", lgl_bc1d: Optional[Sequence[int]] = None):
+                 av_config: Optional[Dict] = None, scheme: str = "rk4", lgl_bc1d: Optional[Sequence[int]] = None,
+                 tile_cols: Optional[int] = None):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -123,6 +124,8 @@ class Plan:
             wts = av_config.get("variable_weights", None) or {}
             for c in range(5):
                 desc.av_weight[c] = float(wts.get(names[c], 1.0))
+        if tile_cols is not None:  # 2D strided-pass tile width (ps_plan_desc.tile_cols; autotune.py)
+            desc.tile_cols = int(tile_cols)
         if lgl_bc1d is not None:  # 1D Legendre boundary codes (ps_plan_desc.lgl_bc1d)
             for i, c in enumerate(lgl_bc1d):
                 desc.lgl_bc1d[i] = int(c)
@@ -309,6 +312,11 @@ class Plan:
         _lib.check(self._lib.ps_derivative(self._handle, int(axis), _ptr(f), _ptr(out), nf,
                                            _stream(self.device)))
         return out
+
+    @property
+    def tile_cols(self) -> int:
+        """Columns per strided-pass tile (2D Fourier plans; 0 otherwise)."""
+        return int(self._lib.ps_plan_tile_cols(self._handle))
 
     def axis_op(self, f: torch.Tensor, axis: int, op: str, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """One-axis operator along ``axis`` (0 = x): op "P" (mask x filter),

@@ -56,21 +56,30 @@ class Ensemble:
     filter are shared by all solves; grids may differ."""
 
     def __init__(self, specs: Sequence[SolveSpec], gamma: float = 1.4, cfl: float = 0.4, dealias: bool = True,
-                 filter_params: Optional[Dict] = None, device: Optional[torch.device] = None):
+                 filter_params: Optional[Dict] = None, device: Optional[torch.device] = None,
+                 autotune: bool = False):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.specs = list(specs)
         groups: Dict[Tuple, List[int]] = {}
         for i, s in enumerate(self.specs):
             groups.setdefault((tuple(s.shape), tuple(float(x) for x in s.lengths)), []).append(i)
         self.groups: List[_Group] = []
+        self.tile_cols: Dict[Tuple, int] = {}
+        t_tune = time.perf_counter()
         for (shape, lengths), idx in groups.items():
-            plan = Plan(shape, lengths, gamma=gamma, dealias=dealias, filter_params=filter_params, cfl=cfl,
-                        device=self.device, nsolve=len(idx))
             U = torch.as_tensor(np.stack([self.specs[i].U0 for i in idx]), dtype=torch.float32,
                                 device=self.device).contiguous()
+            kw = dict(gamma=gamma, dealias=dealias, filter_params=filter_params, cfl=cfl, device=self.device)
+            tc = None
+            if autotune and len(shape) == 2:  # measured strided-pass tile width (autotune.py)
+                from .autotune import tune_tile_cols
+                tc, _ = tune_tile_cols(shape, lengths, U, nsolve=len(idx), **kw)
+                self.tile_cols[(tuple(shape), tuple(lengths))] = tc
+            plan = Plan(shape, lengths, nsolve=len(idx), tile_cols=tc, **kw)
             t = torch.as_tensor([self.specs[i].t0 for i in idx], dtype=torch.float64, device=self.device)
             te = torch.as_tensor([self.specs[i].t_end for i in idx], dtype=torch.float64, device=self.device)
             self.groups.append(_Group(shape, lengths, idx, plan, U, t, te, torch.cuda.Stream(self.device)))
+        self.tune_seconds = time.perf_counter() - t_tune
 
     @property
     def cells(self) -> int:

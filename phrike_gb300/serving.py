@@ -122,11 +122,16 @@ class Request:
         return U
 
 
-def make_plan(family: str, n: int, nsolve: int, device) -> Plan:
+def _plan_kw(family: str, device) -> dict:
     o = FAMILIES[family]
-    return Plan(family_shape(family, n), family_lengths(family, n), gamma=o["gamma"], cfl=o["cfl"],
-                filter_params=o["filter"], device=device, nsolve=nsolve, basis=o.get("basis", "fourier"),
-                gemm_precision=o.get("gemm_precision", "fp32"), equations=o.get("equations", "euler"))
+    return dict(gamma=o["gamma"], cfl=o["cfl"], filter_params=o["filter"], device=device,
+                basis=o.get("basis", "fourier"), gemm_precision=o.get("gemm_precision", "fp32"),
+                equations=o.get("equations", "euler"))
+
+
+def make_plan(family: str, n: int, nsolve: int, device, tile_cols: Optional[int] = None) -> Plan:
+    return Plan(family_shape(family, n), family_lengths(family, n), nsolve=nsolve, tile_cols=tile_cols,
+                **_plan_kw(family, device))
 
 
 def _prepare_state(req: Request, device, projector: Optional[Plan]) -> torch.Tensor:
@@ -194,7 +199,7 @@ class Server:
     """
 
     def __init__(self, device=None, budget_bytes: Optional[int] = None, chunk: int = 20, slots=None,
-                 use_graphs: bool = True, cost=None, priority_seconds: float = 5.0):
+                 use_graphs: bool = True, cost=None, priority_seconds: float = 5.0, autotune: bool = False):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
@@ -209,6 +214,7 @@ class Server:
         # stream's makespan are slowed least by the short ones around them
         self.cost = cost
         self.priority_seconds = float(priority_seconds)
+        self.autotune = autotune  # measured strided-pass tile width for 2D Fourier groups (autotune.py)
         self.groups: List[_Group] = []
         self.used = 0
         self.projectors: Dict[int, Plan] = {}
@@ -243,10 +249,15 @@ class Server:
         need = self._group_bytes(family, n, slots)
         if self.used + need > self.budget:
             return None
-        plan = make_plan(family, n, slots, self.device)
         shape = family_shape(family, n)
         ben = _benign_state(family, shape, FAMILIES[family]["gamma"])
         U = torch.as_tensor(np.stack([ben] * slots), dtype=torch.float32, device=self.device).contiguous()
+        tc = None
+        if self.autotune and len(shape) == 2 and FAMILIES[family].get("basis", "fourier") == "fourier":
+            from .autotune import tune_tile_cols
+            tc, _ = tune_tile_cols(shape, family_lengths(family, n), U, nsolve=slots,
+                                   **_plan_kw(family, self.device))
+        plan = make_plan(family, n, slots, self.device, tile_cols=tc)
         t = torch.zeros(slots, dtype=torch.float64, device=self.device)
         te = torch.zeros(slots, dtype=torch.float64, device=self.device)  # t >= t_end: free
         high = self.cost is not None and float(self.cost(family, n)) >= self.priority_seconds

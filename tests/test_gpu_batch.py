@@ -119,3 +119,26 @@ def test_ensemble_uneven_sizes_graphs(cuda_device):
         t1 = torch.zeros(1, dtype=torch.float64, device=cuda_device)
         alone.run_cfl_(U1, 200, t1, torch.tensor([sp.t_end], dtype=torch.float64, device=cuda_device))
         assert rel_l2(ens.state(i).double().cpu().numpy(), U1.double().cpu().numpy()) < 1e-6
+
+
+def test_autotuned_tile_widths_change_speed_only(cuda_device):
+    """Every allowed strided-pass tile width gives the same state bit for bit
+    (the pencil arithmetic does not depend on it); the autotuner returns one
+    of them with its timing table."""
+    from phrike_gb300.autotune import tune_tile_cols
+    N, ns = 128, 4
+    U0 = np.stack([problems.kelvin_helmholtz_2d(N, N, U0=1.0 + 0.1 * i, A=0.01) for i in range(ns)])
+    U = dev(U0, cuda_device)
+    best, times = tune_tile_cols((N, N), (1.0, 1.0), U, nsolve=ns, cfl=0.4, device=cuda_device)
+    assert best in times and set(times) <= {4, 8, 16} and len(times) >= 2
+    outs = []
+    for T in sorted(times):
+        plan = Plan((N, N), (1.0, 1.0), cfl=0.4, device=cuda_device, nsolve=ns, tile_cols=T)
+        assert plan.tile_cols == T
+        V = U.clone()
+        plan.run_(V, 5, 1e-4)
+        outs.append(V)
+    for V in outs[1:]:
+        assert torch.equal(outs[0], V)
+    with pytest.raises(RuntimeError):
+        Plan((N, N), (1.0, 1.0), device=cuda_device, tile_cols=32)
