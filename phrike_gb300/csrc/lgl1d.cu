@@ -12,6 +12,7 @@
 // inside the step and again at the filter cadence.  The energy slot holds
 // E' = E - E_ref (the energy of the first node), an exact rewrite that keeps
 // float32 rounding relative to the field's variation.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "lgl1d.cuh"
@@ -245,6 +246,265 @@ __global__ void k_lgl1d_bc(float* U, int n, long ss, Bc1D bc, const int* active)
   bc_apply(U + (long)blockIdx.x * ss, n, bc.c, threadIdx.x);
 }
 
+// ---------------------------------------------------------------------------
+// Cluster form for 130..513 nodes (float32 contractions): a cluster of C CTAs
+// per solve, CTA r owning rows [r R, r R + R) of D (R = ceil(n / C) <= 65)
+// in its shared memory, so a stage reads no matrix from L2.  Every CTA keeps
+// the whole stage state and computes the flux of every node (cheap); it
+// evaluates k = -D F for its rows (one warp per row, lanes along the
+// columns), updates those rows, and writes them into every CTA's copy of the
+// state through distributed shared memory between two cluster barriers.
+// The boundary conditions, the CFL speed and the time loop are evaluated
+// identically in every CTA from identical data.  Same algorithm as k_lgl1d;
+// the column sums are split across lanes, so the two forms agree to float32
+// rounding rather than bit for bit (plans pick the form from n alone, so a
+// solve gives the same bits alone and in a batch).
+// ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+constexpr int CL_THREADS = 256;
+constexpr int CL_WARPS = CL_THREADS / 32;
+constexpr int CL_ROWS = 65;
+
+__host__ __device__ constexpr int cl_dl_floats(int n, int C) { return ((((n + C - 1) / C) * n + 3) / 4) * 4; }
+
+template <int C>
+__global__ void __launch_bounds__(CL_THREADS) k_lgl1d_cl(Lgl1DArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int sol = blockIdx.x / C;
+  if (a.active != nullptr && !a.active[sol]) return;  // the same for every CTA of the cluster
+  const int N = a.n;
+  const int R = (N + C - 1) / C;
+  const int i0 = rank * R, nr = max(0, min(N, i0 + R) - i0);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* Dl = reinterpret_cast<float*>(smem_raw);                          // [R][N] rows of D
+  Node4<float>* F = reinterpret_cast<Node4<float>*>(Dl + cl_dl_floats(N, C));  // [N]
+  float* us = reinterpret_cast<float*>(F + N);                             // [3][N] stage state
+  float* un = us + 3 * N;                                                  // [3][N] U^n
+  float* acc = un + 3 * N;                                                 // [3][R] own rows
+  float* mine = acc + 3 * R;                                               // [3][R] own new rows
+  float* kb = mine + 3 * R;                                                // [3][R] own k
+  __shared__ float red[32];
+  __shared__ int codes[6];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float* DT = static_cast<const float*>(a.DT);
+  const float* FT = static_cast<const float*>(a.FT);
+  float* U = a.U + (long)sol * a.solve_stride;
+  if (tid < 6) codes[tid] = a.bc.c[tid];
+  for (int idx = tid; idx < R * N; idx += CL_THREADS) {  // Dl[r][j] = D[i0 + r][j] = DT[j][i0 + r]
+    const int j = idx / R, r = idx - j * R;
+    Dl[r * N + j] = (r < nr) ? DT[(long)j * N + i0 + r] : 0.0f;
+  }
+  const float er = U[2 * N];
+  for (int i = tid; i < 3 * N; i += CL_THREADS) {
+    float v = U[i];
+    if (i >= 2 * N) v -= er;
+    un[i] = v;
+    us[i] = v;
+  }
+  cluster.sync();  // every CTA has read the state before any CTA writes its rows back
+  const float g1 = a.gamma - 1.0f;
+  const float href = a.gamma * er;
+  const float pmin_shift = a.p_min - g1 * er;
+
+  auto flux = [&]() {
+    for (int j = tid; j < N; j += CL_THREADS) {
+      const float rho = us[j], m = us[N + j], E = us[2 * N + j];
+      const float u = m / rho;
+      const float p = g1 * (E - 0.5f * rho * u * u);
+      F[j] = Node4<float>{m, m * u + p, ((E + p) + href) * u, 0.0f};
+    }
+  };
+  // kb = -(D F)_i (+ gravity) for the own rows, summed as D_ij (F_j - F_i)
+  auto own_rhs = [&]() {
+    for (int r = warp; r < nr; r += CL_WARPS) {
+      const int i = i0 + r;
+      const Node4<float> fi = F[i];
+      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+      const float* drow = Dl + r * N;
+      for (int j = lane; j < N; j += 32) {
+        const float d = drow[j];
+        const Node4<float> fj = F[j];
+        s0 = fmaf(d, fj.v0 - fi.v0, s0);
+        s1 = fmaf(d, fj.v1 - fi.v1, s1);
+        s2 = fmaf(d, fj.v2 - fi.v2, s2);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      }
+      if (lane == 0) {
+        float k1 = -s1, k2 = -s2;
+        if (a.gx != 0.0f) {  // gravity source (solver.py:82-91)
+          const float rho = us[i], u = us[N + i] / rho;
+          k1 += rho * a.gx;
+          k2 += rho * a.gx * u;
+        }
+        kb[r] = -s0;
+        kb[R + r] = k1;
+        kb[2 * R + r] = k2;
+      }
+    }
+  };
+  // own new rows (mine) into every CTA's stage state
+  auto exchange = [&]() {
+    cluster.sync();  // every CTA has finished reading its stage state
+    for (int idx = tid; idx < C * 3 * nr; idx += CL_THREADS) {
+      const int q = idx / (3 * nr), rem = idx - q * 3 * nr, c = rem / nr, r = rem - c * nr;
+      float* dst = cluster.map_shared_rank(us, q);
+      dst[c * N + i0 + r] = mine[c * R + r];
+    }
+    cluster.sync();  // the new state is visible everywhere
+  };
+  auto filter_bc = [&]() {
+    if (FT != nullptr) {  // own rows of F u, summed as u_i + F_ij (u_j - u_i)
+      for (int r = tid; r < nr; r += CL_THREADS) {
+        const int i = i0 + r;
+        const float f0 = us[i], f1 = us[N + i], f2 = us[2 * N + i];
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+        for (int j = 0; j < N; ++j) {
+          const float f = FT[(long)j * N + i];
+          s0 = fmaf(f, us[j] - f0, s0);
+          s1 = fmaf(f, us[N + j] - f1, s1);
+          s2 = fmaf(f, us[2 * N + j] - f2, s2);
+        }
+        mine[r] = f0 + s0;
+        mine[R + r] = f1 + s1;
+        mine[2 * R + r] = f2 + s2;
+      }
+      exchange();
+    }
+    bc_apply(us, N, codes, tid);
+    __syncthreads();
+  };
+
+  if (a.rhs_out != nullptr) {  // rhs only
+    bc_apply(us, N, codes, tid);
+    __syncthreads();
+    flux();
+    __syncthreads();
+    own_rhs();
+    __syncthreads();
+    float* Rh = a.rhs_out + (long)sol * a.solve_stride;
+    for (int idx = tid; idx < 3 * nr; idx += CL_THREADS) {
+      const int c = idx / nr, r = idx - c * nr;
+      Rh[c * N + i0 + r] = kb[c * R + r];
+    }
+    cluster.sync();  // no CTA leaves while others may map its shared memory
+    return;
+  }
+
+  float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
+  double tl = (a.t != nullptr) ? a.t[sol] : 0.0;
+  const double te = (a.tend != nullptr) ? a.tend[sol] : 0.0;
+  int taken = 0;
+  const int cad0 = (a.steps_done != nullptr) ? a.steps_done[sol] : a.step_counter0;
+#pragma unroll 1
+  for (int step = 0; step < a.nsteps; ++step) {
+    double dtd = dt;
+    if (a.t != nullptr) {  // CFL step size from the state as given (identical in every CTA)
+      if (tl >= te - 1e-12) break;
+      float sm = 0.0f;
+      for (int i = tid; i < N; i += CL_THREADS) {
+        const float rho = un[i], u = un[N + i] / rho;
+        const float pp = g1 * (un[2 * N + i] - 0.5f * rho * u * u) + g1 * er;
+        sm = fmaxf(sm, fabsf(u) + sqrtf(a.gamma * pp / rho));
+      }
+      sm = block_max(sm, red);
+      if (tid == 0) red[0] = sm;
+      __syncthreads();
+      const double spd = (double)red[0];
+      __syncthreads();
+      dtd = (spd <= 0.0) ? 1e-6 : (double)a.cfl * (double)a.hmin / spd;
+      dtd = fmin(dtd, te - tl);
+      dt = (float)dtd;
+    }
+#pragma unroll 1
+    for (int stage = 0; stage < 4; ++stage) {
+      if (a.rk2 && (stage == 1 || stage == 2)) continue;
+      const RKCoef rc = rk_coef(stage, dt, a.rk2);
+      bc_apply(us, N, codes, tid);
+      __syncthreads();
+      if (stage == 0) {
+        for (int i = tid; i < 3 * N; i += CL_THREADS) un[i] = us[i];
+        __syncthreads();
+      }
+      flux();
+      __syncthreads();
+      own_rhs();
+      __syncthreads();
+      for (int r = tid; r < nr; r += CL_THREADS) {
+        float u3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int s = c * N + i0 + r;
+          const float k = kb[c * R + r];
+          if (stage == 3) {
+            u3[c] = fmaf(rc.wacc, k, acc[c * R + r]);
+          } else {
+            const float v = un[s];
+            acc[c * R + r] = fmaf(rc.wacc, k, (stage == 0) ? v : acc[c * R + r]);
+            u3[c] = fmaf(rc.wnext, k, v);
+          }
+        }
+        clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
+        mine[r] = u3[0];
+        mine[R + r] = u3[1];
+        mine[2 * R + r] = u3[2];
+      }
+      exchange();
+    }
+    filter_bc();  // inside the step (_rk4_step -> _apply_physical_filters)
+    if (((cad0 + step) % a.filter_interval) == 0) filter_bc();  // cadence
+    for (int i = tid; i < 3 * N; i += CL_THREADS) un[i] = us[i];
+    __syncthreads();
+    tl += dtd;
+    ++taken;
+  }
+  if (rank == 0 && tid == 0) {
+    if (a.t != nullptr) a.t[sol] = tl;
+    if (a.steps_done != nullptr) a.steps_done[sol] += taken;
+  }
+  for (int idx = tid; idx < 3 * nr; idx += CL_THREADS) {
+    const int c = idx / nr, r = idx - c * nr;
+    const int i = c * N + i0 + r;
+    U[i] = un[i] + (c == 2 ? er : 0.0f);
+  }
+  cluster.sync();  // no CTA leaves while others may map its shared memory
+}
+
+size_t cl_smem(int n, int C) {
+  const int R = (n + C - 1) / C;
+  return sizeof(float) * (size_t)cl_dl_floats(n, C) + 16 * (size_t)n + sizeof(float) * (6 * (size_t)n + 9 * (size_t)R);
+}
+
+template <int C>
+cudaError_t launch_lgl1d_cl(const Lgl1DArgs& a, int nsolve, cudaStream_t s) {
+  const size_t sm = cl_smem(a.n, C);
+  cudaError_t e = cudaFuncSetAttribute(k_lgl1d_cl<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nsolve * C));
+  cfg.blockDim = dim3(CL_THREADS);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, k_lgl1d_cl<C>, &cfg) != cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return cudaErrorInvalidClusterSize;  // cannot be placed on this device: the caller falls back
+  }
+  return cudaLaunchKernelEx(&cfg, k_lgl1d_cl<C>, a);
+}
+
 }  // namespace
 
 size_t lgl1d_smem(int n, bool fp64) { return (size_t)4 * n * (fp64 ? 8 : 4) + (size_t)9 * n * 4; }
@@ -253,7 +513,16 @@ size_t lgl1d_smem(int n, bool fp64) { return (size_t)4 * n * (fp64 ? 8 : 4) + (s
 // spread evenly and the column loads of D^T have many warps in flight
 static int lgl1d_threads(int n) { return n >= 1024 ? 1024 : ((n + 31) / 32) * 32; }
 
+// clusters of 4 CTAs for 130..257 nodes and 8 for 258..513 (float32), from n alone
+static int lgl1d_cluster(int n, bool fp64) { return (fp64 || n < 130 || n > 8 * CL_ROWS) ? 0 : (n <= 4 * CL_ROWS ? 4 : 8); }
+
 cudaError_t launch_lgl1d(const Lgl1DArgs& a, bool fp64, int nsolve, cudaStream_t s) {
+  const int C = lgl1d_cluster(a.n, fp64);
+  if (C > 0) {
+    const cudaError_t e = (C == 4) ? launch_lgl1d_cl<4>(a, nsolve, s) : launch_lgl1d_cl<8>(a, nsolve, s);
+    if (e != cudaErrorInvalidClusterSize) return e;
+    cudaGetLastError();  // clusters of this shape cannot be placed here: one CTA per solve
+  }
   const size_t sm = lgl1d_smem(a.n, fp64);
   cudaError_t e;
   if (fp64) {

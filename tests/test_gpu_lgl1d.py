@@ -188,3 +188,50 @@ def test_lgl1d_large_grid_properties(cuda_device):
     assert abs(m1 - m0) / m0 < 1e-5
     assert G[1][0] == 0.0 and G[1][-1] == 0.0
     assert p.status() == 0
+
+
+@pytest.mark.parametrize("n", [257, 513])
+@pytest.mark.parametrize("tag", ["wall", "mixed"])
+def test_lgl1d_cluster_form_vs_oracle(cuda_device, n, tag):
+    """130..513 nodes in float32 run as a cluster of CTAs per solve (rows of D
+    in each CTA's shared memory, the stage state exchanged through
+    distributed shared memory): rhs, 20 steps and a CFL run against the
+    float64 oracle with the case's boundary map, filter, scheme and gravity."""
+    import torch
+    from phrike_gb300.engine import Plan
+    c = CASES[tag]
+    codes = L.bc_codes_1d(c["bc"] if c["bc"] is not None else "dirichlet").reshape(-1).tolist()
+    gravity = [c["gravity"]] if c["gravity"] is not None else None
+    mk = lambda cfl=0.4: Plan((n,), (LENGTH,), gamma=GAMMA, filter_params=c["filter_params"], cfl=cfl,  # noqa: E731
+                              basis="legendre", lgl_bc1d=codes, scheme=c["scheme"], gravity=gravity)
+    o = L.LGLSolver1D(n, LENGTH, gamma=GAMMA, filter_params=c["filter_params"], cfl=0.4,
+                      bc=c["bc"] if c["bc"] is not None else "dirichlet", gravity=c["gravity"], scheme=c["scheme"])
+    U0 = initial_state(o.ax.x)
+    r = mk().rhs(_dev(U0)).cpu().numpy()
+    ro = o.rhs(U0.copy())
+    for k in range(3):
+        assert rel_l2(r[k], ro[k]) < 3e-5 * (n / 257), (k, rel_l2(r[k], ro[k]))
+    dt = 0.2 * o.compute_dt(U0)
+    R = U0.copy()
+    for _ in range(20):
+        R = o.step(R, dt)
+    p = mk()
+    U = _dev(U0)
+    p.run_(U, 20, dt)
+    G = U.cpu().numpy()
+    assert max(rel_l2(G[0], R[0]), rel_l2(G[2], R[2])) < 5e-6
+    assert rel_l2(G[1], R[1]) < 1e-4, rel_l2(G[1], R[1])
+    assert p.status() == 0
+    # CFL loop to a short end time, and a batch of two that matches the solve alone
+    t_end = 10 * o.compute_dt(U0)
+    pb = Plan((n,), (LENGTH,), gamma=GAMMA, filter_params=c["filter_params"], cfl=0.4, basis="legendre",
+              lgl_bc1d=codes, scheme=c["scheme"], gravity=gravity, nsolve=2)
+    Ub = _dev(np.stack([U0, U0 * np.array([1.05, 1.0, 1.05])[:, None]]))
+    tb = torch.zeros(2, dtype=torch.float64, device="cuda")
+    pb.run_cfl_(Ub, 40, tb, torch.full((2,), t_end, dtype=torch.float64, device="cuda"))
+    p1 = mk()
+    U1 = _dev(U0)
+    t1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    p1.run_cfl_(U1, 40, t1, torch.full((1,), t_end, dtype=torch.float64, device="cuda"))
+    assert torch.equal(U1, Ub[0]) and abs(float(t1.item()) - t_end) < 1e-12
+    assert pb.steps_done()[0] == p1.steps_done()[0]
