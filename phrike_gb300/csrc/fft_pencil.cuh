@@ -11,7 +11,7 @@
 // The inverse runs the same steps backwards and returns to the input layout,
 // so a forward/multiply/inverse round trip never reorders data in memory.
 //
-// All in-register DFTs are radix-2 decimation-in-frequency with compile-time
+// All in-register DFTs are radix-2 decimation-in-time with compile-time
 // twiddles; the constants are produced at compile time by a Taylor series
 // after octant reduction (see ct_cos2pi / ct_sin2pi).
 #pragma once
@@ -112,27 +112,53 @@ __device__ __forceinline__ float2 twmul(float2 d) {
   }
 }
 
+// Radix-2 decimation-in-time butterfly a, b -> a + W b, a - W b with the
+// compile-time twiddle W = exp(-+ 2 pi i J / M) = c + i s.  A nontrivial W
+// is applied as W b = w * u with u = b + i tau b (two FMAs) and the scale w
+// folded into the butterfly (four FMAs): six instructions instead of the
+// eight of a complex multiply and two complex adds.  tau = s/c, w = c when
+// |c| >= |s|, else tau = c/s, w = s, so |tau| <= 1.
+template <int M, int J, bool INV>
+__device__ __forceinline__ void bfly_dit(float2& a, float2& b) {
+  const float2 x = a;
+  if constexpr (J == 0 || 4 * J == M) {
+    const float2 wb = twmul<M, J, INV>(b);
+    a = cadd(x, wb);
+    b = csub(x, wb);
+  } else {
+    constexpr double cd = ct_cos2pi(J, M);
+    constexpr double sd = INV ? ct_sin2pi(J, M) : -ct_sin2pi(J, M);
+    constexpr bool by_c = (cd < 0 ? -cd : cd) >= (sd < 0 ? -sd : sd);
+    constexpr float tau = by_c ? float(sd / cd) : float(cd / sd);
+    constexpr float w = by_c ? float(cd) : float(sd);
+    float2 u;
+    if constexpr (by_c) u = make_float2(fmaf(-tau, b.y, b.x), fmaf(tau, b.x, b.y));
+    else u = make_float2(fmaf(tau, b.x, -b.y), fmaf(tau, b.y, b.x));
+    a = make_float2(fmaf(w, u.x, x.x), fmaf(w, u.y, x.y));
+    b = make_float2(fmaf(-w, u.x, x.x), fmaf(-w, u.y, x.y));
+  }
+}
+
 // In-register DFT of L points starting at v[OFF]; natural order in and out.
+// Radix-2 decimation in time: the bit-reversed input order is a compile-time
+// renaming of registers, then log2(L) butterfly stages.
 template <int L, bool INV, int OFF = 0, int CAP>
 __device__ __forceinline__ void dft(float2 (&v)[CAP]) {
   if constexpr (L > 1) {
     constexpr int LOG = ilog2(L);
-    sfor<0, LOG>([&](auto sc) {
-      constexpr int span = L >> (decltype(sc)::value + 1);
-      sfor<0, L / (2 * span)>([&](auto gc) {
-        constexpr int start = OFF + decltype(gc)::value * 2 * span;
-        sfor<0, span>([&](auto jc) {
-          constexpr int j = decltype(jc)::value;
-          float2 a = v[start + j];
-          float2 b = v[start + j + span];
-          v[start + j] = cadd(a, b);
-          v[start + j + span] = twmul<2 * span, j, INV>(csub(a, b));
-        });
-      });
-    });
     float2 tmp[L];
     sfor<0, L>([&](auto ic) { tmp[decltype(ic)::value] = v[OFF + bitrev(decltype(ic)::value, LOG)]; });
     sfor<0, L>([&](auto ic) { v[OFF + decltype(ic)::value] = tmp[decltype(ic)::value]; });
+    sfor<0, LOG>([&](auto sc) {
+      constexpr int h = 1 << decltype(sc)::value;
+      sfor<0, L / (2 * h)>([&](auto gc) {
+        constexpr int start = OFF + decltype(gc)::value * 2 * h;
+        sfor<0, h>([&](auto jc) {
+          constexpr int j = decltype(jc)::value;
+          bfly_dit<2 * h, j, INV>(v[start + j], v[start + j + h]);
+        });
+      });
+    });
   }
 }
 
