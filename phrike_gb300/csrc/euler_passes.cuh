@@ -90,6 +90,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
   const float pref = (a.gamma - 1.0f) * er;
   const float href = a.gamma * er;
   const float g1 = a.gamma - 1.0f;
+  const float ig1 = 1.0f / g1;  // one division per thread instead of one per energy flux
   float q[NC][B];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
       float kin = 0.0f;
 #pragma unroll
       for (int d = 0; d < ND; ++d) kin = fmaf(q[1 + d][n2], q[1 + d][n2], kin);
-      const float Ep = pr / g1 + 0.5f * rho * kin;  // E' = E - E_ref
+      const float Ep = fmaf(pr, ig1, 0.5f * rho * kin);  // E' = E - E_ref
       return ((Ep + pr) + href) * ua;              // (E + p) u_dir
     }
     const float rv = rho * ua * q[c][n2];
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst(XFirstArgs a) {
         const float pr = g1 * (q[NC - 1][n2] - 0.5f * rho * kin);
         q[NC - 1][n2] = pr;
         if (a.speed != nullptr && valid) {
-          const float cs = sqrtf(a.gamma * (pr + pref) / rho);
+          const float cs = sqrtf(a.gamma * (pr + pref) * rinv);
           float um = fabsf(vel[0]);
           if (ND == 3) um = fmaxf(um, fmaxf(fabsf(vel[1]), fabsf(vel[ND - 1])));
           // 2D keeps |u_x| + a only (equations.py:137-147)
