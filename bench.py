@@ -60,16 +60,18 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_from_profiles(kind: str):
-    """DRAM bytes per launch of a pass kind, from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "tgv256_passes.md")
-    try:
-        for line in open(path):
-            if line.startswith(f"traffic_bytes_per_launch[{kind}]"):
-                return float(line.split(":", 1)[1].strip())
-    except OSError:
-        pass
-    return None
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# pass kernels of a TGV 256^3 RK4 step, averaged over the step's launches,
+# from ncu captures of the bench command (x pass at 256^3; y and last pass
+# at 128^3, reads scaled by the 8x cell count, writes at their algorithmic
+# size, which every write reaches at 256^3).
+NCU_TRAFFIC_TGV256 = {"x_pass": 1.366e9, "y_pass": 1.678e9, "last_pass": 1.762e9}
+
+
+def traffic_per_launch(kind: str, n: int):
+    if kind not in NCU_TRAFFIC_TGV256 or n != 256:
+        return None
+    return NCU_TRAFFIC_TGV256[kind]
 
 
 class ClockSampler:
@@ -247,7 +249,7 @@ def run_gb300(args, rank: int, world: int):
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-        "traffic": traffic_from_profiles(dom), "algorithmic_bytes_per_launch": per_launch_bytes,
+        "traffic": traffic_per_launch(dom, n), "algorithmic_bytes_per_launch": per_launch_bytes,
         "launch_ms": per_launch_ms,
         "kernels": {k: {"launches": v["launches"], "share": v["ms"] / total_ms,
                         "achieved_GBps": v["bytes"] / (v["ms"] * 1e-3) / 1e9}

@@ -132,11 +132,42 @@ class FourierBox:
         k2 = sum(self._kview(a) ** 2 for a in range(self.ndim))
         return ifftn(-k2 * F, self.axes).real
 
-    def filt(self, f: np.ndarray) -> np.ndarray:
+    def filt(self, f: np.ndarray, real: bool = False) -> np.ndarray:
         """apply_spectral_filter: Re IFFT(mask * sigma * FFT f) (grid.py:524-538,
-        1254-1287, 1723-1726)."""
+        1254-1287, 1723-1726).  ``real``: the same operator through real
+        half-spectrum transforms (equal up to rounding, since mask * sigma is
+        real and even in k)."""
+        if real and _fft is not None:
+            F = _fft.rfftn(f, axes=self.axes, workers=_workers()) * self.mult[..., : self.shape[-1] // 2 + 1]
+            return _fft.irfftn(F, s=self.shape, axes=self.axes, workers=_workers())
         F = fftn(f, self.axes) * self.mult
         return ifftn(F, self.axes).real
+
+    def flux_divergence(self, F: Sequence[np.ndarray]) -> np.ndarray:
+        """sum_d dx1_d F_d with F indexed by direction (0 = x), evaluated as
+        one spectral sum: IFFT(sum_d i k_d m s FFT F_d).
+
+        The same operator as sum_d deriv(F_d, axis(d)) (grid.py:512-519,
+        1226-1252, 1705-1721) by linearity; with the 2/3 mask every Nyquist
+        mode is zero, so real half-spectrum transforms give the reference's
+        real part exactly up to rounding.  Used for large-grid oracle runs
+        (three forward and one inverse real transform per stage instead of
+        three full complex round trips); ``tests/test_oracle_golden.py``
+        checks it against ``deriv``.
+        """
+        if not self.dealias or _fft is None:
+            return sum(self.deriv(Fd, self.ndim - 1 - d) for d, Fd in enumerate(F))
+        nh = self.shape[-1] // 2 + 1
+        mult = self.mult[..., :nh]
+        acc = None
+        for d, Fd in enumerate(F):
+            a = self.ndim - 1 - d
+            kv = self._kview(a)
+            if a == self.ndim - 1:
+                kv = kv[..., :nh]
+            S = _fft.rfftn(Fd, axes=self.axes, workers=_workers()) * (1j * kv)
+            acc = S if acc is None else acc + S
+        return _fft.irfftn(acc * mult, s=self.shape, axes=self.axes, workers=_workers())
 
 
 # ---------------------------------------------------------------------------
@@ -240,6 +271,7 @@ class EulerSolver:
     step_counter: int = 0
     av: Optional[Dict] = None  # artificial-viscosity config (1D/2D), see av_terms
     scheme: str = "rk4"        # "rk4" or the midpoint "rk2"
+    fused: bool = False        # one spectral sum per stage (FourierBox.flux_divergence)
 
     @property
     def ndim(self) -> int:
@@ -299,9 +331,12 @@ class EulerSolver:
 
     def rhs(self, U: np.ndarray) -> np.ndarray:
         F = fluxes(U, self.gamma)
-        r = np.zeros_like(U)
-        for a, Fa in enumerate(F):
-            r -= self.box.deriv(Fa, self.flux_axis_index(a))
+        if self.fused:
+            r = -self.box.flux_divergence(F)
+        else:
+            r = np.zeros_like(U)
+            for a, Fa in enumerate(F):
+                r -= self.box.deriv(Fa, self.flux_axis_index(a))
         if self.av is not None and self.ndim < 3:
             r += self.av_terms(U)
         if self.gravity is not None:
@@ -334,7 +369,7 @@ class EulerSolver:
         Un = U + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4)
         Un = self.clamp(Un)
         if self.ndim == 1:
-            Un = self.box.filt(Un)  # inside _rk4_step (solver.py:119-120)
+            Un = self.box.filt(Un, self.fused)  # inside _rk4_step (solver.py:119-120)
         return Un
 
     def rk2(self, U: np.ndarray, dt: float) -> np.ndarray:
@@ -351,9 +386,9 @@ class EulerSolver:
     def step(self, U: np.ndarray, dt: float) -> np.ndarray:
         Un = self.rk2(U, dt) if self.scheme == "rk2" else self.rk4(U, dt)
         if self.ndim == 3:
-            Un = self.box.filt(Un)  # every step (solver.py:1336)
+            Un = self.box.filt(Un, self.fused)  # every step (solver.py:1336)
         elif self.step_counter % self.filter_interval == 0:
-            Un = self.box.filt(Un)  # cadence (solver.py:265-267, 645-646)
+            Un = self.box.filt(Un, self.fused)  # cadence (solver.py:265-267, 645-646)
         self.step_counter += 1
         return Un
 

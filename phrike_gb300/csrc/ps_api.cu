@@ -205,6 +205,29 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }  // namespace
 
 namespace ps {
+// Plan descriptor checks shared by ps_plan_create / ps_batch_create and the
+// allocation-free ps_rhs_static.
+int validate_desc(const ps_plan_desc* d) { return validate(d); }
+
+// Columns per strided-pass tile of a 2D Fourier grid (nx, ny: points along x
+// and y): the widest of 16, 8, 4 that still gives about two CTAs per SM
+// (small grids get more, narrower CTAs).  2D Euler: the clamped last pass
+// runs at ~168 registers without spills with 128-thread CTAs (8 columns of
+// 16-thread pencils at N <= 256, 4 columns at 512 and up) and three CTAs per
+// SM; the 8-component MHD last pass takes at most 8 columns from 512 rows up.
+int tile_cols_2d(int nx, int ny, int nsolve, bool mhd) {
+  const int cap = mhd ? ((ny >= 1024) ? 8 : 16) : ((ny >= 512) ? 4 : (ny >= 256) ? 8 : 16);
+  int tc = 4;
+  for (int T = cap; T >= 4; T /= 2) {
+    if ((long)((nx + T - 1) / T) * nsolve >= 2L * 148) {
+      tc = T;
+      break;
+    }
+  }
+  if (mhd && ny >= 512 && tc > 8) tc = 8;
+  return tc;
+}
+
 // 4-D map over a [nf][Nz][Ny][Nx] float32 buffer (n = {Nx, Ny, Nz}) with the
 // tile box of the TMA strided passes for pencils along `axis` (1 = y, 2 = z).
 // Host-only: fills the 128-byte map, allocates nothing.
@@ -1040,20 +1063,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   }
   p->av = av_params(d);
   if (p->nd == 2 && !lgl) {
-    // columns per strided-pass tile: the widest of 16, 8, 4 that still gives
-    // about two CTAs per SM (small grids get more, narrower CTAs)
-    // 2D Euler: the clamped last pass runs at ~168 registers without spills
-    // with 128-thread CTAs (8 columns of 16-thread pencils at N <= 256, 4
-    // columns at 512 and up) and three CTAs per SM
     const int cap = p->mhd ? ((p->n[1] >= 1024) ? 8 : 16) : ((p->n[1] >= 512) ? 4 : (p->n[1] >= 256) ? 8 : 16);
-    p->tcols = 4;
-    for (int T = cap; T >= 4; T /= 2) {
-      if ((long)((p->n[0] + T - 1) / T) * nsolve >= 2L * 148) {
-        p->tcols = T;
-        break;
-      }
-    }
-    if (p->mhd && p->n[1] >= 512 && p->tcols > 8) p->tcols = 8;  // 8-component last pass: 256 threads
+    p->tcols = ps::tile_cols_2d(p->n[0], p->n[1], nsolve, p->mhd);
     if (d->tile_cols != 0) {  // explicit choice (autotuner): 4, 8 or 16, at most the cap
       const int maxT = (p->mhd && p->n[1] >= 512) ? 8 : (p->n[1] >= 1024) ? 8 : cap;
       if ((d->tile_cols != 4 && d->tile_cols != 8 && d->tile_cols != 16) || d->tile_cols > maxT)

@@ -38,6 +38,8 @@
 namespace ps {
 int record_error(int code, const char* msg);
 int encode_field_map(CUtensorMap* m, const float* base, const int n[3], int nf, int axis, int tcols = 0);
+int validate_desc(const ps_plan_desc* d);
+int tile_cols_2d(int nx, int ny, int nsolve, bool mhd);
 }
 
 namespace {
@@ -108,17 +110,14 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   if (desc->ndim != 2 && desc->ndim != 3)
     return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: only 2D and 3D grids are supported");
   if (desc->equations != PS_EQ_EULER) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: Euler equations only");
-  long cells = 1;
-  for (int a = 0; a < desc->ndim; ++a) {
+  for (int a = 0; a < desc->ndim; ++a)
     if (desc->basis[a] != PS_BASIS_FOURIER) return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: Fourier basis only");
   if (desc->av_mode != PS_AV_OFF || desc->gravity[0] != 0.0 || desc->gravity[1] != 0.0 || desc->gravity[2] != 0.0)
     return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: no artificial viscosity or gravity terms");
-    if (!ps::supported_n(desc->n[a]))
-      return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: axis length must be a power of two in 8..1024");
-    if (!(desc->length[a] > 0.0)) return fail(PS_ERR_INVALID, "ps_rhs_static: lengths must be positive");
-    cells *= desc->n[a];
-  }
-  if (!(desc->gamma > 1.0)) return fail(PS_ERR_INVALID, "ps_rhs_static: gamma must exceed 1");
+  int rc = ps::validate_desc(desc);  // the checks ps_plan_create makes
+  if (rc != PS_OK) return rc;
+  long cells = 1;
+  for (int a = 0; a < desc->ndim; ++a) cells *= desc->n[a];
   if (cells > kMaxCells) {
     char msg[200];
     snprintf(msg, sizeof(msg), "ps_rhs_static: grid of %ld cells exceeds the static scratch limit of %ld cells",
@@ -181,13 +180,14 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   e = ps::dispatch_n(nx, [&](auto n) { return ps::launch_xfirst<decltype(n)::value>(nd, xa, s); });
   if (e != cudaSuccess) return fail_cuda(e, "x pass");
 
-  // tensor maps of the scratch intermediates and of U (host structs, no allocation)
+  // tensor maps of the scratch intermediates and of U (host structs, no
+  // allocation); 2D grids take the plan's tile width (the maps' box width)
   const int n3[3] = {nx, ny, nz};
+  const int tc = (nd == 2) ? ps::tile_cols_2d(nx, ny, 1, false) : 0;
   CUtensorMap mG, mAB, mU;
-  int rc;
-  if ((rc = ps::encode_field_map(&mG, G, n3, (nd == 3) ? 15 : 8, 1)) != PS_OK) return rc;
+  if ((rc = ps::encode_field_map(&mG, G, n3, (nd == 3) ? 15 : 8, 1, tc)) != PS_OK) return rc;
   if (nd == 3 && (rc = ps::encode_field_map(&mAB, AB, n3, 10, 2)) != PS_OK) return rc;
-  if ((rc = ps::encode_field_map(&mU, U, n3, nc, (nd == 3) ? 2 : 1)) != PS_OK) return rc;
+  if ((rc = ps::encode_field_map(&mU, U, n3, nc, (nd == 3) ? 2 : 1, tc)) != PS_OK) return rc;
   const ps::StridedGeom gy{nx, (long)nx, (long)nx * ny, nz};
   if (nd == 3) {
     ps::YMidTArgs ya{};
@@ -233,6 +233,7 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
   la.eref = eref;
   la.filter_last = 0;
   la.status = nullptr;
+  la.tcols = tc;
   const int nlast = (nd == 3) ? nz : ny;
   // rhs mode reads no U^n or accumulator tiles; U's map fills those slots
   e = ps::dispatch_n(nlast, [&](auto n) {

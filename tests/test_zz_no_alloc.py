@@ -72,6 +72,22 @@ def test_static_rhs_matches_plan_rhs_two_calls(cuda_device):
     plan2.close()
 
 
+@pytest.mark.parametrize("nx,ny", [(1024, 64), (64, 1024), (512, 128)])
+def test_static_rhs_long_pencils_at_the_limit(cuda_device, nx, ny):
+    """Grids of exactly the cell limit whose long axis takes the grouped
+    pencils (group twiddles built on the device), filter on, two calls."""
+    U = torch.as_tensor(problems.kelvin_helmholtz_2d(nx, ny, U0=0.9, A=0.015), dtype=torch.float32,
+                        device=cuda_device).contiguous()
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    plan = Plan((ny, nx), (1.0, 1.0), filter_params=fp, device=cuda_device)
+    ref = plan.rhs(U)
+    for _ in range(2):
+        got = _static_rhs(_desc((nx, ny), (1.0, 1.0), filt=True), U)
+        assert torch.isfinite(got).all()
+        assert _rel(got, ref) < 1e-6, _rel(got, ref)
+    plan.close()
+
+
 def test_static_rhs_rejects_oversize_grid(cuda_device):
     lib = _lib.load()
     U = torch.zeros((5, 64, 64, 32), dtype=torch.float32, device=cuda_device)  # 131072 cells
