@@ -38,8 +38,8 @@ class _SpectralSolverBase:
                 scheme = method
             else:
                 scheme = adaptive_config.get("fallback_scheme", "rk4")
-        if adaptive is None and str(scheme).lower() not in ("rk4", "rk2"):
-            raise NotImplementedError(f"backend 'gb300': fixed-step schemes are rk4 and rk2 (got {scheme!r})")
+        # fixed steps: "rk2" is the midpoint rule and every other name is RK4,
+        # as the reference's _fixed_step dispatch (solver.py:259-265, 639-645, 990-996, 1330-1337)
         if adaptive is not None and getattr(grid, "_basis", "fourier") != "fourier":
             raise NotImplementedError("backend 'gb300': adaptive stepping on LGL grids is not implemented")
         av = None

@@ -57,6 +57,8 @@ def main(ref_path: str, only: str = "") -> None:
         return mhd3d_fixtures(grid, equations, solver, problems)
     if only == "tracers":
         return tracer_fixtures(grid, equations, solver, problems)
+    if only == "problems":
+        return problem_ic_fixtures(ref_path)
     if only == "lgl1d":
         return lgl1d_fixtures(grid, equations, solver, problems)
 
@@ -527,6 +529,75 @@ def mhd_fixtures(grid, equations, solver, problems) -> None:
                             cons0=np.array([cons0[k] for k in ("mass", "momentum_x", "momentum_y", "momentum_z",
                                                                "energy", "magnetic_energy", "cross_helicity")]),
                             divb_P0=s.max_div_b(P0), divb_U0=s.max_div_b(U0))
+
+
+# (problem name, shipped config file, grid overrides) for the initial-condition
+# fixtures: each shipped config of a registered problem, at a small grid
+PROBLEM_CASES = [
+    ("sod", "sod.yaml", {"N": 64}),
+    ("sod", "legendre_sod.yaml", {"N": 33}),
+    ("acoustic1d", "acoustic1d.yaml", {"N": 64}),
+    ("gaussian_wave1d", "gaussian_wave_traveling.yaml", {"N": 64}),
+    ("gaussian_wave1d", "acoustic_legendre_dirichlet.yaml", {"N": 33}),
+    ("shu_osher1d", "shu_osher1d.yaml", {"N": 64}),
+    ("hse_1d", "hse_1d_test.yaml", {"N": 33}),
+    ("rti_1d", "rti_1d_athena.yaml", {"N": 33}),
+    ("alfven1d", "alfven1d.yaml", {"N": 64}),
+    ("khi2d", "khi2d.yaml", {"Nx": 32, "Ny": 16}),
+    ("khi2d", "khi2d_4k.yaml", {"Nx": 48, "Ny": 27}),
+    ("uniform_2d", "uniform_2d_small.yaml", {"Nx": 9, "Ny": 9}),
+    ("rti", "rti.yaml", {"Nx": 17, "Ny": 33}),
+    ("gaussian_wave2d", "gaussian_wave2d.yaml", {"Nx": 17, "Ny": 17}),
+    ("gaussian_wave2d_y", "gaussian_wave2d_y.yaml", {"Nx": 17, "Ny": 17}),
+    ("orszag_tang2d", "orszag_tang2d.yaml", {"Nx": 32, "Ny": 16}),
+    ("tgv3d", "tgv3d.yaml", {"Nx": 16, "Ny": 16, "Nz": 8}),
+    ("turb3d", "turb3d.yaml", {"Nx": 16, "Ny": 16, "Nz": 16}),
+    ("alfven3d", "alfven3d.yaml", {"Nx": 16, "Ny": 8, "Nz": 8}),
+    ("mhd_turb3d", "mhd_turb3d.yaml", {"Nx": 16, "Ny": 16, "Nz": 16}),
+]
+
+
+def problem_ic_fixtures(ref_path: str) -> None:
+    """Initial states of the reference's registered problems from its shipped
+    configs (grids shrunk): the config (read with phrike_gb300.config.load_yaml,
+    PyYAML being absent), the reference grid's node coordinates in their own
+    dtype, and the problem's create_initial_conditions(grid).  Written to
+    problem_ics.npz."""
+    import json
+    import tempfile
+    from phrike.problems import ProblemRegistry
+    from phrike.problems import register  # noqa: F401
+    from phrike_gb300.config import load_yaml
+    out = {}
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)  # the problems create their output directories
+        try:
+            for i, (name, fname, over) in enumerate(PROBLEM_CASES):
+                with open(os.path.join(ref_path, "configs", fname)) as f:
+                    cfg = load_yaml(f.read())
+                cfg["grid"].update(over)
+                cfg.setdefault("io", {})["outdir"] = os.path.join(tmp, f"case{i}")
+                prob = ProblemRegistry.create_problem(name, config=json.loads(json.dumps(cfg)))
+                grid = prob.create_grid("numpy", None, False)
+                U0 = np.asarray(prob.create_initial_conditions(grid), dtype=np.float64)
+                out[f"c{i}_name"] = name
+                out[f"c{i}_file"] = fname
+                out[f"c{i}_config"] = json.dumps(cfg)
+                out[f"c{i}_gamma"] = prob.gamma
+                for ax in ("x", "y", "z"):
+                    if getattr(grid, ax, None) is not None:
+                        out[f"c{i}_{ax}"] = np.asarray(getattr(grid, ax))  # native dtype (float32 for single)
+                out[f"c{i}_L"] = np.array([float(getattr(grid, a)) for a in ("Lx", "Ly", "Lz") if hasattr(grid, a)])
+                out[f"c{i}_legendre"] = int(getattr(grid, "_legendre_basis", None) is not None
+                                            or str(getattr(grid, "basis", "fourier")).lower() == "legendre"
+                                            or str(getattr(grid, "basis_x", "fourier")).lower() == "legendre")
+                out[f"c{i}_U0"] = U0
+                print(name, fname, U0.shape)
+        finally:
+            os.chdir(cwd)
+    out["ncases"] = len(PROBLEM_CASES)
+    np.savez_compressed(os.path.join(HERE, "problem_ics.npz"), **out)
 
 
 if __name__ == "__main__":

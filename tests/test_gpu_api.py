@@ -67,7 +67,7 @@ def test_run_simulation_sod_fixed_dt(cuda_device):
            "physics": {"gamma": 1.4},
            "integration": {"t0": 0.0, "t_end": 2e-3, "dt": 2e-5, "output_interval": 1e-3,
                            "spectral_filter": {"enabled": True, "p": 8, "alpha": 36.0}}}
-    solver, hist = run_simulation("sod", config=cfg, backend="gb300")
+    solver, hist = run_simulation("baseline_sod1d", config=cfg, backend="gb300")
     s = O.EulerSolver(O.FourierBox((256,), (1.0,), dealias=True, filter_enabled=True))
     ref = problems.sod_smoothed(256).astype(np.float32).astype(np.float64)
     for _ in range(100):
