@@ -241,14 +241,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_step1d(Step1DArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const int s = sl(c, n2);
-          if (stage == 3) {
-            u3[c] = fmaf(rc.wacc, k[c], s_acc[s]);
-          } else {
-            const float un = s_un[s];
-            const float ac = (stage == 0) ? un : s_acc[s];
-            s_acc[s] = fmaf(rc.wacc, k[c], ac);
-            u3[c] = fmaf(rc.wnext, k[c], un);
-          }
+          u3[c] = rk_update_incr(stage, rc, k[c], s_un[s], s_acc[s]);
         }
         clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll

@@ -381,13 +381,9 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const long g = so + c * cells + o;
-        if (a.stage == 3) {
-          u[c] = fmaf(rk.wacc, k[c], a.acc[g]);
-        } else {
-          const float un = a.Un[g];
-          a.acc[g] = fmaf(rk.wacc, k[c], (a.stage == 0) ? un : a.acc[g]);
-          u[c] = fmaf(rk.wnext, k[c], un);
-        }
+        float ac = (a.stage == 0) ? 0.0f : a.acc[g];
+        u[c] = rk_update_incr(a.stage, rk, k[c], a.Un[g], ac);
+        if (a.stage != 3) a.acc[g] = ac;
       }
       clamp_state<2>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll

@@ -188,13 +188,7 @@ __global__ void __launch_bounds__(1024) k_lgl1d(Lgl1DArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const int s = c * N + i;
-          if (stage == 3) {
-            u3[c] = fmaf(rc.wacc, k[c], acc[s]);
-          } else {
-            const float v = un[s];
-            acc[s] = fmaf(rc.wacc, k[c], (stage == 0) ? v : acc[s]);
-            u3[c] = fmaf(rc.wnext, k[c], v);
-          }
+          u3[c] = rk_update_incr(stage, rc, k[c], un[s], acc[s]);
         }
         clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
         us[i] = u3[0];
@@ -440,14 +434,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_lgl1d_cl(Lgl1DArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const int s = c * N + i0 + r;
-          const float k = kb[c * R + r];
-          if (stage == 3) {
-            u3[c] = fmaf(rc.wacc, k, acc[c * R + r]);
-          } else {
-            const float v = un[s];
-            acc[c * R + r] = fmaf(rc.wacc, k, (stage == 0) ? v : acc[c * R + r]);
-            u3[c] = fmaf(rc.wnext, k, v);
-          }
+          u3[c] = rk_update_incr(stage, rc, kb[c * R + r], un[s], acc[c * R + r]);
         }
         clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
         mine[r] = u3[0];

@@ -159,7 +159,7 @@ int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, do
   u.g[1] = (float)p->desc.gravity[1];
   u.gravity = (p->desc.gravity[0] != 0.0 || p->desc.gravity[1] != 0.0) ? 1 : 0;
   u.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
-  const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
+  const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 20.0 : 24.0;
   ProfScope prof(p, s, PS_KIND_LAST, words * field_bytes(p));
   LGL_CU(launch_lgl_update(u, s), "LGL stage update");
   return PS_OK;
@@ -175,7 +175,7 @@ int stage(ps_plan p, float* in, int st, float* Un, float* out, double dt, const 
     LGL_CU(launch_lgl_x(a, mode_of(p), s), "LGL x contraction");
   }
   {
-    const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 16.0 : 24.0;
+    const double words = (st < 0) ? 12.0 : (st == 0) ? 20.0 : (st == 3) ? 20.0 : 24.0;
     ProfScope prof(p, s, PS_KIND_LGL_Y, words * field_bytes(p));
     LGL_CU(launch_lgl_y(a, mode_of(p), s), "LGL y contraction + stage update");
   }

@@ -249,14 +249,7 @@ __global__ void __launch_bounds__(Shape<N>::A) k_mhd1d(Mhd1DArgs a) {
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           const int s = sl(c, n2);
-          const float k = S.kb[s];
-          if (stage == 3) {
-            u[c] = fmaf(rc.wacc, k, s_acc[s]);
-          } else {
-            const float un = s_un[s];
-            s_acc[s] = fmaf(rc.wacc, k, (stage == 0) ? un : s_acc[s]);
-            u[c] = fmaf(rc.wnext, k, un);
-          }
+          u[c] = rk_update_incr(stage, rc, S.kb[s], s_un[s], s_acc[s]);
         }
         clamp_mhd(u, a.gamma, a.rho_min, a.p_min);
 #pragma unroll

@@ -31,6 +31,7 @@ __device__ __forceinline__ void clamp_mhd(float (&u)[8], float gamma, float rho_
   const float v2 = ux * ux + uy * uy + uz * uz;
   const float b2 = u[5] * u[5] + u[6] * u[6] + u[7] * u[7];
   const float p = (gamma - 1.0f) * (u[4] - 0.5f * rho * v2 - 0.5f * b2);
+  if (rho >= rho_min && p >= p_min) return;  // no floor acts: the round trip is the identity
   const float rc = fmaxf(rho, rho_min);
   const float pc = fmaxf(p, p_min);
   u[0] = rc;

@@ -115,6 +115,18 @@ __device__ __forceinline__ RKCoef rk_coef(int stage, float dt, int rk2) {
   return c;
 }
 
+// One RK stage update of a state value with the accumulator in increment
+// form: acc holds only sum_i w_i k_i, and U^n is added once, at the last
+// stage (u = U^n + (acc + w_4 k_4)).  The sum is the same as RK4's
+// U^n + sum_i w_i k_i; its float32 rounding is relative to the increments
+// instead of to |U^n|.  Used where the accumulator lives in shared memory or
+// where U^n is read at the last stage anyway (LGL, 1D kernels).
+__device__ __forceinline__ float rk_update_incr(int stage, const RKCoef& rk, float k, float un, float& acc) {
+  if (stage == 3) return un + fmaf(rk.wacc, k, acc);
+  acc = (stage == 0) ? rk.wacc * k : fmaf(rk.wacc, k, acc);
+  return fmaf(rk.wnext, k, un);
+}
+
 // Multiplier of the one-axis operators at spectral index k (tables hold
 // m s / N and k m s / N):
 //   deriv 0: P  = m s / N
@@ -136,7 +148,7 @@ __device__ __forceinline__ float2 op_symbol(float2 w, int k, int deriv, float sc
   return make_float2(w.x * s, w.y * s);
 }
 
-// Energy-perturbation form.// Energy-perturbation form.  Inside the engine the energy slot of a state holds
+// Energy-perturbation form.  Inside the engine the energy slot of a state holds
 // E' = E - E_ref for a per-run constant E_ref (the energy of the first cell
 // when the run starts).  With p_ref = (gamma-1) E_ref the primitive pressure
 // becomes p' = p - p_ref = (gamma-1)(E' - rho|u|^2/2), computed from small
@@ -161,6 +173,10 @@ __device__ __forceinline__ void clamp_state(float (&u)[ND + 2], float gamma, flo
     kin = fmaf(vel[a], vel[a], kin);
   }
   const float p = (gamma - 1.0f) * (u[ND + 1] - 0.5f * rho * kin);
+  // where no floor acts the reference's primitive -> conservative round trip
+  // is the identity (to float64 rounding): keep the state as it is instead of
+  // adding float32 rounding to E and the momenta
+  if (rho >= rho_min && p >= pmin_shift) return;
   const float rc = fmaxf(rho, rho_min);
   const float pc = fmaxf(p, pmin_shift);
   u[0] = rc;

@@ -148,24 +148,56 @@ def test_lgl_tensor_cores_match_cuda_core_split(cuda_device, n):
     assert pa.status() == 0
 
 
+# Momentum after a run, against the float64 oracle started from the same
+# float32 initial state (the engine's input).  FP64 and FP32 contractions sit
+# at the float32-state floor; split-bf16 x3 keeps about 16 significand bits
+# of each operand (measured 1.1e-5 at 65^2, 3.0e-5 at 257^2 and 4.6e-5 at
+# 513^2 after 500 steps).
+MOM_TOL = {"fp64": 1e-5, "fp32": 1e-5, "bf16x3": 6e-5, "bf16x3_simt": 6e-5}
+
+
+def _oracle_steps(n, U0, nsteps, dt, **kw):
+    s = L.LGLSolver2D(n, n, gamma=GAMMA, **kw)
+    R = U0.astype(np.float32).astype(np.float64)
+    for _ in range(nsteps):
+        R = s.step(R, dt)
+    return R
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_lgl_acoustic_pulse_vs_oracle(cuda_device, prec):
     """The acoustic Gaussian pulse (amplitude 0.01, width^2 0.01) on 65 x 65
-    LGL nodes, 200 steps of dt = 1e-5, against the float64 oracle (measured:
-    momentum 2.5e-5 for every precision, the float32-state floor)."""
-    n, nsteps, dt = 65, 200, 1e-5
+    LGL nodes, 500 steps of dt = 1e-5 (measured momentum 4.2e-7 for FP64 and
+    FP32 contractions, 1.1e-5 for split-bf16 x3)."""
+    n, nsteps, dt = 65, 500, 1e-5
     U0 = _pulse(n, n)
-    s = L.LGLSolver2D(n, n, gamma=GAMMA)
-    R = U0.copy()
-    for _ in range(nsteps):
-        R = s.step(R, dt)
+    R = _oracle_steps(n, U0, nsteps, dt)
     p = _plan(n, n, prec)
     U = _dev(U0)
     p.run_(U, nsteps, dt)
     G = U.cpu().numpy()
     assert rel_l2(G[0], R[0]) < 1e-6
     assert rel_l2(G[3], R[3]) < 1e-7
-    assert rel_l2(G[1:3], R[1:3]) < 1e-4, rel_l2(G[1:3], R[1:3])
+    tol = 2e-6 if prec in ("fp32", "fp64") else 3e-5
+    assert rel_l2(G[1:3], R[1:3]) < tol, rel_l2(G[1:3], R[1:3])
+    assert p.status() == 0
+
+
+@pytest.mark.parametrize("n,prec", [(257, "fp32"), (257, "bf16x3"), (513, "fp32"), (513, "bf16x3")])
+def test_lgl_workload_size_500_steps(cuda_device, n, prec):
+    """The precision workload at its stated sizes: 257^2 and 513^2 nodes, 500
+    steps of dt = 1e-5 (measured momentum: FP32 2.1e-6 and 8.6e-6,
+    split-bf16 x3 3.0e-5 and 4.6e-5; density 6.4e-7, energy 4.4e-9)."""
+    U0 = _pulse(n, n)
+    R = _oracle_steps(n, U0, 500, 1e-5)
+    p = _plan(n, n, prec)
+    U = _dev(U0)
+    p.run_(U, 500, 1e-5)
+    G = U.cpu().numpy()
+    e = (rel_l2(G[0], R[0]), rel_l2(G[1:3], R[1:3]), rel_l2(G[3], R[3]))
+    print(f"\nLGL {n}^2 {prec} 500 steps: rho {e[0]:.2e} mom {e[1]:.2e} E {e[2]:.2e}")
+    assert e[0] < 2e-6 and e[2] < 1e-7, e
+    assert e[1] < MOM_TOL[prec], e
     assert p.status() == 0
 
 
@@ -173,8 +205,8 @@ def test_lgl_filter_in_step(cuda_device):
     n, nsteps, dt = 33, 20, 1e-4
     fp = {"enabled": True, "p": 8, "alpha": 36.0, "interval": 3}
     U0 = _pulse(n, n, amp=0.2, width2=0.05)
+    R = _oracle_steps(n, U0, 0, dt)
     s = L.LGLSolver2D(n, n, gamma=GAMMA, filter_params=fp)
-    R = U0.copy()
     for _ in range(nsteps):
         R = s.step(R, dt)
     p = _plan(n, n, "fp32", filt=fp)
@@ -183,7 +215,7 @@ def test_lgl_filter_in_step(cuda_device):
         p.step_(U, dt)
     G = U.cpu().numpy()
     assert max(rel_l2(G[0], R[0]), rel_l2(G[3], R[3])) < 2e-6
-    assert rel_l2(G[1:3], R[1:3]) < 1e-4
+    assert rel_l2(G[1:3], R[1:3]) < 1e-5, rel_l2(G[1:3], R[1:3])
 
 
 def test_lgl_cfl_run_vs_oracle(cuda_device):
@@ -191,7 +223,7 @@ def test_lgl_cfl_run_vs_oracle(cuda_device):
     n, t_end = 33, 0.02
     U0 = _pulse(n, n, amp=0.2, width2=0.05)
     s = L.LGLSolver2D(n, n, gamma=GAMMA, cfl=0.3)
-    R, t, steps = U0.copy(), 0.0, 0
+    R, t, steps = U0.astype(np.float32).astype(np.float64), 0.0, 0
     while t < t_end - 1e-12:
         dt = min(s.compute_dt(R), t_end - t)
         R = s.step(R, dt)
@@ -206,7 +238,7 @@ def test_lgl_cfl_run_vs_oracle(cuda_device):
     assert p.steps_done() == [steps]
     G = U.cpu().numpy()
     assert max(rel_l2(G[0], R[0]), rel_l2(G[3], R[3])) < 2e-6
-    assert rel_l2(G[1:3], R[1:3]) < 1e-4
+    assert rel_l2(G[1:3], R[1:3]) < 1e-5, rel_l2(G[1:3], R[1:3])
 
 
 def test_lgl_batch_matches_alone(cuda_device):

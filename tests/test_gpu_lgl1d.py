@@ -119,14 +119,14 @@ def test_lgl1d_long_run_vs_oracle(cuda_device, tag):
     """200 steps of dt = 2e-4 against the float64 oracle."""
     s, o = _solver(tag), _oracle(tag)
     U0 = initial_state(L.LGLAxis(CASES[tag]["n"], LENGTH).x)
-    R = U0.copy()
+    R = U0.astype(np.float32).astype(np.float64)  # the oracle from the engine's float32 input
     for _ in range(200):
         R = o.step(R, DT)
     U = _dev(U0)
     s.plan.run_(U, 200, DT)
     G = U.cpu().numpy()
     assert max(rel_l2(G[0], R[0]), rel_l2(G[2], R[2])) < 5e-6
-    assert rel_l2(G[1], R[1]) < 1e-4, rel_l2(G[1], R[1])
+    assert rel_l2(G[1], R[1]) < 1e-5, rel_l2(G[1], R[1])
     assert s.plan.status() == 0
 
 
@@ -135,7 +135,7 @@ def test_lgl1d_cfl_run_vs_oracle(cuda_device):
     tag, t_end = "wall", 0.05
     s, o = _solver(tag, cfl=0.3), _oracle(tag, cfl=0.3)
     U0 = initial_state(o.ax.x)
-    R, t, steps = U0.copy(), 0.0, 0
+    R, t, steps = U0.astype(np.float32).astype(np.float64), 0.0, 0
     while t < t_end - 1e-12:
         dt = min(o.compute_dt(R), t_end - t)
         R = o.step(R, dt)
@@ -149,7 +149,7 @@ def test_lgl1d_cfl_run_vs_oracle(cuda_device):
     assert s.plan.steps_done() == [steps]
     G = U.cpu().numpy()
     assert max(rel_l2(G[0], R[0]), rel_l2(G[2], R[2])) < 5e-6
-    assert rel_l2(G[1], R[1]) < 1e-4
+    assert rel_l2(G[1], R[1]) < 1e-5, rel_l2(G[1], R[1])
 
 
 def test_lgl1d_batch_matches_alone(cuda_device):
@@ -212,7 +212,7 @@ def test_lgl1d_cluster_form_vs_oracle(cuda_device, n, tag):
     for k in range(3):
         assert rel_l2(r[k], ro[k]) < 3e-5 * (n / 257), (k, rel_l2(r[k], ro[k]))
     dt = 0.2 * o.compute_dt(U0)
-    R = U0.copy()
+    R = U0.astype(np.float32).astype(np.float64)
     for _ in range(20):
         R = o.step(R, dt)
     p = mk()
@@ -220,7 +220,7 @@ def test_lgl1d_cluster_form_vs_oracle(cuda_device, n, tag):
     p.run_(U, 20, dt)
     G = U.cpu().numpy()
     assert max(rel_l2(G[0], R[0]), rel_l2(G[2], R[2])) < 5e-6
-    assert rel_l2(G[1], R[1]) < 1e-4, rel_l2(G[1], R[1])
+    assert rel_l2(G[1], R[1]) < 1e-5, rel_l2(G[1], R[1])
     assert p.status() == 0
     # CFL loop to a short end time, and a batch of two that matches the solve alone
     t_end = 10 * o.compute_dt(U0)
