@@ -212,11 +212,14 @@ int validate_desc(const ps_plan_desc* d) { return validate(d); }
 // Columns per strided-pass tile of a 2D Fourier grid (nx, ny: points along x
 // and y): the widest of 16, 8, 4 that still gives about two CTAs per SM
 // (small grids get more, narrower CTAs).  2D Euler: the clamped last pass
-// runs at ~168 registers without spills with 128-thread CTAs (8 columns of
-// 16-thread pencils at N <= 256, 4 columns at 512 and up) and three CTAs per
-// SM; the 8-component MHD last pass takes at most 8 columns from 512 rows up.
+// runs at ~168 registers with 128-thread CTAs (8 columns of 16-thread pencils
+// at N <= 256) and three CTAs per SM; at 512 points 8 columns (256 threads,
+// 230 registers, one CTA per SM) move whole 32-byte sectors and measured
+// 12% faster than 4 on a batch of sixteen 512^2 solves (194 vs 220 us); 4
+// columns from 1024 up.  The 8-component MHD last pass takes at most 8
+// columns from 512 rows up.
 int tile_cols_2d(int nx, int ny, int nsolve, bool mhd) {
-  const int cap = mhd ? ((ny >= 1024) ? 8 : 16) : ((ny >= 512) ? 4 : (ny >= 256) ? 8 : 16);
+  const int cap = mhd ? ((ny >= 1024) ? 8 : 16) : ((ny >= 1024) ? 4 : (ny >= 256) ? 8 : 16);
   int tc = 4;
   for (int T = cap; T >= 4; T /= 2) {
     if ((long)((nx + T - 1) / T) * nsolve >= 2L * 148) {
@@ -1063,10 +1066,10 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   }
   p->av = av_params(d);
   if (p->nd == 2 && !lgl) {
-    const int cap = p->mhd ? ((p->n[1] >= 1024) ? 8 : 16) : ((p->n[1] >= 512) ? 4 : (p->n[1] >= 256) ? 8 : 16);
+    const int cap = p->mhd ? ((p->n[1] >= 1024) ? 8 : 16) : ((p->n[1] >= 1024) ? 4 : (p->n[1] >= 256) ? 8 : 16);
     p->tcols = ps::tile_cols_2d(p->n[0], p->n[1], nsolve, p->mhd);
     if (d->tile_cols != 0) {  // explicit choice (autotuner): 4, 8 or 16, at most the cap
-      const int maxT = (p->mhd && p->n[1] >= 512) ? 8 : (p->n[1] >= 1024) ? 8 : cap;
+      const int maxT = (p->n[1] >= 512) ? 8 : cap;
       if ((d->tile_cols != 4 && d->tile_cols != 8 && d->tile_cols != 16) || d->tile_cols > maxT)
         return cleanup(fail(PS_ERR_INVALID, "tile_cols %d not allowed here (4..%d, powers of two)", d->tile_cols,
                             maxT));

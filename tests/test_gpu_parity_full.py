@@ -29,7 +29,7 @@ TGV_COMPONENT_TOL = 4e-5
 KHI_TOL = {64: 1e-5, 128: 1e-5, 256: 1e-5, 512: 1.2e-4}
 
 
-@pytest.mark.parametrize("n", [128])
+@pytest.mark.parametrize("n", [128, 256])
 def test_tgv_workload_size_200_steps(cuda_device, n):
     z = golden(f"tgv3d_{n}_200.npz")
     plan = Plan((n, n, n), (2 * np.pi,) * 3, device=cuda_device)
