@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/phrike_gb300.h"
+#include "mixed_radix.cuh"
 #include "pass_common.cuh"
 
 struct ps_plan_s {
@@ -89,6 +90,10 @@ struct ps_plan_s {
   void* FYT = nullptr;                    // [2][nsolve*4][nx][pitch_y] transposed y flux
   CUtensorMap map_FX{}, map_Dx{}, map_Dy{}, map_FYT{};
   int nt_x = 0, nt_y = 0;                 // N tiles of the two contractions
+
+  // Fourier axes of any 5-smooth length (mixed-radix passes, mr_plan.cu)
+  bool mr = false;
+  ps::MrAxis mrax[3] = {};
 
   ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
   long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
@@ -180,5 +185,17 @@ int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
               cudaStream_t s);
 int lgl_derivative(ps_plan p, int axis, const float* f, float* out, int nf, cudaStream_t s);
 int lgl_filter(ps_plan p, const float* f, float* out, int nf, cudaStream_t s);
+
+// Fourier plans on the mixed-radix passes (mr_plan.cu)
+bool mr_axis_ok(int n);
+int mr_setup(ps_plan p);
+int mr_apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, bool complement,
+                const int* active, long ss_in, cudaStream_t s);
+int mr_xfirst(ps_plan p, const float* U, float* Uw, float* speed, bool shift_in, const int* active, cudaStream_t s);
+int mr_ymid(ps_plan p, const int* active, cudaStream_t s);
+int mr_last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
+            const int* active, cudaStream_t s);
+int mr_steps_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
+                cudaStream_t s);
 
 }  // namespace ps

@@ -77,6 +77,16 @@ bool is_lgl(const ps_plan_desc* d) {
   return false;
 }
 
+// every axis has a length the power-of-two pencil kernels are compiled for
+bool pow2_axes(const ps_plan_desc* d) {
+  for (int a = 0; a < d->ndim && a < 3; ++a)
+    if (d->ndim == 1 ? !ps::supported_n_1d(d->n[a]) : !ps::supported_n(d->n[a])) return false;
+  return true;
+}
+
+// a Fourier grid with some other axis length: the mixed-radix passes
+bool is_mr(const ps_plan_desc* d) { return !is_lgl(d) && !pow2_axes(d); }
+
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
   if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
@@ -100,13 +110,20 @@ int validate(const ps_plan_desc* d) {
   for (int a = 0; a < d->ndim; ++a) {
     if (d->basis[a] != PS_BASIS_FOURIER)
       return fail(PS_ERR_UNSUPPORTED, "axis %d: only the Fourier basis is supported by this plan type", a);
-    if (d->ndim == 1 ? !ps::supported_n_1d(d->n[a]) : !ps::supported_n(d->n[a]))
-      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (powers of two 8..%d)", a, d->n[a],
-                  d->ndim == 1 ? 4096 : 1024);
+    const bool p2 = d->ndim == 1 ? ps::supported_n_1d(d->n[a]) : ps::supported_n(d->n[a]);
+    if (!p2 && !ps::mr_axis_ok(d->n[a]))
+      return fail(PS_ERR_UNSUPPORTED, "axis %d: N=%d not supported (2^a 3^b 5^c from 2 to 4096%s)", a, d->n[a],
+                  d->ndim == 1 ? ", powers of two to 4096" : "");
     if (!(d->length[a] > 0.0)) return fail(PS_ERR_INVALID, "axis %d: length must be positive", a);
   }
   if (!(d->gamma > 1.0)) return fail(PS_ERR_INVALID, "gamma must exceed 1");
   if (d->filter_interval < 1) return fail(PS_ERR_INVALID, "filter_interval must be >= 1");
+  if (is_mr(d)) {
+    if (d->equations != PS_EQ_EULER)
+      return fail(PS_ERR_UNSUPPORTED, "MHD plans need power-of-two axes (8..1024; 2048 in 1D)");
+    if (d->av_mode != PS_AV_OFF)
+      return fail(PS_ERR_UNSUPPORTED, "artificial viscosity needs power-of-two axes");
+  }
   if (d->av_mode != PS_AV_OFF) {
     if (d->av_mode != PS_AV_SENSOR && d->av_mode != PS_AV_CONSTANT)
       return fail(PS_ERR_INVALID, "av_mode must be PS_AV_OFF, PS_AV_SENSOR or PS_AV_CONSTANT");
@@ -287,6 +304,7 @@ ps::StridedGeom geom_z(const ps_plan_s* p) {
 int apply_op(ps_plan p, int axis, const float* in, float* out, int nf, int deriv, float scale, cudaStream_t s,
              bool complement = false, const int* active = nullptr, long ss_in = 0) {
   ProfScope prof(p, s, PS_KIND_OP, 8.0 * nf * p->cells * p->nsolve);
+  if (p->mr) return ps::mr_apply_op(p, axis, in, out, nf, deriv, scale, complement, active, ss_in, s);
   cudaError_t e;
   const float kunit = (float)(2.0 * M_PI / p->desc.length[axis]);
   if (axis != 0 && ss_in != 0) return fail(PS_ERR_INVALID, "field-subset input is supported along x only");
@@ -353,6 +371,7 @@ int xfirst(ps_plan p, const float* U, float* Uw, float* speed, cudaStream_t s, b
   a.shift_in = shift_in ? 1 : 0;
   ProfScope prof(p, s, PS_KIND_X,
                  4.0 * p->cells * p->nsolve * (p->nc * (Uw ? 2 : 1) + p->nd * p->nc));
+  if (p->mr) return ps::mr_xfirst(p, U, Uw, speed, shift_in, active, s);
   cudaError_t e = ps::dispatch_n(p->n[0], [&](auto nc) {
     return ps::launch_xfirst<decltype(nc)::value>(p->nd, a, s);
   });
@@ -371,6 +390,7 @@ int ymid(ps_plan p, cudaStream_t s, const int* active) {
   a.active = active;
   a.status = p->status;
   ProfScope prof(p, s, PS_KIND_Y, 4.0 * p->cells * p->nsolve * 25);
+  if (p->mr) return ps::mr_ymid(p, active, s);
   cudaError_t e = ps::dispatch_n(p->n[1], [&](auto nc) {
     return ps::launch_ymid3_t<decltype(nc)::value>(p->map_G_y, a, s);
   });
@@ -381,6 +401,11 @@ int ymid(ps_plan p, cudaStream_t s, const int* active) {
 int last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
          cudaStream_t s, const int* active) {
   int rc;
+  if (p->mr) {
+    const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
+    ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * p->nsolve * p->nc * (2 + st_words));
+    return ps::mr_last(p, stage, Un, out, dt, d_dt, filter_last, active, s);
+  }
   if ((rc = state_maps(p, Un)) != PS_OK) return rc;
   ps::LastTArgs a{};
   const int nc = p->nc;
@@ -453,6 +478,7 @@ bool filter_due(ps_plan p, long counter) {
 
 int step_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
             cudaStream_t s) {
+  if (p->mr) return ps::mr_steps_1d(p, U, nsteps, dt, d_dt, d_t, d_tend, s);
   ps::Step1DArgs a{};
   a.U = U;
   a.solve_stride = p->ss(3);
@@ -1029,7 +1055,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     return code;
   };
   const bool lgl = is_lgl(d);
-  for (int a = 0; a < p->nd && !lgl; ++a) {
+  const bool mr = is_mr(d);
+  for (int a = 0; a < p->nd && !lgl && !mr; ++a) {
     std::vector<float> P, dd;
     std::vector<float2> twf, twi;
     build_axis(p->n[a], d->length[a], d->dealias, d->filter_enabled, d->filter_p, d->filter_alpha, P, dd, twf, twi);
@@ -1048,6 +1075,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
   const long c = p->cells * nsolve;
   if (p->nd == 1) {
     if ((rc = dalloc(p, &p->F1, 3 * c)) != PS_OK) return cleanup(rc);
+    if (mr && ((rc = dalloc(p, &p->acc, 3 * c)) != PS_OK || (rc = dalloc(p, &p->Us, 3 * c)) != PS_OK))
+      return cleanup(rc);
     if (!p->mhd && p->n[0] >= 4096 && (rc = dalloc(p, &p->acc, 6 * c)) != PS_OK) return cleanup(rc);
     // 1D MHD from 2048 points: U^n and the accumulator in global scratch
     if (p->mhd && p->n[0] >= 2048 && (rc = dalloc(p, &p->acc, 16 * c)) != PS_OK) return cleanup(rc);
@@ -1065,7 +1094,7 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
   }
   p->av = av_params(d);
-  if (p->nd == 2 && !lgl) {
+  if (p->nd == 2 && !lgl && !mr) {
     const int cap = p->mhd ? ((p->n[1] >= 1024) ? 8 : 16) : ((p->n[1] >= 1024) ? 4 : (p->n[1] >= 256) ? 8 : 16);
     p->tcols = ps::tile_cols_2d(p->n[0], p->n[1], nsolve, p->mhd);
     if (d->tile_cols != 0) {  // explicit choice (autotuner): 4, 8 or 16, at most the cap
@@ -1095,6 +1124,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     return cleanup(fail(PS_ERR_CUDA, "scalar initialisation failed"));
   if (lgl) {
     if ((rc = ps::lgl_setup(p)) != PS_OK) return cleanup(rc);
+  } else if (mr) {
+    if ((rc = ps::mr_setup(p)) != PS_OK) return cleanup(rc);
   } else if (p->nd >= 2 && !(p->mhd && p->nd == 3)) {
     if ((rc = make_map(&p->map_G_y, p->G, p, p->mhd ? 16 : (p->nd == 3) ? 15 : 8, 1)) != PS_OK)
       return cleanup(rc);
@@ -1157,7 +1188,12 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   size_t tables = 0;
   for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + 2 * sizeof(float2));
   if (is_lgl(d)) tables = ps::lgl_scratch_bytes(d, nsolve);
+  if (is_mr(d)) {  // P, d and the twiddles W_N^q per axis
+    tables = 0;
+    for (int a = 0; a < d->ndim; ++a) tables += (size_t)d->n[a] * (2 * sizeof(float) + sizeof(float2));
+  }
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
+  if (is_mr(d) && d->ndim == 1) fields += 6;  // stage input and increments
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
   const bool mhd = d->equations == PS_EQ_MHD;
   if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
@@ -1304,6 +1340,8 @@ int ps_run_adaptive(ps_plan p, float* U, int nattempts, const ps_adaptive_desc* 
   if (!p || !U || !ad || !d_t || !d_tend || !d_dt) return fail(PS_ERR_INVALID, "null argument");
   if (nattempts < 0) return fail(PS_ERR_INVALID, "nattempts must be >= 0");
   if (p->lgl) return fail(PS_ERR_UNSUPPORTED, "adaptive stepping is not supported on LGL grids");
+  if (p->mr && p->nd == 1)
+    return fail(PS_ERR_UNSUPPORTED, "1D adaptive stepping needs a power-of-two grid (8..4096)");
   ps::ArkTableau tab;
   if (ps::ark_tableau(ad->method, &tab) != 0) return fail(PS_ERR_INVALID, "unknown adaptive method %d", ad->method);
   if (!(ad->rtol >= 0.0) || !(ad->atol >= 0.0) || !(ad->safety_factor > 0.0) || !(ad->min_dt_factor > 0.0) ||

@@ -116,6 +116,9 @@ extern "C" int ps_rhs_static(const ps_plan_desc* desc, const float* U, float* rh
     return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: no artificial viscosity or gravity terms");
   int rc = ps::validate_desc(desc);  // the checks ps_plan_create makes
   if (rc != PS_OK) return rc;
+  for (int a = 0; a < desc->ndim; ++a)  // plans take any 5-smooth length; the static tables hold powers of two
+    if (!ps::supported_n(desc->n[a]))
+      return fail(PS_ERR_UNSUPPORTED, "ps_rhs_static: axis lengths are powers of two from 8 to 1024");
   long cells = 1;
   for (int a = 0; a < desc->ndim; ++a) cells *= desc->n[a];
   if (cells > kMaxCells) {

@@ -49,6 +49,11 @@ GPU_CASES = {  # names distinct from CASES
     # of a rejected attempt is sensitive to rounding: step sizes compare to 3%
     "ot32_rk45": dict(kind="mhd", shape=(32, 32), lengths=(2 * np.pi,) * 2, filt=True, cfl=0.3, method="rk45",
                       ctrl=dict(rtol=1e-5, max_dt_factor=2.0), t_end=0.15, dt_rtol=3e-2),
+    # grids with axes of other lengths (the mixed-radix passes)
+    "khi60x48_rk23_grav": dict(kind="euler", shape=(60, 48), lengths=(1.0, 1.0), filt=True, cfl=0.4,
+                               method="rk23", ctrl=dict(rtol=1e-4), t_end=0.05, gravity=[0.3, -1.0]),
+    "tgv24x20x18_rk78": dict(kind="euler", shape=(24, 20, 18), lengths=(2 * np.pi,) * 3, filt=False, cfl=0.25,
+                             method="rk78", ctrl=dict(rtol=3e-7), t_end=0.05),
 }
 
 

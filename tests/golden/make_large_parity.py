@@ -1,6 +1,6 @@
 """Float64 oracle states at the workloads' full sizes, stored on a sub-lattice.
 
-    python tests/golden/make_large_parity.py [tgv128|tgv256|khi] ...
+    python tests/golden/make_large_parity.py [tgv128|tgv256|khi|khi4k] ...
 
 Runs the oracle (``oracle/spectral.py``, the NumPy float64 restatement of the
 reference pinned to the reference's own outputs by tests/test_oracle_golden.py)
@@ -8,7 +8,9 @@ with ``fused=True``: one spectral sum per stage, the same operator as the
 reference's per-derivative full transforms up to rounding.  The initial
 states are rounded to float32 first, as the float32 engine receives them.
 
-Writes tests/golden/tgv3d_{128,256}_200.npz and tests/golden/khi_c4_t1.npz.
+Writes tests/golden/tgv3d_{128,256}_200.npz, tests/golden/khi_c4_t1.npz and
+tests/golden/khi2d_4k_steps.npz (the reference's khi2d problem on its shipped
+3840 x 2160 grid, a few CFL steps).
 """
 from __future__ import annotations
 
@@ -59,9 +61,30 @@ def khi() -> None:
     np.savez_compressed(os.path.join(HERE, "khi_c4_t1.npz"), **out)
 
 
+def khi4k() -> None:
+    cfg = PC.khi4k_config()
+    U = PC.khi4k_initial_state(cfg).astype(np.float32).astype(np.float64)
+    g = cfg["grid"]
+    sf = cfg["integration"]["spectral_filter"]
+    box = O.FourierBox((int(g["Ny"]), int(g["Nx"])), (float(g["Ly"]), float(g["Lx"])), dealias=True,
+                       filter_enabled=True, filter_p=int(sf["p"]), filter_alpha=float(sf["alpha"]))
+    s = O.EulerSolver(box, gamma=float(cfg["physics"]["gamma"]), cfl=float(cfg["integration"]["cfl"]), fused=True)
+    dts = []
+    t0 = time.time()
+    for i in range(PC.KHI4K_STEPS):
+        dt = s.compute_dt(U)
+        U = s.step(U, dt)
+        dts.append(dt)
+        print(f"khi4k step {i} dt={dt:.3e} {time.time() - t0:.0f}s", flush=True)
+    st = PC.KHI4K_STRIDE
+    np.savez_compressed(os.path.join(HERE, "khi2d_4k_steps.npz"), U=PC.sub(U, st), stride=st, dts=np.array(dts))
+
+
 if __name__ == "__main__":
-    for what in sys.argv[1:] or ["tgv128", "tgv256", "khi"]:
-        if what == "khi":
+    for what in sys.argv[1:] or ["tgv128", "tgv256", "khi", "khi4k"]:
+        if what == "khi4k":
+            khi4k()
+        elif what == "khi":
             khi()
         else:
             tgv(int(what[3:]))

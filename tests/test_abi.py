@@ -32,10 +32,10 @@ def test_error_paths_without_device(built_lib):
     from phrike_gb300 import _lib
     desc = _lib.PlanDesc()
     assert built_lib.ps_plan_desc_init(C.byref(desc), 3) == 0
-    desc.n[0] = desc.n[1] = desc.n[2] = 48  # not a supported pencil length
+    desc.n[0] = desc.n[1] = desc.n[2] = 14  # 2 * 7: no pencil transform for the factor 7
     h = C.c_void_p()
     rc = built_lib.ps_plan_create(C.byref(desc), C.byref(h))
-    assert rc == 2 and b"N=48" in built_lib.ps_last_error()
+    assert rc == 2 and b"N=14" in built_lib.ps_last_error()
     desc.ndim = 4
     assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 1
     size = C.c_size_t()
@@ -73,3 +73,39 @@ def test_lgl_descriptor_validation_without_device(built_lib):
         desc.basis[a] = _lib.PS_BASIS_LEGENDRE
     assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2  # 3D Legendre
     assert built_lib.ps_lgl_build(1, 2.0, None, None, None, None) == 1
+
+
+def test_mixed_radix_descriptor_validation_without_device(built_lib):
+    """Fourier axes of any 2^a 3^b 5^c length up to 4096 validate (the
+    khi2d_4k grid 3840 x 2160 among them); other factors, lengths above 4096,
+    MHD and artificial viscosity on such axes are refused before any device
+    work, and so is the static right-hand side."""
+    import ctypes as C
+    from phrike_gb300 import _lib
+    desc = _lib.PlanDesc()
+    size = C.c_size_t()
+    h = C.c_void_p()
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 2) == 0
+    desc.n[0], desc.n[1] = 3840, 2160
+    assert built_lib.ps_batch_scratch_bytes(C.byref(desc), 1, C.byref(size)) == 0
+    assert size.value >= 16 * 3840 * 2160 * 4
+    for n in (48, 96, 384, 45, 15, 6, 4096, 3000):
+        assert built_lib.ps_plan_desc_init(C.byref(desc), 1) == 0
+        desc.n[0] = n
+        assert built_lib.ps_plan_scratch_bytes(C.byref(desc), C.byref(size)) == 0, n
+    for n in (14, 4100, 5120, 1):
+        desc.n[0] = n
+        assert built_lib.ps_plan_scratch_bytes(C.byref(desc), C.byref(size)) == 2, n
+    assert built_lib.ps_plan_desc_init(C.byref(desc), 2) == 0
+    desc.n[0], desc.n[1] = 48, 48
+    desc.equations = _lib.PS_EQ_MHD
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2
+    assert b"power-of-two" in built_lib.ps_last_error()
+    desc.equations = _lib.PS_EQ_EULER
+    desc.av_mode = _lib.PS_AV_SENSOR
+    assert built_lib.ps_plan_create(C.byref(desc), C.byref(h)) == 2
+    assert b"viscosity" in built_lib.ps_last_error()
+    desc.av_mode = _lib.PS_AV_OFF
+    fake = C.c_void_p(256)  # never dereferenced: the call is refused first
+    assert built_lib.ps_rhs_static(C.byref(desc), fake, fake, None) == 2
+    assert b"powers of two" in built_lib.ps_last_error()
