@@ -15,6 +15,11 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
+// floor(j / d) for 0 <= j < 2^21, through the float reciprocal: (j + 1/2)
+// (1/d) is within (j/d) 2^-22 of its exact value, less than the distance
+// 1/(2d) to the nearest integer.
+__device__ __forceinline__ int qdiv(int j, float inv_d) { return __float2int_rz(((float)j + 0.5f) * inv_d); }
+
 // -i z for the forward transform, +i z for the inverse
 __device__ __forceinline__ float2 rot(float2 z, bool inv) {
   return inv ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x);
@@ -75,27 +80,30 @@ __device__ __forceinline__ void dft_small<5>(float2 (&v)[5], bool inv) {
 // registers (at most MJ of them: ntp >= n/16 keeps ceil(n / (R ntp)) <= MJ),
 // then writes them back.  The register file v is shared by all radices so
 // that the stage loop keeps one set of live values.
-constexpr int kMrV = 20;  // max MJ * R over the radices
-constexpr int kMrJ = 8;   // max MJ
+__host__ __device__ constexpr int mr_mj(int R) { return (kMrDiv + R - 1) / R; }
+__host__ __device__ constexpr int mr_max(int a, int b) { return a > b ? a : b; }
+constexpr int kMrV = mr_max(mr_max(2 * mr_mj(2), 3 * mr_mj(3)), mr_max(4 * mr_mj(4), 5 * mr_mj(5)));
+constexpr int kMrJ = mr_mj(2);
 
 template <int R, int MJ>
-__device__ __forceinline__ void mr_read(const float2* buf, int n, int ns, const float2* __restrict__ tw, int tp,
+__device__ __forceinline__ void mr_read(const float2* buf, int n, int ns, const float2* tw, int tp,
                                         int ntp, bool act, bool inv, float2 (&v)[kMrV], int (&dst)[kMrJ]) {
   static_assert(MJ * R <= kMrV && MJ <= kMrJ, "stage register budget");
   const int nb = n / R;
   const int tstep = n / (ns * R);
+  const float ins = 1.0f / (float)ns;
 #pragma unroll
   for (int jj = 0; jj < MJ; ++jj) {
     const int j = tp + jj * ntp;
     dst[jj] = -1;
     if (act && j < nb) {
-      const int k = j % ns;
+      const int k = j - qdiv(j, ins) * ns;
       float2 x[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         x[r] = buf[j + r * nb];
         if (r > 0) {
-          const float2 w = __ldg(tw + k * r * tstep);
+          const float2 w = tw[k * r * tstep];
           x[r] = inv ? cmulc(x[r], w) : cmul(x[r], w);
         }
       }
@@ -129,15 +137,15 @@ __device__ __forceinline__ void mr_fft(float2* base, int pitch, int npen, const 
 #pragma unroll 1
   for (int s = 0; s < ax.nst; ++s) {
     const int R = (int)((ax.rcode >> (4 * s)) & 15u);
-    if (R == 4) mr_read<4, 4>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
-    else if (R == 3) mr_read<3, 6>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
-    else if (R == 5) mr_read<5, 4>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
-    else mr_read<2, 8>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
+    if (R == 4) mr_read<4, mr_mj(4)>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
+    else if (R == 3) mr_read<3, mr_mj(3)>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
+    else if (R == 5) mr_read<5, mr_mj(5)>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
+    else mr_read<2, mr_mj(2)>(buf, ax.n, ns, ax.tw, tp, ax.ntp, act, inv, v, dst);
     __syncthreads();
-    if (R == 4) mr_write<4, 4>(buf, ns, v, dst);
-    else if (R == 3) mr_write<3, 6>(buf, ns, v, dst);
-    else if (R == 5) mr_write<5, 4>(buf, ns, v, dst);
-    else mr_write<2, 8>(buf, ns, v, dst);
+    if (R == 4) mr_write<4, mr_mj(4)>(buf, ns, v, dst);
+    else if (R == 3) mr_write<3, mr_mj(3)>(buf, ns, v, dst);
+    else if (R == 5) mr_write<5, mr_mj(5)>(buf, ns, v, dst);
+    else mr_write<2, mr_mj(2)>(buf, ns, v, dst);
     __syncthreads();
     ns *= R;
   }
@@ -176,13 +184,15 @@ __device__ __forceinline__ void mr_bases(const MrGeom& g, long* pb) {
 template <typename F>
 __device__ __forceinline__ void mr_each(const MrGeom& g, const long* pb, F&& f) {
   const int tot = g.pg * g.n;
+  const bool rows = g.es == 1;
+  const float inv = 1.0f / (float)(rows ? g.n : g.pg);
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     int q, i;
-    if (g.es == 1) {
-      q = e / g.n;
+    if (rows) {
+      q = qdiv(e, inv);
       i = e - q * g.n;
     } else {
-      i = e / g.pg;
+      i = qdiv(e, inv);
       q = e - i * g.pg;
     }
     const long b = pb[q];
@@ -195,8 +205,9 @@ template <typename F>
 __device__ __forceinline__ void mr_spectra(float2* sig, const MrGeom& g, int nsig, F&& f) {
   const int n = g.n, pitch = n + 1;
   const int tot = nsig * g.pg * n;
+  const float inv = 1.0f / (float)n;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-    const int p2 = e / n, k = e - p2 * n;
+    const int p2 = qdiv(e, inv), k = e - p2 * n;
     f(p2 / g.pg, k, sig[p2 * pitch + k]);
   }
 }
@@ -204,13 +215,17 @@ __device__ __forceinline__ void mr_spectra(float2* sig, const MrGeom& g, int nsi
 // ---------------------------------------------------------------------------
 // out = op(in) along one axis
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_mr_op(MrOpArgs a) {
+__global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_op(MrOpArgs a) {
   extern __shared__ __align__(16) float2 mr_sig[];
   __shared__ long pb[kMrMaxPencils];
   const int sol = blockIdx.y;
   if (a.active != nullptr && a.active[sol] == 0) return;
   mr_bases(a.g, pb);
-  const int pg = a.g.pg, pitch = a.g.n + 1;
+  const int pg = a.g.pg, n = a.g.n, pitch = n + 1;
+  float2* tws = mr_sig + 2 * pg * pitch;  // twiddles W_n^q in shared memory
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = __ldg(a.ax.tw + i);
+  MrAxis ax = a.ax;
+  ax.tw = tws;
   const float* in = a.in + (long)sol * a.ss_in;
   float* out = a.out + (long)sol * a.ss_out;
   for (int f0 = 0; f0 < a.nf; f0 += 4) {
@@ -226,12 +241,12 @@ __global__ void __launch_bounds__(512) k_mr_op(MrOpArgs a) {
         mr_sig[(s * pg + q) * pitch + i] = v;
       }
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, false);
     mr_spectra(mr_sig, a.g, nsig, [&](int, int k, float2& w) {
       if (a.complement) w = cscale(w, complement_factor(a.ax, k));
       else w = mr_symbol(w, k, a.g.n, a.deriv, a.scale, a.kunit, a.ax.P, a.ax.d);
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, true);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long off) {
       if (off < 0) return;
       for (int s = 0; s < nsig; ++s) {
@@ -257,7 +272,7 @@ __global__ void __launch_bounds__(512) k_mr_op(MrOpArgs a) {
 // x pass: [fused filter P_x of the state], CFL speed, G = [D_x F^x, P_x F^y (, P_x F^z)]
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(512) k_mr_x(MrXArgs a) {
+__global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_x(MrXArgs a) {
   constexpr int NC = ND + 2;
   constexpr int NPAIR = (NC + 1) / 2;
   extern __shared__ __align__(16) float2 mr_sig[];
@@ -267,7 +282,11 @@ __global__ void __launch_bounds__(512) k_mr_x(MrXArgs a) {
   if (a.active != nullptr && a.active[sol] == 0) return;
   mr_bases(a.g, pb);
   const int pg = a.g.pg, n = a.g.n, pitch = n + 1;
-  float* prim = reinterpret_cast<float*>(mr_sig + 2 * pg * pitch);  // [NC][pg][n]
+  float2* tws = mr_sig + 2 * pg * pitch;  // twiddles W_n^q in shared memory
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = __ldg(a.ax.tw + i);
+  MrAxis ax = a.ax;
+  ax.tw = tws;
+  float* prim = reinterpret_cast<float*>(tws + n);  // [NC][pg][n]
   auto pv = [&](int c, int q, int i) -> float& { return prim[(c * pg + q) * n + i]; };
   const float er = a.eref[sol];
   const float eshift = a.shift_in ? er : 0.0f;
@@ -293,9 +312,9 @@ __global__ void __launch_bounds__(512) k_mr_x(MrXArgs a) {
           mr_sig[(s * pg + q) * pitch + i] = make_float2(pv(ca, q, i), cb < NC ? pv(cb, q, i) : 0.0f);
         }
       });
-      mr_fft(mr_sig, pitch, nsig * pg, a.ax, false);
+      mr_fft(mr_sig, pitch, nsig * pg, ax, false);
       mr_spectra(mr_sig, a.g, nsig, [&](int, int k, float2& w) { w = cscale(w, complement_factor(a.ax, k)); });
-      mr_fft(mr_sig, pitch, nsig * pg, a.ax, true);
+      mr_fft(mr_sig, pitch, nsig * pg, ax, true);
       mr_each(a.g, pb, [&](int q, int i, long off) {
         for (int s = 0; s < nsig; ++s) {
           const int ca = c0 + 2 * s, cb = ca + 1;
@@ -365,12 +384,12 @@ __global__ void __launch_bounds__(512) k_mr_x(MrXArgs a) {
         mr_sig[(s * pg + q) * pitch + i] = make_float2(flux(dir, c, q, i), (c + 1 < NC) ? flux(dir, c + 1, q, i) : 0.0f);
       }
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, false);
     mr_spectra(mr_sig, a.g, nsig, [&](int s, int k, float2& w) {
       const int dir = (j0 + s) / NPAIR;
       w = mr_symbol(w, k, n, dir == 0 ? 1 : 0, 1.0f, 0.0f, a.ax.P, a.ax.d);
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, true);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long off) {
       if (off < 0) return;
       for (int s = 0; s < nsig; ++s) {
@@ -386,13 +405,17 @@ __global__ void __launch_bounds__(512) k_mr_x(MrXArgs a) {
 // ---------------------------------------------------------------------------
 // 3D y pass: AB = [P_y G + D_y H^y (5), P_y H^z (5)]
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_mr_y3(MrY3Args a) {
+__global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_y3(MrY3Args a) {
   extern __shared__ __align__(16) float2 mr_sig[];
   __shared__ long pb[kMrMaxPencils];
   const int sol = blockIdx.y;
   if (a.active != nullptr && a.active[sol] == 0) return;
   mr_bases(a.g, pb);
   const int pg = a.g.pg, n = a.g.n, pitch = n + 1;
+  float2* tws = mr_sig + 2 * pg * pitch;  // twiddles W_n^q in shared memory
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = __ldg(a.ax.tw + i);
+  MrAxis ax = a.ax;
+  ax.tw = tws;
   const float* G = a.G + (long)sol * a.ssG;
   float* out = a.out + (long)sol * a.ssOut;
   // jobs 0..2: sums over component pairs (0,1), (2,3), (4); jobs 3..5: P_y H^z pairs
@@ -413,13 +436,13 @@ __global__ void __launch_bounds__(512) k_mr_y3(MrY3Args a) {
       mr_sig[q * pitch + i] = za;
       mr_sig[(pg + q) * pitch + i] = zb;
     });
-    mr_fft(mr_sig, pitch, 2 * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, 2 * pg, ax, false);
     mr_spectra(mr_sig, a.g, 1, [&](int, int k, float2& w) {
       const float2 z = mr_sig[(&w - mr_sig) + pg * pitch];
       const float P = __ldg(a.ax.P + k), d = __ldg(a.ax.d + k);
       w = make_float2(fmaf(P, w.x, -d * z.y), fmaf(P, w.y, d * z.x));
     });
-    mr_fft(mr_sig, pitch, pg, a.ax, true);
+    mr_fft(mr_sig, pitch, pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long off) {
       if (off < 0) return;
       const float2 w = mr_sig[q * pitch + i];
@@ -441,9 +464,9 @@ __global__ void __launch_bounds__(512) k_mr_y3(MrY3Args a) {
         mr_sig[(s * pg + q) * pitch + i] = v;
       }
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, false);
     mr_spectra(mr_sig, a.g, nsig, [&](int, int k, float2& w) { w = cscale(w, __ldg(a.ax.P + k)); });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, true);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long off) {
       if (off < 0) return;
       for (int s = 0; s < nsig; ++s) {
@@ -462,7 +485,7 @@ __global__ void __launch_bounds__(512) k_mr_y3(MrY3Args a) {
 // sum acc = U^n + sum w_i k_i, as in the power-of-two last pass.
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(512) k_mr_last(MrLastArgs a) {
+__global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_last(MrLastArgs a) {
   constexpr int NC = ND + 2;
   extern __shared__ __align__(16) float2 mr_sig[];
   __shared__ long pb[kMrMaxPencils];
@@ -470,7 +493,11 @@ __global__ void __launch_bounds__(512) k_mr_last(MrLastArgs a) {
   if (a.active != nullptr && a.active[sol] == 0) return;
   mr_bases(a.g, pb);
   const int pg = a.g.pg, n = a.g.n, pitch = n + 1;
-  float* rb = reinterpret_cast<float*>(mr_sig + 2 * pg * pitch);  // [NC][pg][n]
+  float2* tws = mr_sig + 2 * pg * pitch;  // twiddles W_n^q in shared memory
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = __ldg(a.ax.tw + i);
+  MrAxis ax = a.ax;
+  ax.tw = tws;
+  float* rb = reinterpret_cast<float*>(tws + n);  // [NC][pg][n]
   auto rv = [&](int c, int q, int i) -> float& { return rb[(c * pg + q) * n + i]; };
   const float* AB = a.AB + (long)sol * a.ssAB;
   for (int c = 0; c < NC; c += 2) {
@@ -489,13 +516,13 @@ __global__ void __launch_bounds__(512) k_mr_last(MrLastArgs a) {
       mr_sig[q * pitch + i] = za;
       mr_sig[(pg + q) * pitch + i] = zb;
     });
-    mr_fft(mr_sig, pitch, 2 * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, 2 * pg, ax, false);
     mr_spectra(mr_sig, a.g, 1, [&](int, int k, float2& w) {
       const float2 z = mr_sig[(&w - mr_sig) + pg * pitch];
       const float P = -__ldg(a.ax.P + k), d = -__ldg(a.ax.d + k);
       w = make_float2(fmaf(P, w.x, -d * z.y), fmaf(P, w.y, d * z.x));
     });
-    mr_fft(mr_sig, pitch, pg, a.ax, true);
+    mr_fft(mr_sig, pitch, pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long) {
       const float2 w = mr_sig[q * pitch + i];
       rv(c, q, i) = w.x;
@@ -560,9 +587,9 @@ __global__ void __launch_bounds__(512) k_mr_last(MrLastArgs a) {
         mr_sig[(s * pg + q) * pitch + i] = make_float2(rv(ca, q, i), cb < NC ? rv(cb, q, i) : 0.0f);
       }
     });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, false);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, false);
     mr_spectra(mr_sig, a.g, nsig, [&](int, int k, float2& w) { w = cscale(w, complement_factor(a.ax, k)); });
-    mr_fft(mr_sig, pitch, nsig * pg, a.ax, true);
+    mr_fft(mr_sig, pitch, nsig * pg, ax, true);
     mr_each(a.g, pb, [&](int q, int i, long off) {
       if (off < 0) return;
       for (int s = 0; s < nsig; ++s) {
@@ -579,13 +606,18 @@ __global__ void __launch_bounds__(512) k_mr_last(MrLastArgs a) {
 // 1D stage: k = -D F(U) (+ gravity), increment-form RK update, 1D clamp.  One
 // pencil per solve.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_mr_line(MrLineArgs a) {
+__global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_line(MrLineArgs a) {
   extern __shared__ __align__(16) float2 mr_sig[];
   __shared__ long pb[kMrMaxPencils];
   const int sol = blockIdx.y;
   if (a.active != nullptr && a.active[sol] == 0) return;
   mr_bases(a.g, pb);
-  const int n = a.g.n, pitch = n + 1;
+  const int pg = 1, n = a.g.n, pitch = n + 1;
+  float2* tws = mr_sig + 2 * pg * pitch;  // twiddles W_n^q in shared memory
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = __ldg(a.ax.tw + i);
+  MrAxis ax = a.ax;
+  ax.tw = tws;
+
   const float er = a.eref[sol];
   const float g1 = a.gamma - 1.0f, href = a.gamma * er;
   const float* in = a.in + (long)sol * a.ss;
@@ -597,12 +629,12 @@ __global__ void __launch_bounds__(512) k_mr_line(MrLineArgs a) {
     mr_sig[i] = make_float2(mom, mom * u + p);
     mr_sig[pitch + i] = make_float2(((E + p) + href) * u, 0.0f);
   });
-  mr_fft(mr_sig, pitch, 2, a.ax, false);
+  mr_fft(mr_sig, pitch, 2, ax, false);
   mr_spectra(mr_sig, a.g, 2, [&](int, int k, float2& w) {
     const float dd = __ldg(a.ax.d + k);
     w = make_float2(w.y * dd, -w.x * dd);
   });
-  mr_fft(mr_sig, pitch, 2, a.ax, true);
+  mr_fft(mr_sig, pitch, 2, ax, true);
   const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
   const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   const float pmin_shift = a.p_min - g1 * er;
@@ -665,16 +697,16 @@ MrGeom mr_geom(const MrAxis& ax, long es, long npen, int extra_per_pencil) {
   g.npen = npen;
   const int per = 2 * (ax.n + 1) * (int)sizeof(float2) + extra_per_pencil;
   const int budget = 100 * 1024;  // two or more CTAs per SM where the pencils allow it
-  int pg = 512 / (2 * ax.ntp);
+  int pg = kMrThreads / (2 * ax.ntp);
   if (pg < 1) pg = 1;
-  while (pg > 1 && pg * per > budget) --pg;
+  while (pg > 1 && pg * per + ax.n * (int)sizeof(float2) > budget) --pg;
   if (pg > kMrMaxPencils) pg = kMrMaxPencils;
   if (pg > npen) pg = (int)npen;
   if (pg < 1) pg = 1;
   g.pg = pg;
   const int t = 2 * pg * ax.ntp;
   g.threads = (t + 31) / 32 * 32;
-  g.smem = pg * per;
+  g.smem = pg * per + ax.n * (int)sizeof(float2);  // + the twiddle table
   return g;
 }
 

@@ -34,13 +34,25 @@ namespace ps {
 constexpr int kMrMaxStages = 14;  // 4 bits each in MrAxis::rcode
 constexpr int kMrMaxLen = 4096;
 constexpr int kMrMaxPencils = 64;  // pencils per CTA
+#ifndef MR_DIV
+#define MR_DIV 12
+#endif
+#ifndef MR_LB
+#define MR_LB 768
+#endif
+#ifndef MR_MINB
+#define MR_MINB 1
+#endif
+constexpr int kMrDiv = MR_DIV;         // values a thread holds per stage: ntp = ceil(n / kMrDiv)
+constexpr int kMrThreads = MR_LB;      // threads per CTA at most
+constexpr int kMrMinBlocks = MR_MINB;  // resident CTAs per SM the register allocation allows
 
 // One Fourier axis: factorisation, threads per pencil and device tables.
 struct MrAxis {
   int n;                     // pencil length
   int nst;                   // Stockham stages
   unsigned long long rcode;  // radix of stage s in bits [4s, 4s + 4)
-  int ntp;                   // threads per pencil (>= ceil(n / 16))
+  int ntp;                   // threads per pencil, ceil(n / kMrDiv)
   const float2* tw;          // W_n^q = exp(-2 pi i q / n), q < n
   const float* P;            // m s / n
   const float* d;            // kphys m s / n, zero at the Nyquist index of even n

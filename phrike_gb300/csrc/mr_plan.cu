@@ -89,7 +89,9 @@ int mr_setup(ps_plan p) {
     ax.n = N;
     ax.rcode = 0;
     for (int s = 0; s < ax.nst; ++s) ax.rcode |= (unsigned long long)radix[s] << (4 * s);
-    ax.ntp = (N + 15) / 16;
+    ax.ntp = (N + kMrDiv - 1) / kMrDiv;
+    if (2 * ax.ntp > kMrThreads)  // two signals of one pencil per CTA at least
+      return errorf(PS_ERR_UNSUPPORTED, "axis %d: N=%d needs more than %d threads per CTA", a, N, kMrThreads);
     ax.tw = p->twf[a];
     ax.P = p->P[a];
     ax.d = p->d[a];
