@@ -133,7 +133,13 @@ int ps_batch_scratch_bytes(const ps_plan_desc* desc, int nsolve, size_t* bytes);
  * LegendreLobattoBasis2D, basis/legendre.py:894-934): n >= 3 nodes per axis,
  * solid walls (bc "dirichlet", grid.py:994-1154) applied in place to every
  * stage input and after every step, the 2D positivity clamp after every RK
- * stage, the nodal filter (legendre.py:825-859) when enabled. */
+ * stage, the nodal filter (legendre.py:825-859) when enabled.
+ * Fourier axis lengths: any N whose prime factors are 2, 3 and 5, from 2 to
+ * 4096 (the reference's grids take any N, grid.py:47-63, 87-115).  Powers of
+ * two from 8 to 1024 (to 4096 in 1D) run on register-resident pencils; other
+ * lengths run on mixed-radix passes with the same results, for the Euler
+ * equations without artificial viscosity (MHD and viscosity return
+ * PS_ERR_UNSUPPORTED there, and so does 1D adaptive stepping). */
 int ps_plan_create(const ps_plan_desc* desc, ps_plan* out);
 int ps_plan_destroy(ps_plan plan);
 
