@@ -295,12 +295,28 @@ int ps_project_state(ps_plan plan, float* U, void* stream);
  * the exact trigonometric interpolant the reference evaluates without finufft
  * (and to its eps = 1e-6 with it).  f holds nf (1..3) fields of the plan's
  * grid (solve 0), points is [ndim][npoints] float64 (x row, then y, z), out
- * [nf][npoints] float32.  Cost O(npoints x cells).  Fourier plans only.
+ * [nf][npoints] float32.  Fourier plans only; see ps_tracer_method for the
+ * interpolation (exact, O(npoints x cells), or NUFFT).
  * Replaces Grid1D.evaluate_fourier_at_points_1d (grid.py:581-618),
  * Grid2D.evaluate_fourier_at_points (grid.py:1180-1222) and the 3D single
  * and batched forms (grid.py:1520-1632). */
 int ps_eval_points(ps_plan plan, const float* f, int nf, const double* points, int npoints, float* out,
                    void* stream);
+
+/* How ps_eval_points and ps_tracers_step interpolate:
+ *   PS_TRACERS_EXACT  the exact trigonometric interpolant, O(npoints x cells);
+ *   PS_TRACERS_NUFFT  type-2 NUFFT interpolation (the method of the
+ *                     reference's finufft branch, grid.py:611, 1214, 1555):
+ *                     exponential-of-semicircle kernel, 8 points per axis on a
+ *                     2x oversampled grid, within 1e-6 of the exact
+ *                     interpolant; O(cells log cells + npoints); axes of
+ *                     2^a 3^b 5^c points up to 2048;
+ *   PS_TRACERS_AUTO   (default) NUFFT once npoints x cells exceeds 2^24 and the
+ *                     grid allows it, else exact. */
+#define PS_TRACERS_AUTO 0
+#define PS_TRACERS_EXACT 1
+#define PS_TRACERS_NUFFT 2
+int ps_tracer_method(ps_plan plan, int method);
 
 /* One leap-frog step of tracer particles in the velocity u_a = U[1+a]/U[0]
  * of the state U (solve 0), interpolated as in ps_eval_points:

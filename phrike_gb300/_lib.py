@@ -20,6 +20,7 @@ PS_BASIS_LEGENDRE = 1
 PS_EQ_EULER = 0
 PS_EQ_MHD = 1
 PS_AV_OFF, PS_AV_SENSOR, PS_AV_CONSTANT = 0, 1, 2
+PS_TRACERS_AUTO, PS_TRACERS_EXACT, PS_TRACERS_NUFFT = 0, 1, 2
 PS_AV_Q_DENSITY, PS_AV_Q_PRESSURE, PS_AV_Q_SPEED = 0, 1, 2
 PS_OP_P, PS_OP_D, PS_OP_L = 0, 1, 2
 PS_SCHEME_RK4, PS_SCHEME_RK2 = 0, 1
@@ -115,6 +116,7 @@ _SIGNATURES = [
     ("ps_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_profile_collect", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
+    ("ps_tracer_method", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_rhs_static", C.c_int, [C.POINTER(PlanDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_lgl_build", C.c_int, [C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ps_apply_boundary_conditions", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

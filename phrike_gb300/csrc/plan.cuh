@@ -94,6 +94,14 @@ struct ps_plan_s {
   // Fourier axes of any 5-smooth length (mixed-radix passes, mr_plan.cu)
   bool mr = false;
   ps::MrAxis mrax[3] = {};
+  // point evaluation: 0 auto, 1 exact interpolant, 2 NUFFT (nufft.cu, tables made on first use)
+  int tracer_method = 0;
+  bool nu_ready = false;
+  ps::MrAxis nu_axn[3] = {}, nu_axm[3] = {};
+  float* nu_s[3] = {nullptr, nullptr, nullptr};
+  float* nu_g = nullptr;    // [3][2Nz][2Ny][2Nx] oversampled grid (real part)
+  float2* nu_t1 = nullptr;  // x resampled
+  float2* nu_t2 = nullptr;  // x and y resampled (3D)
 
   ps::AxisOps ax(int a) const { return ps::AxisOps{P[a], d[a], twf[a], twi[a]}; }
   long ss(int nf) const { return (long)nf * cells; }  // solve stride of an nf-field buffer
@@ -197,5 +205,10 @@ int mr_last(ps_plan p, int stage, const float* Un, float* out, double dt, const 
             const int* active, cudaStream_t s);
 int mr_steps_1d(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, double* d_t, const double* d_tend,
                 cudaStream_t s);
+
+// NUFFT point evaluation (nufft.cu)
+bool nufft_supported(const ps_plan_s* p);
+int nufft_points(ps_plan p, const float* f, int nf, bool velocity, double* pos, double* prev, int np, int first,
+                 double dt, float* out, cudaStream_t s);
 
 }  // namespace ps

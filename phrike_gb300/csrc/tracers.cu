@@ -291,10 +291,31 @@ int tracer_args(ps_plan p, TracerArgs& a) {
   return PS_OK;
 }
 
+// Exact interpolant or NUFFT: the plan's choice; automatic picks NUFFT once
+// points x cells exceeds 2^24 (the exact sweep's cost) where the grid allows it
+int tracer_route(ps_plan p, int np, bool* nu) {
+  const bool ok = nufft_supported(p);
+  if (p->tracer_method == PS_TRACERS_NUFFT && !ok)
+    return errorf(PS_ERR_UNSUPPORTED, "NUFFT point evaluation needs Fourier axes of 2^a 3^b 5^c points up to 2048");
+  *nu = (p->tracer_method == PS_TRACERS_NUFFT) ||
+        (p->tracer_method == PS_TRACERS_AUTO && ok && (double)np * (double)p->cells > 16777216.0);
+  return PS_OK;
+}
+
 }  // namespace
 }  // namespace ps
 
 extern "C" {
+
+int ps_tracer_method(ps_plan p, int method) {
+  if (p == nullptr) return ps::errorf(PS_ERR_INVALID, "null plan");
+  if (method < PS_TRACERS_AUTO || method > PS_TRACERS_NUFFT)
+    return ps::errorf(PS_ERR_INVALID, "method must be PS_TRACERS_AUTO, PS_TRACERS_EXACT or PS_TRACERS_NUFFT");
+  if (method == PS_TRACERS_NUFFT && !ps::nufft_supported(p))
+    return ps::errorf(PS_ERR_UNSUPPORTED, "NUFFT point evaluation needs Fourier axes of 2^a 3^b 5^c points up to 2048");
+  p->tracer_method = method;
+  return PS_OK;
+}
 
 int ps_eval_points(ps_plan p, const float* f, int nf, const double* points, int npoints, float* out, void* stream) {
   ps::TracerArgs a{};
@@ -303,6 +324,11 @@ int ps_eval_points(ps_plan p, const float* f, int nf, const double* points, int 
   if (nf < 1 || nf > 3) return ps::errorf(PS_ERR_INVALID, "nf must be 1..3 (got %d)", nf);
   if (npoints < 0 || (npoints > 0 && (f == nullptr || points == nullptr || out == nullptr)))
     return ps::errorf(PS_ERR_INVALID, "null buffer or negative point count");
+  bool nu = false;
+  if ((rc = ps::tracer_route(p, npoints, &nu)) != PS_OK) return rc;
+  if (nu)
+    return ps::nufft_points(p, f, nf, false, const_cast<double*>(points), nullptr, npoints, 0, 0.0, out,
+                            (cudaStream_t)stream);
   a.f = f;
   a.velocity = 0;
   a.nf = nf;
@@ -322,6 +348,10 @@ int ps_tracers_step(ps_plan p, const float* U, double* pos, double* prev, int np
   if (rc != PS_OK) return rc;
   if (npoints < 0 || (npoints > 0 && (U == nullptr || pos == nullptr || prev == nullptr)))
     return ps::errorf(PS_ERR_INVALID, "null buffer or negative tracer count");
+  bool nu = false;
+  if ((rc = ps::tracer_route(p, npoints, &nu)) != PS_OK) return rc;
+  if (nu)
+    return ps::nufft_points(p, U, p->nd, true, pos, prev, npoints, first, dt, velocity_out, (cudaStream_t)stream);
   a.f = U;
   a.velocity = 1;
   a.nf = p->nd;

@@ -366,6 +366,16 @@ class Plan:
             raise RuntimeError("position arrays differ in length")
         return int(pts.shape[1])
 
+    def tracer_method(self, method: str) -> None:
+        """Interpolation of eval_points / tracers_step_: "auto" (NUFFT once
+        points x cells exceeds 2^24, where the grid allows it), "exact" (the
+        trigonometric interpolant, O(points x cells)) or "nufft" (type-2
+        NUFFT, within 1e-6 of the exact interpolant)."""
+        codes = {"auto": _lib.PS_TRACERS_AUTO, "exact": _lib.PS_TRACERS_EXACT, "nufft": _lib.PS_TRACERS_NUFFT}
+        if method not in codes:
+            raise ValueError(f"tracer method must be one of {sorted(codes)}, got {method!r}")
+        _lib.check(self._lib.ps_tracer_method(self._handle, codes[method]))
+
     def eval_points(self, f: torch.Tensor, points: torch.Tensor, out: Optional[torch.Tensor] = None
                     ) -> torch.Tensor:
         """Spectral interpolant of the fields f (nf, *shape) (nf <= 3, one
