@@ -103,6 +103,15 @@ cudaError_t last_t_T(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, cons
   } else if (a.mhd) {
     if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;
     k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+  } else if (a.rhs2d && a.stage < 0) {
+    // the right-hand side alone: the unclamped body holds one pair of
+    // components at a time (fewer registers, more CTAs per SM)
+    if constexpr (NN >= 256) {
+      if ((e = set_smem(k_last_t<NN, T, 2, false, R>, sm)) != cudaSuccess) return e;
+      k_last_t<NN, T, 2, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+    } else {
+      return cudaErrorInvalidValue;
+    }
   } else {
     if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;
     k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);

@@ -141,6 +141,7 @@ int stage_tc(ps_plan p, const float* in, int st, const float* Un, float* out, do
   LglUpdateArgs u{};
   u.Gx = Gx;
   u.Gy = Gy;
+  u.ksign = -1.0f;
   u.Un = Un;
   u.acc = p->acc;
   u.out = out;

@@ -377,7 +377,8 @@ __global__ void k_lgl_update(LglUpdateArgs a) {
   for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < cells; o += (long)gridDim.x * blockDim.x) {
     float k[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) k[c] = -(a.Gx[so + c * cells + o] + a.Gy[so + c * cells + o]);
+    for (int c = 0; c < 4; ++c)
+      k[c] = a.ksign * (a.Gy != nullptr ? a.Gx[so + c * cells + o] + a.Gy[so + c * cells + o] : a.Gx[so + c * cells + o]);
     if (a.gravity) {  // rho g on the momenta, g . m on the energy (solver.py:453-464)
       const float rho = a.Uin[so + o], mx = a.Uin[so + cells + o], my = a.Uin[so + 2 * cells + o];
       k[1] = fmaf(rho, a.g[0], k[1]);

@@ -43,10 +43,13 @@ int encode_split_map(CUtensorMap* m, const void* base, int nk, int rows, int bat
 int umma_n_tile(int M, int N, int batch);
 cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const UmmaArgs& g, int nt, cudaStream_t s);
 
-// k = -(Gx + Gy); stage -1 writes k, stages 0..3 the RK4 update and clamp
+// k = ksign (Gx + Gy) (LGL: ksign = -1; a Fourier right-hand side R passed
+// as Gx with Gy null: ksign = 1); stage -1 writes k, stages 0..3 the RK4
+// update and the 2D clamp
 struct LglUpdateArgs {
   const float* Gx;
-  const float* Gy;
+  const float* Gy;    // may be null
+  float ksign;
   const float* Un;
   float* acc;
   float* out;

@@ -301,6 +301,7 @@ struct LastTArgs {
   float grav[3];
   int gravity;
   int rk2;             // midpoint RK2 coefficients (stages 0 and 3 only)
+  int rhs2d;           // 2D Euler, stage -1: the unclamped instantiation writes the right-hand side
 };
 
 // Gravity source at one point of solve-local offset o (element index of

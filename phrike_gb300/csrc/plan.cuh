@@ -31,6 +31,10 @@ struct ps_plan_s {
   float* acc = nullptr;  // RK accumulator (nc fields)
   float* Us = nullptr;   // stage input (nc fields)
   float* F1 = nullptr;   // 1D flux for ps_rhs (3 fields)
+  // 2D Euler from 256 rows: the last pass writes the right-hand side R (4
+  // fields) and an elementwise kernel applies the RK stage and the clamp
+  bool split2d = false;
+  float* R2 = nullptr;
   // per-solve device scalars
   float* speed = nullptr;  // CFL wave speed maxima
   float* eref = nullptr;   // E_ref of the energy-perturbation form

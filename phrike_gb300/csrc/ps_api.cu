@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/phrike_gb300.h"
+#include "lgl_tc.cuh"
 #include "adaptive.cuh"
 #include "av.cuh"
 #include "launch.cuh"
@@ -86,6 +87,15 @@ bool pow2_axes(const ps_plan_desc* d) {
 
 // a Fourier grid with some other axis length: the mixed-radix passes
 bool is_mr(const ps_plan_desc* d) { return !is_lgl(d) && !pow2_axes(d); }
+
+// 2D Euler on power-of-two grids from 256 rows: the last pass is split into
+// the right-hand side and an elementwise stage update (the clamped last pass
+// holds every component's right-hand side in registers and runs one CTA per
+// SM at these lengths).  Chosen from the grid alone, so a solve gives the
+// same bits alone and in a batch.
+bool split2d_grid(const ps_plan_desc* d) {
+  return d->ndim == 2 && d->equations == PS_EQ_EULER && !is_lgl(d) && !is_mr(d) && d->n[1] >= 256;
+}
 
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
@@ -406,6 +416,40 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
     ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * p->nsolve * p->nc * (2 + st_words));
     return ps::mr_last(p, stage, Un, out, dt, d_dt, filter_last, active, s);
   }
+  if (p->split2d && stage >= 0) {
+    // 2D Euler from 256 rows: the right-hand side of the stage input (with
+    // gravity) into R, the RK stage and the clamp elementwise (increment-form
+    // accumulator), then the y factor of the end-of-step filter
+    const float* in = (stage == 0) ? Un : p->Us;
+    if ((rc = last(p, -1, in, p->R2, 0.0, nullptr, false, s, active)) != PS_OK) return rc;
+    ps::LglUpdateArgs u{};
+    u.Gx = p->R2;
+    u.Gy = nullptr;
+    u.ksign = 1.0f;
+    u.Un = Un;
+    u.acc = p->acc;
+    u.out = out;
+    u.cells = p->cells;
+    u.nsolve = p->nsolve;
+    u.stage = stage;
+    u.dt_dev = d_dt;
+    u.dt = dt;
+    u.gamma = (float)p->desc.gamma;
+    u.rho_min = 1e-8f;  // _positivity_clamp_2d floors (solver.py:467)
+    u.p_min = 1e-10f;
+    u.eref = p->eref;
+    u.active = active;
+    u.gravity = 0;  // already in R
+    u.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+    {
+      const double words = (stage == 0) ? 16.0 : 20.0;
+      ProfScope prof(p, s, PS_KIND_LAST, words * 4.0 * p->cells * p->nsolve);
+      PS_CU(ps::launch_lgl_update(u, s), "stage update");
+    }
+    if (stage == 3 && filter_last && (rc = apply_op(p, 1, out, out, p->nc, 0, 1.0f, s, true, active)) != PS_OK)
+      return rc;
+    return PS_OK;
+  }
   if ((rc = state_maps(p, Un)) != PS_OK) return rc;
   ps::LastTArgs a{};
   const int nc = p->nc;
@@ -460,6 +504,7 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   }
   if (p->mhd) a.gravity = 0;
   a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+  a.rhs2d = (p->split2d && stage < 0) ? 1 : 0;
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
@@ -1092,6 +1137,8 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if (p->nd == 3 && !mhd3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
+    if (split2d_grid(d) && (rc = dalloc(p, &p->R2, 4 * c)) != PS_OK) return cleanup(rc);
+    p->split2d = split2d_grid(d);
   }
   p->av = av_params(d);
   if (p->nd == 2 && !lgl && !mr) {
@@ -1194,6 +1241,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   }
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
   if (is_mr(d) && d->ndim == 1) fields += 6;  // stage input and increments
+  if (split2d_grid(d)) fields += 4;            // the 2D right-hand side
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
   const bool mhd = d->equations == PS_EQ_MHD;
   if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator
