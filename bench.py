@@ -235,6 +235,21 @@ def run_gb300(args, rank: int, world: int):
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_value = cells * e2e_steps * world / float(te.item())
     state_bytes = U.numel() * 4
+    # the same with the copies in line: each step waits for its state to land,
+    # steps, and copies the result back before the next state is sent
+    dev_state = torch.empty_like(U)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dev_state.copy_(hin, non_blocking=True)
+        plan.step_(dev_state, DT)
+        hout.copy_(dev_state, non_blocking=True)
+        torch.cuda.synchronize()
+    ti = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(ti, op=dist.ReduceOp.MAX)
+    e2e_inline = cells * e2e_steps * world / float(ti.item())
 
     if rank != 0:
         return
@@ -275,7 +290,10 @@ def run_gb300(args, rank: int, world: int):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "steps": e2e_steps,
                 "path": "phrike_gb300.engine.Plan.step_host_stream -> ps_step_rk4 (C ABI): pinned host state "
-                        "in and out every step, copies of neighbouring states overlapped with each step"},
+                        "in and out every step, copies of neighbouring states overlapped with each step",
+                "inline_value": e2e_inline,
+                "inline_path": "per step: pinned host state to the device, Plan.step_ (ps_step_rk4), result back "
+                               "to pinned host memory, synchronize; no overlap"},
         "gpu_launches": sum(v["launches"] for v in prof.values()),
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -515,8 +533,44 @@ def run_lgl(args):
             row[prec] = ent
             plan.close()
         table.append(row)
+    # a batch of --lgl-batch solves of the last size on the tensor cores: the
+    # contraction of one solve fills one wave of CTAs; a batch fills the GPU
+    batch = None
+    if args.lgl_batch > 1:
+        n = int(args.lgl_sizes.split(",")[-1])
+        ax = L.LGLAxis(n, 2.0)
+        U0 = problems.acoustic_pulse_lgl_2d(ax.x - 1.0, ax.x - 1.0, gamma=1.4)
+        nb = args.lgl_batch
+        plan = Plan((n, n), (2.0, 2.0), gamma=1.4, basis="legendre", gemm_precision="bf16x3", device=device,
+                    nsolve=nb)
+        UB = torch.as_tensor(np.stack([U0] * nb), dtype=torch.float32, device=device).contiguous()
+        plan.run_(UB, 3, dt)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bsteps = max(10, min(nsteps, 50))
+        e0.record(st)
+        plan.run_(UB, bsteps, dt)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / bsteps
+        plan.profile(True)
+        plan.run_(UB, 3, dt)
+        prof = plan.collect_profile()
+        plan.profile(False)
+        batch = {"solves": nb, "n": n, "ms_per_step": ms, "cell_updates_per_s": nb * n * n / (ms * 1e-3),
+                 "status": plan.status()}
+        fl = 3 * 2.0 * (4 * n) * n * n * nb
+        for kind in ("lgl_x", "lgl_y"):
+            if kind in prof:
+                per = prof[kind]["ms"] / prof[kind]["launches"]
+                batch[f"{kind}_us"] = per * 1e3
+                batch[f"{kind}_tflops_issued"] = fl / (per * 1e-3) / 1e12
+                batch[f"{kind}_tensor_frac_of_measured_bf16"] = fl / (per * 1e-3) / 1e12 / tc_peak
+        plan.close()
     line = {
         "metric": "LGL 2D acoustic pulse: cell-updates/s and rel-L2 vs float64 oracle per contraction precision",
+        "batch_bf16x3": batch,
         "value": headline, "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
         "data": "synthetic (analytic acoustic pulse initial condition)",
         "config": {"workload": f"LGL x LGL acoustic pulse, walls, RK4 dt=1e-5, {nsteps} steps, "
@@ -1117,6 +1171,7 @@ def main():
     ap.add_argument("--plain-t-end", type=float, default=0.05)
     ap.add_argument("--lgl-sizes", default="257,513")
     ap.add_argument("--lgl-steps", type=int, default=500)
+    ap.add_argument("--lgl-batch", type=int, default=16)
     ap.add_argument("--nsolve", type=int, default=512)
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--chunk", type=int, default=50)
