@@ -541,9 +541,11 @@ def run_lgl(args):
         ax = L.LGLAxis(n, 2.0)
         U0 = problems.acoustic_pulse_lgl_2d(ax.x - 1.0, ax.x - 1.0, gamma=1.4)
         nb = args.lgl_batch
-        plan = Plan((n, n), (2.0, 2.0), gamma=1.4, basis="legendre", gemm_precision="bf16x3", device=device,
-                    nsolve=nb)
         UB = torch.as_tensor(np.stack([U0] * nb), dtype=torch.float32, device=device).contiguous()
+        from phrike_gb300.autotune import tune_umma_n_tile
+        nt, nt_times = tune_umma_n_tile((n, n), (2.0, 2.0), UB, nsolve=nb, dt=dt, gamma=1.4, device=device)
+        plan = Plan((n, n), (2.0, 2.0), gamma=1.4, basis="legendre", gemm_precision="bf16x3", device=device,
+                    nsolve=nb, umma_n_tile=nt)
         plan.run_(UB, 3, dt)
         torch.cuda.synchronize()
         st = torch.cuda.current_stream(device)
@@ -559,7 +561,8 @@ def run_lgl(args):
         prof = plan.collect_profile()
         plan.profile(False)
         batch = {"solves": nb, "n": n, "ms_per_step": ms, "cell_updates_per_s": nb * n * n / (ms * 1e-3),
-                 "status": plan.status()}
+                 "status": plan.status(), "umma_n_tile": nt,
+                 "umma_n_tile_ms_per_step": {str(k): v for k, v in nt_times.items()}}
         fl = 3 * 2.0 * (4 * n) * n * n * nb
         for kind in ("lgl_x", "lgl_y"):
             if kind in prof:

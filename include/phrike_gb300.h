@@ -100,10 +100,16 @@ typedef struct {
    * grid.py:620-735).  Default: walls, {0, 1, 0, 0, 1, 0}. */
   int lgl_bc1d[6];
   /* 2D Fourier plans: columns per tile of the strided passes, 4, 8 or 16 (at
-   * most the plan's cap: 16 up to 256-point y pencils, 8 at 256-511 (Euler),
-   * 4 beyond); 0 (default): the plan's heuristic.  The arithmetic of a pencil
-   * does not depend on it; phrike_gb300/autotune.py picks it by timing. */
+   * most the plan's cap: 16 below 256-point y pencils, then 8 (Euler to 1023
+   * points, MHD beyond), 4 for Euler from 1024); 0 (default): the plan's
+   * heuristic.  The arithmetic of a pencil does not depend on it;
+   * phrike_gb300/autotune.py picks it by timing. */
   int tile_cols;
+  /* LGL x LGL plans with PS_GEMM_BF16X3: N tile of the tcgen05 contractions,
+   * 64, 128, 176 or 256 columns; 0 (default): the smallest tile whose grid
+   * fits one wave, else 256.  Every output element is the same dot product
+   * for every tile; phrike_gb300/autotune.py picks it by timing. */
+  int umma_n_tile;
 } ps_plan_desc;
 
 #define PS_SCHEME_RK4 0

@@ -68,6 +68,7 @@ class PlanDesc(C.Structure):
         ("mhd_cfl_diff", C.c_double),
         ("lgl_bc1d", C.c_int * 6),
         ("tile_cols", C.c_int),
+        ("umma_n_tile", C.c_int),
     ]
 
 

@@ -371,6 +371,12 @@ int lgl_setup(ps_plan p) {
     // A operands (128-row boxes): D_x and F_y^T; B operands (N-tile boxes): F_x and D_y
     p->nt_x = umma_n_tile(nx, p->nsolve * 4 * ny, 1);
     p->nt_y = umma_n_tile(nx, ny, p->nsolve * 4);
+    const int nt = p->desc.umma_n_tile;
+    if (nt != 0) {  // an explicit tile (autotuner)
+      if (nt != 64 && nt != 128 && nt != 176 && nt != 256)
+        return errorf(PS_ERR_INVALID, "umma_n_tile must be 0, 64, 128, 176 or 256 (got %d)", nt);
+      p->nt_x = p->nt_y = nt;
+    }
     int e = 0;
     if ((e = encode_split_map(&p->map_Dx, p->Dsplit[0], nx, nx, 1, p->pitch[0], 128)) != 0 ||
         (e = encode_split_map(&p->map_FX, p->FX, nx, p->nsolve * 4 * ny, 1, p->pitch[0], p->nt_x)) != 0 ||

@@ -55,7 +55,7 @@ class Plan:
                  device: Optional[torch.device] = None, nsolve: int = 1, basis: str = "fourier",
                  gemm_precision: str = "fp32", equations: str = "euler", mhd_config: Optional[Dict] = None,
                  av_config: Optional[Dict] = None, scheme: str = "rk4", lgl_bc1d: Optional[Sequence[int]] = None,
-                 tile_cols: Optional[int] = None):
+                 tile_cols: Optional[int] = None, umma_n_tile: Optional[int] = None):
         lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -126,6 +126,8 @@ class Plan:
                 desc.av_weight[c] = float(wts.get(names[c], 1.0))
         if tile_cols is not None:  # 2D strided-pass tile width (ps_plan_desc.tile_cols; autotune.py)
             desc.tile_cols = int(tile_cols)
+        if umma_n_tile is not None:  # N tile of the tcgen05 LGL contractions (autotune.py)
+            desc.umma_n_tile = int(umma_n_tile)
         if lgl_bc1d is not None:  # 1D Legendre boundary codes (ps_plan_desc.lgl_bc1d)
             for i, c in enumerate(lgl_bc1d):
                 desc.lgl_bc1d[i] = int(c)

@@ -129,9 +129,10 @@ def _plan_kw(family: str, device) -> dict:
                 equations=o.get("equations", "euler"))
 
 
-def make_plan(family: str, n: int, nsolve: int, device, tile_cols: Optional[int] = None) -> Plan:
+def make_plan(family: str, n: int, nsolve: int, device, tile_cols: Optional[int] = None,
+              umma_n_tile: Optional[int] = None) -> Plan:
     return Plan(family_shape(family, n), family_lengths(family, n), nsolve=nsolve, tile_cols=tile_cols,
-                **_plan_kw(family, device))
+                umma_n_tile=umma_n_tile, **_plan_kw(family, device))
 
 
 def _prepare_state(req: Request, device, projector: Optional[Plan]) -> torch.Tensor:
@@ -252,12 +253,16 @@ class Server:
         shape = family_shape(family, n)
         ben = _benign_state(family, shape, FAMILIES[family]["gamma"])
         U = torch.as_tensor(np.stack([ben] * slots), dtype=torch.float32, device=self.device).contiguous()
-        tc = None
+        tc = nt = None
         if self.autotune and len(shape) == 2 and FAMILIES[family].get("basis", "fourier") == "fourier":
             from .autotune import tune_tile_cols
             tc, _ = tune_tile_cols(shape, family_lengths(family, n), U, nsolve=slots,
                                    **_plan_kw(family, self.device))
-        plan = make_plan(family, n, slots, self.device, tile_cols=tc)
+        if self.autotune and len(shape) == 2 and FAMILIES[family].get("gemm_precision") == "bf16x3":
+            from .autotune import tune_umma_n_tile
+            kw = {k: v for k, v in _plan_kw(family, self.device).items() if k not in ("basis", "gemm_precision")}
+            nt, _ = tune_umma_n_tile(shape, family_lengths(family, n), U, nsolve=slots, **kw)
+        plan = make_plan(family, n, slots, self.device, tile_cols=tc, umma_n_tile=nt)
         t = torch.zeros(slots, dtype=torch.float64, device=self.device)
         te = torch.zeros(slots, dtype=torch.float64, device=self.device)  # t >= t_end: free
         high = self.cost is not None and float(self.cost(family, n)) >= self.priority_seconds

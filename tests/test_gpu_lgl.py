@@ -277,3 +277,32 @@ def test_lgl_properties_257(cuda_device):
     np.testing.assert_array_equal(G[2][0, :], 0.0)
     assert p.status() == 0
     del torch
+
+
+def test_tensor_core_n_tiles_give_the_same_bits(cuda_device):
+    """The N tile of the tcgen05 contractions (64, 128, 176, 256 and the
+    plan's own choice) changes which columns a CTA computes, not the dot
+    product of any output value: two solves stepped five times end bitwise
+    equal for every tile; the autotuner returns one of them."""
+    import torch
+    from phrike_gb300.autotune import tune_umma_n_tile
+    from phrike_gb300.engine import Plan
+    n = 65
+    ax = L.LGLAxis(n, 2.0)
+    U0 = problems.acoustic_pulse_lgl_2d(ax.x - 1.0, ax.x - 1.0, gamma=GAMMA)
+    UB = torch.as_tensor(np.stack([U0, U0[:, ::-1, :].copy()]), dtype=torch.float32, device=cuda_device).contiguous()
+    outs = []
+    for nt in (None, 64, 128, 176, 256):
+        plan = Plan((n, n), (2.0, 2.0), gamma=GAMMA, basis="legendre", gemm_precision="bf16x3", nsolve=2,
+                    umma_n_tile=nt, device=cuda_device)
+        V = UB.clone()
+        plan.run_(V, 5, 1e-5)
+        assert plan.status() == 0
+        outs.append(V)
+        plan.close()
+    for V in outs[1:]:
+        assert torch.equal(outs[0], V)
+    best, times = tune_umma_n_tile((n, n), (2.0, 2.0), UB, nsolve=2, gamma=GAMMA, device=cuda_device)
+    assert best in (64, 128, 176, 256) and set(times) == {64, 128, 176, 256}
+    with pytest.raises(RuntimeError):
+        Plan((n, n), (2.0, 2.0), basis="legendre", gemm_precision="bf16x3", umma_n_tile=96, device=cuda_device)
