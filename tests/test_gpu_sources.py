@@ -131,3 +131,30 @@ def test_artificial_viscosity_2d_batch_and_cfl(cuda_device):
     p.run_cfl_(U, steps + 2, tt, te)
     assert p.steps_done() == [steps]
     assert max(_errs(U.cpu().numpy(), R)) < 2e-5
+
+
+@pytest.mark.parametrize("scheme", ["rk4", "rk2"])
+def test_split_2d_last_pass_with_viscosity_and_gravity_vs_oracle(cuda_device, scheme):
+    """From 256 rows the 2D Euler last pass runs as a right-hand-side pass and
+    an elementwise stage update: KHI 256 x 128 (Ny x Nx) with sensor
+    artificial viscosity (filter cadence 5, as the 2D solver sets it with AV),
+    gravity and the filter, RK4 and midpoint RK2, against the oracle."""
+    from oracle import spectral as O
+    from phrike_gb300.engine import Plan
+    ny, nx = 256, 128
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    U0 = problems.kelvin_helmholtz_2d(nx, ny, U0=1.0, A=0.01)
+    U0f = U0.astype(np.float32).astype(np.float64)
+    box = O.FourierBox((ny, nx), (1.0, 1.0), dealias=True, filter_enabled=True)
+    s = O.EulerSolver(box, cfl=0.4, gravity=[0.3, -1.0], av=AV_SENSOR, filter_interval=5, scheme=scheme)
+    dt = 0.5 * s.compute_dt(U0f)
+    R = U0f
+    for _ in range(12):
+        R = s.step(R, dt)
+    plan = Plan((ny, nx), (1.0, 1.0), filter_params=dict(fp, interval=5), gravity=[0.3, -1.0],
+                av_config=AV_SENSOR, scheme=scheme)
+    U = _dev(U0)
+    plan.run_(U, 12, dt)
+    errs = _errs(U.cpu().numpy(), R)
+    print(f"\nsplit 2D last pass ({scheme}) 12 steps rel-L2 {errs}")
+    assert max(errs) < 1e-5, errs
