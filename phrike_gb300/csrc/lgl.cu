@@ -393,31 +393,47 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
 }
 
 // Large tiles when they already give about one CTA per SM, else small ones.
-static bool big_tiles(int nx, int ny, int nsolve) {
-  const long ctas = (long)((nx + 63) / 64) * ((ny + 31) / 32) * nsolve;
-  return ctas >= 148;
+// Tile of the CUDA-core contractions: 32 x 64 outputs per 256-thread CTA
+// once those fill four waves of the SMs, else 16 x 32 per 128 threads once
+// those fill two, else 8 x 32 per 128 threads: one CTA per SM leaves the
+// contraction latency-bound, and smaller tiles put more warps on each SM.
+// Measured (one solve, ms per RK4 step, FP32 / FP64): 257^2 0.40 / 3.28 with
+// the 16 x 32 tile, 0.35 / 2.21 with 8 x 32; 513^2 1.02 / 20.1 with 32 x 64,
+// 0.82 / 12.6 with 16 x 32 (0.99 / 15.3 with 8 x 32).
+static int tile_kind(int nx, int ny, int nsolve) {
+  const long big = (long)((nx + 63) / 64) * ((ny + 31) / 32) * nsolve;
+  const long small = (long)((nx + 31) / 32) * ((ny + 15) / 16) * nsolve;
+  return big >= 4 * 148 ? 0 : (small >= 2 * 148 ? 1 : 2);
 }
 
 template <int MODE>
 static cudaError_t lgl_x_mode(const LglStageArgs& a, cudaStream_t s) {
-  if (big_tiles(a.nx, a.ny, a.nsolve)) {
+  const int k = tile_kind(a.nx, a.ny, a.nsolve);
+  if (k == 0) {
     const dim3 grid((a.nx + 63) / 64, (a.ny + 31) / 32, a.nsolve);
     k_lgl_x<MODE, 32, 64, 2, 4><<<grid, 256, 0, s>>>(a);
-  } else {
+  } else if (k == 1) {
     const dim3 grid((a.nx + 31) / 32, (a.ny + 15) / 16, a.nsolve);
     k_lgl_x<MODE, 16, 32, 2, 2><<<grid, 128, 0, s>>>(a);
+  } else {
+    const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, a.nsolve);
+    k_lgl_x<MODE, 8, 32, 1, 2><<<grid, 128, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
 
 template <int MODE>
 static cudaError_t lgl_y_mode(const LglStageArgs& a, cudaStream_t s) {
-  if (big_tiles(a.nx, a.ny, a.nsolve)) {
+  const int k = tile_kind(a.nx, a.ny, a.nsolve);
+  if (k == 0) {
     const dim3 grid((a.nx + 63) / 64, (a.ny + 31) / 32, a.nsolve);
     k_lgl_y<MODE, 32, 64, 4, 2><<<grid, 256, 0, s>>>(a);
-  } else {
+  } else if (k == 1) {
     const dim3 grid((a.nx + 31) / 32, (a.ny + 15) / 16, a.nsolve);
     k_lgl_y<MODE, 16, 32, 2, 2><<<grid, 128, 0, s>>>(a);
+  } else {
+    const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, a.nsolve);
+    k_lgl_y<MODE, 8, 32, 1, 2><<<grid, 128, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
