@@ -191,7 +191,11 @@ struct PencilBase {
   static constexpr int B = Shape<N>::B;
   static constexpr int J = B / A;
   static_assert(B % A == 0, "pencil shape needs B multiple of A");
-  static constexpr int PAD = STRIDED ? 0 : 1;
+  // contiguous layout: rows of A + 2 elements once A >= 16, so that a thread's
+  // A consecutive elements start on a 16-byte boundary and move as 128-bit
+  // words (conflict-free: eight lanes cover the 32 banks); A + 1 below
+  static constexpr int PAD = STRIDED ? 0 : (A >= 16 ? 2 : 1);
+  static constexpr bool VEC = !STRIDED && A >= 16;
   // contiguous layout: pencil blocks of B*(A+1) float2, rounded up to = A
   // (mod 16) when A < 16, so that the pencils sharing a warp fall on
   // different banks (A lanes x 8 bytes each)
@@ -232,10 +236,20 @@ struct PencilBase {
     bar();
     sfor<0, J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
-      sfor<0, A>([&](auto nc) {
-        constexpr int n1 = decltype(nc)::value;
-        v[j * A + n1] = buf[xi(t + A * j, n1)];
-      });
+      if constexpr (VEC) {
+        const float4* src = reinterpret_cast<const float4*>(buf + xi(t + A * j, 0));
+        sfor<0, A / 2>([&](auto hc) {
+          constexpr int h = decltype(hc)::value;
+          const float4 w = src[h];
+          v[j * A + 2 * h] = make_float2(w.x, w.y);
+          v[j * A + 2 * h + 1] = make_float2(w.z, w.w);
+        });
+      } else {
+        sfor<0, A>([&](auto nc) {
+          constexpr int n1 = decltype(nc)::value;
+          v[j * A + n1] = buf[xi(t + A * j, n1)];
+        });
+      }
       dft<A, false, j * A>(v);
     });
   }
@@ -252,10 +266,19 @@ struct PencilBase {
     bar();
     sfor<0, J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
-      sfor<0, A>([&](auto nc) {
-        constexpr int n1 = decltype(nc)::value;
-        buf[xi(t + A * j, n1)] = v[j * A + n1];
-      });
+      if constexpr (VEC) {
+        float4* dst = reinterpret_cast<float4*>(buf + xi(t + A * j, 0));
+        sfor<0, A / 2>([&](auto hc) {
+          constexpr int h = decltype(hc)::value;
+          dst[h] = make_float4(v[j * A + 2 * h].x, v[j * A + 2 * h].y, v[j * A + 2 * h + 1].x,
+                               v[j * A + 2 * h + 1].y);
+        });
+      } else {
+        sfor<0, A>([&](auto nc) {
+          constexpr int n1 = decltype(nc)::value;
+          buf[xi(t + A * j, n1)] = v[j * A + n1];
+        });
+      }
     });
     bar();
     sfor<0, B>([&](auto kc) {
