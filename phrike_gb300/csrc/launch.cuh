@@ -93,10 +93,16 @@ cudaError_t last_t_T(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, cons
   const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);
   const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);
   cudaError_t e;
+  const bool fl = a.filter_last && a.stage == 3;  // the launch applies the last filter factor
   if (nd == 3) {
     if constexpr (T == TmaTile<NN>::T) {
-      if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;
-      k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      if (fl) {
+        if ((e = set_smem(k_last_t<NN, T, 3, false, R>, sm)) != cudaSuccess) return e;
+        k_last_t<NN, T, 3, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      } else {
+        if ((e = set_smem(k_last_t<NN, T, 3, false, R, 0, false>, sm)) != cudaSuccess) return e;
+        k_last_t<NN, T, 3, false, R, 0, false><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      }
     } else {
       return cudaErrorInvalidValue;
     }
@@ -107,8 +113,8 @@ cudaError_t last_t_T(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, cons
     // the right-hand side alone: the unclamped body holds one pair of
     // components at a time (fewer registers, more CTAs per SM)
     if constexpr (NN >= 256) {
-      if ((e = set_smem(k_last_t<NN, T, 2, false, R>, sm)) != cudaSuccess) return e;
-      k_last_t<NN, T, 2, false, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      if ((e = set_smem(k_last_t<NN, T, 2, false, R, 0, false>, sm)) != cudaSuccess) return e;
+      k_last_t<NN, T, 2, false, R, 0, false><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
     } else {
       return cudaErrorInvalidValue;
     }

@@ -331,8 +331,11 @@ constexpr int clamp_min_blocks() {
 }
 
 // PHYS 0: Euler (ND + 2 components, energy-perturbation clamp); PHYS 1: 2D
-// ideal MHD (8 components, MHD clamp, mhd_passes.cuh).
-template <int N, int T, int ND, bool CLAMP, int R, int PHYS = 0>
+// ideal MHD (8 components, MHD clamp, mhd_passes.cuh).  FL: the launch may
+// apply the last factor of the end-of-step filter (stage 3); the other
+// launches run an instantiation without those two transforms, whose smaller
+// code stays in the instruction cache.
+template <int N, int T, int ND, bool CLAMP, int R, int PHYS = 0, bool FL = true>
 __global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP, PHYS>())
     k_last_t(const __grid_constant__ CUtensorMap mAB, const __grid_constant__ CUtensorMap mU,
              const __grid_constant__ CUtensorMap mAcc, LastTArgs a) {
@@ -472,7 +475,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP,
         w[n2] = make_float2(res[0], res[1]);
       }
       if (need_un || need_acc) rc.release(ti - 1);
-      if (a.stage == 3 && a.filter_last) filter_pair(w);
+      if (FL && a.stage == 3 && a.filter_last) filter_pair(w);
       if (valid) {
 #pragma unroll
         for (int n2 = 0; n2 < B; ++n2) {
@@ -598,7 +601,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP,
           default:
             break;
         }
-        if (a.stage == 3 && a.filter_last) filter_pair(w);
+        if (FL && a.stage == 3 && a.filter_last) filter_pair(w);
         if (valid) {
 #pragma unroll
           for (int n2 = 0; n2 < B; ++n2) {
