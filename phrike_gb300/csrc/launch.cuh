@@ -106,18 +106,25 @@ cudaError_t last_t_T(int nd, const CUtensorMap& mAB, const CUtensorMap& mU, cons
     } else {
       return cudaErrorInvalidValue;
     }
-  } else if (a.mhd) {
-    if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;
-    k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
   } else if (a.rhs2d && a.stage < 0) {
     // the right-hand side alone: the unclamped body holds one pair of
-    // components at a time (fewer registers, more CTAs per SM)
+    // components at a time (fewer registers, more CTAs per SM); on grids with
+    // few column tiles the pairs are split over gridDim.z
+    const dim3 gz(grid.x, grid.y, a.pair_groups > 1 ? a.pair_groups : 1);
     if constexpr (NN >= 256) {
-      if ((e = set_smem(k_last_t<NN, T, 2, false, R, 0, false>, sm)) != cudaSuccess) return e;
-      k_last_t<NN, T, 2, false, R, 0, false><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      if (a.mhd) {
+        if ((e = set_smem(k_last_t<NN, T, 2, false, R, 1, false>, sm)) != cudaSuccess) return e;
+        k_last_t<NN, T, 2, false, R, 1, false><<<gz, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      } else {
+        if ((e = set_smem(k_last_t<NN, T, 2, false, R, 0, false>, sm)) != cudaSuccess) return e;
+        k_last_t<NN, T, 2, false, R, 0, false><<<gz, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
+      }
     } else {
       return cudaErrorInvalidValue;
     }
+  } else if (a.mhd) {
+    if ((e = set_smem(k_last_t<NN, T, 2, true, R, 1>, sm)) != cudaSuccess) return e;
+    k_last_t<NN, T, 2, true, R, 1><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
   } else {
     if ((e = set_smem(k_last_t<NN, T, 2, true, R>, sm)) != cudaSuccess) return e;
     k_last_t<NN, T, 2, true, R><<<grid, Shape<NN>::A * T, sm, s>>>(mAB, mU, mAcc, a);
@@ -148,23 +155,62 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
   return cudaErrorInvalidValue;
 }
 
+// Pencils per CTA of the contiguous-pencil passes of 2D/3D plans: the largest
+// of TC, TC/2 and TC/4 (never less than one full warp per CTA) whose grid
+// still gives two CTAs per SM; at TC, small single solves leave most of the
+// 152 SMs idle.  Each pencil's arithmetic is the same at every width, so the
+// results do not depend on it.
+constexpr int cmax_int(int a, int b) { return a > b ? a : b; }
+template <int NN>
+struct RowWidths {
+  static constexpr int T0 = Tile<NN>::TC;
+  static constexpr int TMIN = cmax_int(cmax_int(1, 32 / Shape<NN>::A), T0 / 4);
+  static constexpr int T1 = cmax_int(T0 / 2, TMIN);
+};
+template <int NN, typename F>
+cudaError_t dispatch_rows(long units, F&& f) {
+  using W = RowWidths<NN>;
+  if ((units + W::T0 - 1) / W::T0 >= 2L * 148) return f(std::integral_constant<int, W::T0>{});
+  if ((units + W::T1 - 1) / W::T1 >= 2L * 148) return f(std::integral_constant<int, W::T1>{});
+  return f(std::integral_constant<int, W::TMIN>{});
+}
+
+// Columns per CTA of the projection's y pass over the half spectra (strided
+// pencils; the grouped 512/1024-point pencils keep T * N / 256 <= 32): the
+// largest of 16, 8, 4 and 2 that gives two CTAs per SM.
+template <int NN, typename F>
+cudaError_t dispatch_proj_cols(long units, F&& f) {
+  constexpr int TMAX = (NN >= 1024) ? 8 : 16;
+  constexpr int TMIN = cmax_int(2, 32 / Shape<NN>::A);
+  if constexpr (TMAX >= 16 && TMIN <= 16)
+    if ((units + 15) / 16 >= 2L * 148) return f(std::integral_constant<int, 16>{});
+  if constexpr (TMIN <= 8)
+    if ((units + 7) / 8 >= 2L * 148 || TMIN == 8) return f(std::integral_constant<int, 8>{});
+  if constexpr (TMIN <= 4)
+    if ((units + 3) / 4 >= 2L * 148 || TMIN == 4) return f(std::integral_constant<int, 4>{});
+  if constexpr (TMIN <= 2) return f(std::integral_constant<int, 2>{});
+  return f(std::integral_constant<int, TMAX>{});
+}
+
 #define PS_DEFINE_LAUNCHERS(NN)                                                                       \
   template <>                                                                                         \
   cudaError_t launch_xfirst<NN>(int nd, const XFirstArgs& a, cudaStream_t s) {                        \
-    constexpr int T = Tile<NN>::TC;                                                                   \
-    const dim3 grid((a.rows + T - 1) / T);                                                            \
-    const dim3 block(Shape<NN>::A * T);                                                               \
-    cudaError_t e;                                                                                    \
-    if (nd == 3) {                                                                                    \
-      const size_t sm = sizeof(XFirstSmem<NN, T, 3>);                                                 \
-      if ((e = set_smem(k_xfirst<NN, T, 3>, sm)) != cudaSuccess) return e;                            \
-      k_xfirst<NN, T, 3><<<grid, block, sm, s>>>(a);                                                  \
-    } else {                                                                                          \
-      const size_t sm = sizeof(XFirstSmem<NN, T, 2>);                                                 \
-      if ((e = set_smem(k_xfirst<NN, T, 2>, sm)) != cudaSuccess) return e;                            \
-      k_xfirst<NN, T, 2><<<grid, block, sm, s>>>(a);                                                  \
-    }                                                                                                 \
-    return cudaGetLastError();                                                                        \
+    return dispatch_rows<NN>(a.rows, [&](auto tw) -> cudaError_t {                                    \
+      constexpr int T = decltype(tw)::value;                                                          \
+      const dim3 grid((a.rows + T - 1) / T);                                                          \
+      const dim3 block(Shape<NN>::A * T);                                                             \
+      cudaError_t e;                                                                                  \
+      if (nd == 3) {                                                                                  \
+        const size_t sm = sizeof(XFirstSmem<NN, T, 3>);                                               \
+        if ((e = set_smem(k_xfirst<NN, T, 3>, sm)) != cudaSuccess) return e;                          \
+        k_xfirst<NN, T, 3><<<grid, block, sm, s>>>(a);                                                \
+      } else {                                                                                        \
+        const size_t sm = sizeof(XFirstSmem<NN, T, 2>);                                               \
+        if ((e = set_smem(k_xfirst<NN, T, 2>, sm)) != cudaSuccess) return e;                          \
+        k_xfirst<NN, T, 2><<<grid, block, sm, s>>>(a);                                                \
+      }                                                                                               \
+      return cudaGetLastError();                                                                      \
+    });                                                                                               \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_op<NN>(bool strided, const OpArgs& a, cudaStream_t s) {                          \
@@ -201,38 +247,49 @@ cudaError_t dispatch_tcols(int tcols, F&& f) {
   template <>                                                                                         \
   cudaError_t launch_xfirst_mhd<NN>(const MhdXArgs& a, cudaStream_t s) {                              \
     constexpr int T = Tile<NN>::TC;                                                                   \
+    const int tiles = (a.rows + T - 1) / T;                                                           \
+    int groups = 1; /* job groups: two CTAs per SM where the grid allows */                           \
+    while (groups < 8 && (long)tiles * groups < 2L * 148) groups *= 2;                                \
     const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_xfirst_mhd<NN, T>, sm)) != cudaSuccess) return e;                             \
-    k_xfirst_mhd<NN, T><<<(a.rows + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                         \
+    k_xfirst_mhd<NN, T><<<dim3(tiles, groups), Shape<NN>::A * T, sm, s>>>(a);                         \
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_proj_xf<NN>(const ProjArgs& a, cudaStream_t s) {                                 \
-    constexpr int T = Tile<NN>::TC;                                                                   \
-    const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_proj_xf<NN, T>, sm)) != cudaSuccess) return e;                                \
-    k_proj_xf<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                   \
-    return cudaGetLastError();                                                                        \
+    return dispatch_rows<NN>((long)a.ny * a.nsolve, [&](auto tw) -> cudaError_t {                     \
+      constexpr int T = decltype(tw)::value;                                                          \
+      const size_t sm = sizeof(MhdXSmem<NN, T>);                                                      \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_proj_xf<NN, T>, sm)) != cudaSuccess) return e;                              \
+      const int tiles = (a.ny * a.nsolve + T - 1) / T;                                                \
+      const int fgroups = (tiles < 2 * 148) ? 2 : 1; /* Bx and By in separate CTAs */                 \
+      k_proj_xf<NN, T><<<dim3(tiles, fgroups), Shape<NN>::A * T, sm, s>>>(a);                         \
+      return cudaGetLastError();                                                                      \
+    });                                                                                               \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_proj_y<NN>(const ProjArgs& a, cudaStream_t s) {                                  \
-    constexpr int T = (NN >= 512) ? 8 : 16;                                                           \
-    const size_t sm = sizeof(ProjYSmem<NN, T>);                                                       \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_proj_y<NN, T>, sm)) != cudaSuccess) return e;                                 \
-    k_proj_y<NN, T><<<dim3((a.hx + T - 1) / T, a.nsolve), Shape<NN>::A * T, sm, s>>>(a);               \
-    return cudaGetLastError();                                                                        \
+    return dispatch_proj_cols<NN>((long)a.hx * a.nsolve, [&](auto tw) -> cudaError_t {                \
+      constexpr int T = decltype(tw)::value;                                                          \
+      const size_t sm = sizeof(ProjYSmem<NN, T>);                                                     \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_proj_y<NN, T>, sm)) != cudaSuccess) return e;                               \
+      k_proj_y<NN, T><<<dim3((a.hx + T - 1) / T, a.nsolve), Shape<NN>::A * T, sm, s>>>(a);             \
+      return cudaGetLastError();                                                                      \
+    });                                                                                               \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_proj_xi<NN>(const ProjArgs& a, cudaStream_t s) {                                 \
-    constexpr int T = Tile<NN>::TC;                                                                   \
-    const size_t sm = sizeof(MhdXSmem<NN, T>);                                                        \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_proj_xi<NN, T>, sm)) != cudaSuccess) return e;                                \
-    k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                   \
-    return cudaGetLastError();                                                                        \
+    return dispatch_rows<NN>((long)a.ny * a.nsolve, [&](auto tw) -> cudaError_t {                     \
+      constexpr int T = decltype(tw)::value;                                                          \
+      const size_t sm = sizeof(MhdXSmem<NN, T>);                                                      \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_proj_xi<NN, T>, sm)) != cudaSuccess) return e;                              \
+      k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                 \
+      return cudaGetLastError();                                                                      \
+    });                                                                                               \
   }                                                                                                   \
   template <>                                                                                         \
   cudaError_t launch_step1d<NN>(const Step1DArgs& a, int nsolve, cudaStream_t s) {                    \

@@ -69,15 +69,16 @@ __global__ void __launch_bounds__(EW_THREADS) k_mhd3_flux(Mhd3FluxArgs a) {
 }
 
 // k = -(dx1 Fx + dy1 Fy + dz1 Fz) + eta lap B + nu lap(rho u) (solver.py:932-954),
-// then the RK stage with the MHD clamp (solver.py:956-964, 988-1006)
+// or (rhs_in) the 2D right-hand side written by the unclamped last pass, then
+// the RK stage with the MHD clamp (solver.py:956-964, 988-1006)
 __global__ void __launch_bounds__(EW_THREADS) k_mhd3_update(Mhd3UpdateArgs a) {
   const int sol = blockIdx.y;
   if (a.active != nullptr && a.active[sol] == 0) return;
   const long cells = a.cells;
   const long so = (long)sol * 8 * cells;
   const float* F0 = a.F + so;
-  const float* F1 = a.F + (long)a.nsolve * 8 * cells + so;
-  const float* F2 = a.F + (long)2 * a.nsolve * 8 * cells + so;
+  const float* F1 = a.rhs_in ? F0 : a.F + (long)a.nsolve * 8 * cells + so;
+  const float* F2 = a.rhs_in ? F0 : a.F + (long)2 * a.nsolve * 8 * cells + so;
   const float dt = (a.dt_dev != nullptr) ? (float)a.dt_dev[sol] : (float)a.dt;
   const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_mhd3_update(Mhd3UpdateArgs a) {
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const long o = (long)c * cells + i;
-      k[c] = -(F0[o] + F1[o] + F2[o]);
+      k[c] = a.rhs_in ? F0[o] : -(F0[o] + F1[o] + F2[o]);
     }
     if (a.dif != nullptr) {
       const long ds = (long)a.nsolve * 6 * cells;

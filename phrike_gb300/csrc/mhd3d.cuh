@@ -34,7 +34,8 @@ struct Mhd3FluxArgs {
 };
 
 struct Mhd3UpdateArgs {
-  const float* F;     // the three blocks after the operator passes
+  const float* F;     // the three blocks after the operator passes, or (rhs_in) the right-hand side
+  int rhs_in;         // 1: F is one 8-field block holding the right-hand side itself (2D)
   const float* dif;   // nullable: the three Laplacian blocks
   float eta, nu;
   const float* Un;    // U^n

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst_mhd(MhdXArgs a) {
 #pragma unroll
     for (int c = 4; c < 8; ++c) q[c][n2] = u[c];
   }
-  if (a.speed != nullptr) {
+  if (a.speed != nullptr && blockIdx.y == 0) {
     float smax = 0.0f;
     if (valid) {
 #pragma unroll
@@ -141,9 +141,15 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_xfirst_mhd(MhdXArgs a) {
     }
   }
   __syncthreads();
-  // jobs 0..3: D_x on Fx pairs (2j, 2j+1); jobs 4..7: P_x on Fy pairs
+  // jobs 0..3: D_x on Fx pairs (2j, 2j+1); jobs 4..7: P_x on Fy pairs.  On
+  // grids with few pencil tiles the jobs are split over gridDim.y equal
+  // groups of CTAs (each group rebuilds the primitives of its rows), which
+  // shortens the chain of transforms each CTA runs.
+  const int jpg = (8 + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int j_lo = jpg * (int)blockIdx.y;
+  const int j_hi = min(8, j_lo + jpg);
 #pragma unroll 1
-  for (int j = 0; j < 8; ++j) {
+  for (int j = j_lo; j < j_hi; ++j) {
     float2 v[B];
     switch (j) {
 #define PS_MHD_JOB(J)                                                                                      \
@@ -226,8 +232,9 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_proj_xf(ProjArgs a) {
   PF pf{p, t, S.buf, S.ax.twf, S.ax.twi};
   load_axis<N>(S.ax, a.ax);
   __syncthreads();
+  // Bx and By: both in each CTA, or one per CTA row of a two-row grid
 #pragma unroll 1
-  for (int f = 0; f < 2; ++f) {
+  for (int f = (int)blockIdx.y; f < 2; f += (int)gridDim.y) {
     const float* src = ((f == 0) ? a.Bx : a.By) + (long)sol * a.ss + (long)j * N;
     float2 v[B];
 #pragma unroll

@@ -301,7 +301,8 @@ struct LastTArgs {
   float grav[3];
   int gravity;
   int rk2;             // midpoint RK2 coefficients (stages 0 and 3 only)
-  int rhs2d;           // 2D Euler, stage -1: the unclamped instantiation writes the right-hand side
+  int rhs2d;           // 2D, stage -1: the unclamped instantiation writes the right-hand side
+  int pair_groups;     // unclamped launches: gridDim.z groups of component pairs (0 or 1: one)
 };
 
 // Gravity source at one point of solve-local offset o (element index of
@@ -324,8 +325,8 @@ __device__ __forceinline__ void gravity_source(const LastTArgs& a, const float* 
 // registers (2D Euler) without spilling; MHD needs all 255.
 template <int N, int T, bool CLAMP, int PHYS>
 constexpr int clamp_min_blocks() {
-  if (PHYS == 1) return 1;
   if (!CLAMP) return tma_min_blocks<N, T>();
+  if (PHYS == 1) return 1;
   const int m = 65536 / (Shape<N>::A * T * 168);
   return m > 0 ? m : 1;
 }
@@ -354,9 +355,14 @@ __global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP,
   ring_init(S.ring);
   const bool need_un = !CLAMP && a.stage >= 0 && a.stage != 3;
   const bool need_acc = !CLAMP && a.stage >= 1;
+  // component pairs [c_lo, c_hi) of this CTA: all of them, or one of gridDim.z
+  // equal groups (unclamped launches on grids with few column tiles)
+  const int ppg = ((NC + 1) / 2 + (int)gridDim.z - 1) / (int)gridDim.z;
+  const int c_lo = CLAMP ? 0 : 2 * ppg * (int)blockIdx.z;
+  const int c_hi = CLAMP ? NC : min(NC, c_lo + 2 * ppg);
   if (threadIdx.x == 0) {
     int n = 0;
-    for (int c = 0; c < NC; c += 2) {
+    for (int c = c_lo; c < c_hi; c += 2) {
       const int m = (c + 1 < NC) ? 2 : 1;
       for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fa0 + c + q;
       for (int q = 0; q < m; ++q) S.ring.sched[n++] = a.fb0 + c + q;
@@ -416,7 +422,7 @@ __global__ void __launch_bounds__(Shape<N>::A * T, clamp_min_blocks<N, T, CLAMP,
 
   if constexpr (!CLAMP) {
 #pragma unroll 1
-    for (int c = 0; c < NC; c += 2) {
+    for (int c = c_lo; c < c_hi; c += 2) {
       const bool two = c + 1 < NC;
       const int m = two ? 2 : 1;
       float2 w[B];

@@ -88,14 +88,19 @@ bool pow2_axes(const ps_plan_desc* d) {
 // a Fourier grid with some other axis length: the mixed-radix passes
 bool is_mr(const ps_plan_desc* d) { return !is_lgl(d) && !pow2_axes(d); }
 
-// 2D Euler on power-of-two grids from 256 rows: the last pass is split into
-// the right-hand side and an elementwise stage update (the clamped last pass
-// holds every component's right-hand side in registers and runs one CTA per
-// SM at these lengths).  Chosen from the grid alone, so a solve gives the
-// same bits alone and in a batch.
+// 2D Euler and 2D MHD on power-of-two grids from 256 rows: the last pass is
+// split into the right-hand side and an elementwise stage update (the clamped
+// last pass holds every component's right-hand side in registers and runs one
+// CTA per SM at these lengths).  Chosen from the grid alone, so a solve gives
+// the same bits alone and in a batch.  The MHD update repeats the clamped
+// pass's stage arithmetic (accumulator form, then the clamp).
 bool split2d_grid(const ps_plan_desc* d) {
-  return d->ndim == 2 && d->equations == PS_EQ_EULER && !is_lgl(d) && !is_mr(d) && d->n[1] >= 256;
+  return d->ndim == 2 && (d->equations == PS_EQ_EULER || d->equations == PS_EQ_MHD) && !is_lgl(d) && !is_mr(d) &&
+         d->n[1] >= 256;
 }
+
+// Fields of the split 2D right-hand side buffer.
+int split2d_fields(const ps_plan_desc* d) { return d->equations == PS_EQ_MHD ? 8 : 4; }
 
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
@@ -416,6 +421,34 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
     ProfScope prof(p, s, PS_KIND_LAST, 4.0 * p->cells * p->nsolve * p->nc * (2 + st_words));
     return ps::mr_last(p, stage, Un, out, dt, d_dt, filter_last, active, s);
   }
+  if (p->split2d && stage >= 0 && p->mhd) {
+    // 2D MHD from 256 rows: the right-hand side into R, then the RK stage and
+    // the MHD clamp elementwise, in the clamped pass's accumulator form
+    const float* in = (stage == 0) ? Un : p->Us;
+    if ((rc = last(p, -1, in, p->R2, 0.0, nullptr, false, s, active)) != PS_OK) return rc;
+    ps::Mhd3UpdateArgs u{};
+    u.F = p->R2;
+    u.rhs_in = 1;
+    u.dif = nullptr;
+    u.Un = Un;
+    u.acc = p->acc;
+    u.out = out;
+    u.cells = p->cells;
+    u.nsolve = p->nsolve;
+    u.stage = stage;
+    u.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
+    u.dt_dev = d_dt;
+    u.dt = dt;
+    u.gamma = (float)p->desc.gamma;
+    u.rho_min = (float)p->desc.mhd_rho_min;  // SpectralSolverMHD._clamp floors (solver.py:876-877)
+    u.p_min = (float)p->desc.mhd_p_min;
+    u.active = active;
+    // words per cell: R, U^n (not at stage 3), acc read (from stage 1), acc write (to stage 2), output
+    const double words = 8.0 * ((stage == 0) ? 4 : (stage == 3) ? 3 : 5);
+    ProfScope prof(p, s, PS_KIND_LAST, words * 4.0 * p->cells * p->nsolve);
+    PS_CU(ps::launch_mhd3_update(u, s), "MHD stage update");
+    return PS_OK;
+  }
   if (p->split2d && stage >= 0) {
     // 2D Euler from 256 rows: the right-hand side of the stage input (with
     // gravity) into R, the RK stage and the clamp elementwise (increment-form
@@ -505,6 +538,13 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   if (p->mhd) a.gravity = 0;
   a.rk2 = (p->desc.scheme == PS_SCHEME_RK2) ? 1 : 0;
   a.rhs2d = (p->split2d && stage < 0) ? 1 : 0;
+  if (a.rhs2d) {  // fewer column tiles than two per SM: split the component pairs over gridDim.z
+    const long tiles = (long)((a.g.ncol + p->tcols - 1) / p->tcols) * a.g.nouter * p->nsolve;
+    const int npair = (nc + 1) / 2;
+    a.pair_groups = 1;
+    while (a.pair_groups < npair && tiles * a.pair_groups < 2L * 148 && npair % (2 * a.pair_groups) == 0)
+      a.pair_groups *= 2;
+  }
   const int naxis = (p->nd == 3) ? p->n[2] : p->n[1];
   // words per cell: 2*nc inputs, plus U^n / acc reads and acc / output writes
   const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
@@ -1137,7 +1177,7 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if (p->nd == 3 && !mhd3 && (rc = dalloc(p, &p->AB, 10 * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->acc, p->nc * c)) != PS_OK) return cleanup(rc);
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
-    if (split2d_grid(d) && (rc = dalloc(p, &p->R2, 4 * c)) != PS_OK) return cleanup(rc);
+    if (split2d_grid(d) && (rc = dalloc(p, &p->R2, split2d_fields(d) * c)) != PS_OK) return cleanup(rc);
     p->split2d = split2d_grid(d);
   }
   p->av = av_params(d);
@@ -1241,7 +1281,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   }
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
   if (is_mr(d) && d->ndim == 1) fields += 6;  // stage input and increments
-  if (split2d_grid(d)) fields += 4;            // the 2D right-hand side
+  if (split2d_grid(d)) fields += split2d_fields(d);  // the 2D right-hand side
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
   const bool mhd = d->equations == PS_EQ_MHD;
   if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator

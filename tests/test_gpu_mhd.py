@@ -108,6 +108,30 @@ def test_mhd_batch_matches_alone(cuda_device):
         assert torch.equal(U1, Ub[i]), i
 
 
+def test_mhd_batch_of_sixteen_256_matches_alone(cuda_device):
+    """On 256^2 grids the last pass is split into the right-hand side and an
+    elementwise update; a batch of sixteen runs the passes in other shapes
+    than a solve alone: the MHD x pass with its 8 transform jobs in one CTA
+    instead of one job per CTA, the projection's x passes 8 pencils per CTA
+    instead of 2 and its y pass 4 columns instead of 2, the right-hand side
+    8 columns with all component pairs in one CTA instead of 4 columns with
+    one pair per CTA.  Each pencil's arithmetic is the same in every shape:
+    the states are bit-identical."""
+    import torch
+    n = 256
+    states = [problems.orszag_tang_2d(n, n, gamma=G53, B0=0.5 + 0.05 * b) for b in range(16)]
+    fp = {"enabled": True, "p": 8, "alpha": 36.0}
+    pb = _plan(n, n, nsolve=16, filt=fp)
+    Ub = _dev(np.stack(states))
+    pb.run_(Ub, 3, 1e-3)
+    for i in (0, 9, 15):
+        p1 = _plan(n, n, filt=fp)
+        U1 = _dev(states[i])
+        p1.run_(U1, 3, 1e-3)
+        assert torch.equal(U1, Ub[i]), i
+    assert pb.status() == 0
+
+
 def test_mhd_cfl_run_vs_oracle(cuda_device):
     import torch
     n, t_end = 64, 0.05
