@@ -363,14 +363,29 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
       const int i = i0 + tc + NTC * q;
       if (i >= nx) continue;
       const long o = (long)j * nx + i;
+      // the point's loads before its stores (a store between them would make
+      // each component wait for the previous one's round trip to memory)
+      float gx[4], un[4], ac[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const long g = so + c * cells + o;
+        gx[c] = Gx[c * cells + o];
+        un[c] = (a.stage >= 0) ? a.Un[g] : 0.0f;
+        ac[c] = (a.stage >= 1) ? a.acc[g] : 0.0f;
+      }
+      float grho = 0.0f, gmx = 0.0f, gmy = 0.0f;
+      if (a.gravity) {
+        grho = U[o];
+        gmx = U[cells + o];
+        gmy = U[2 * cells + o];
+      }
       float k[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) k[c] = -(Gx[c * cells + o] + (float)acc[c][m][q]);
+      for (int c = 0; c < 4; ++c) k[c] = -(gx[c] + (float)acc[c][m][q]);
       if (a.gravity) {  // rho g on the momenta, g . m on the energy, from the stage input
-        const float rho = U[o], mx = U[cells + o], my = U[2 * cells + o];
-        k[1] = fmaf(rho, a.g[0], k[1]);
-        k[2] = fmaf(rho, a.g[1], k[2]);
-        k[3] += a.g[0] * mx + a.g[1] * my;
+        k[1] = fmaf(grho, a.g[0], k[1]);
+        k[2] = fmaf(grho, a.g[1], k[2]);
+        k[3] += a.g[0] * gmx + a.g[1] * gmy;
       }
       if (a.stage < 0) {
 #pragma unroll
@@ -379,11 +394,10 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_lgl_y(LglStageArgs a)
       }
       float u[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const long g = so + c * cells + o;
-        float ac = (a.stage == 0) ? 0.0f : a.acc[g];
-        u[c] = rk_update_incr(a.stage, rk, k[c], a.Un[g], ac);
-        if (a.stage != 3) a.acc[g] = ac;
+      for (int c = 0; c < 4; ++c) u[c] = rk_update_incr(a.stage, rk, k[c], un[c], ac[c]);
+      if (a.stage != 3) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) a.acc[so + c * cells + o] = ac[c];
       }
       clamp_state<2>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll

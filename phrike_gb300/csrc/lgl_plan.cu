@@ -473,10 +473,16 @@ int lgl_steps(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, do
       LGL_CU(launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
              "step control");
     }
+    // The CUDA-core y contraction reads its stage input along whole columns
+    // while its epilogue writes the next stage input, so that stage's input
+    // and output must differ: stages 1 and 2 alternate between Us and the
+    // free upper half of G (the x contraction writes the lower half).  The
+    // tensor-core path updates in a separate kernel after both contractions.
+    float* const alt = tensor_cores(p) ? p->Us : p->G + 4 * p->cells * p->nsolve;
     for (int st = 0; st < 4; ++st) {
       if (p->desc.scheme == PS_SCHEME_RK2 && (st == 1 || st == 2)) continue;  // midpoint RK2
-      float* in = (st == 0) ? U : p->Us;
-      float* out = (st < 3) ? p->Us : U;
+      float* in = (st == 0) ? U : (st == 2) ? alt : p->Us;
+      float* out = (st == 1) ? alt : (st < 3) ? p->Us : U;
       if ((rc = stage(p, in, st, U, out, dt, dtp, act, s)) != PS_OK) return rc;
     }
     if (due) {

@@ -366,7 +366,7 @@ cudaError_t launch_umma_x3(const CUtensorMap& mA, const CUtensorMap& mB, const U
 // ---------------------------------------------------------------------------
 // k = -(Gx + Gy), RK4 stage update and the 2D clamp, per cell (E' form)
 // ---------------------------------------------------------------------------
-__global__ void k_lgl_update(LglUpdateArgs a) {
+__global__ void __launch_bounds__(256, 4) k_lgl_update(LglUpdateArgs a) {
   const int sol = blockIdx.y;
   if (a.active != nullptr && a.active[sol] == 0) return;
   const long cells = a.cells;
@@ -375,15 +375,29 @@ __global__ void k_lgl_update(LglUpdateArgs a) {
   const RKCoef rk = rk_coef(a.stage < 0 ? 0 : a.stage, dt, a.rk2);
   const float pmin_shift = a.p_min - (a.gamma - 1.0f) * a.eref[sol];
   for (long o = blockIdx.x * (long)blockDim.x + threadIdx.x; o < cells; o += (long)gridDim.x * blockDim.x) {
-    float k[4];
+    // every load of the cell first, then the arithmetic, then the stores: a
+    // store between loads (acc may alias nothing the compiler can prove) would
+    // make each component wait for the previous one's round trip to memory
+    float k[4], un[4], ac[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
-      k[c] = a.ksign * (a.Gy != nullptr ? a.Gx[so + c * cells + o] + a.Gy[so + c * cells + o] : a.Gx[so + c * cells + o]);
+    for (int c = 0; c < 4; ++c) {
+      const long g = so + c * cells + o;
+      k[c] = a.Gy != nullptr ? a.Gx[g] + a.Gy[g] : a.Gx[g];
+      un[c] = (a.stage >= 0) ? a.Un[g] : 0.0f;
+      ac[c] = (a.stage >= 1) ? a.acc[g] : 0.0f;
+    }
+    float grho = 0.0f, gmx = 0.0f, gmy = 0.0f;
+    if (a.gravity) {
+      grho = a.Uin[so + o];
+      gmx = a.Uin[so + cells + o];
+      gmy = a.Uin[so + 2 * cells + o];
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) k[c] = a.ksign * k[c];
     if (a.gravity) {  // rho g on the momenta, g . m on the energy (solver.py:453-464)
-      const float rho = a.Uin[so + o], mx = a.Uin[so + cells + o], my = a.Uin[so + 2 * cells + o];
-      k[1] = fmaf(rho, a.g[0], k[1]);
-      k[2] = fmaf(rho, a.g[1], k[2]);
-      k[3] += a.g[0] * mx + a.g[1] * my;
+      k[1] = fmaf(grho, a.g[0], k[1]);
+      k[2] = fmaf(grho, a.g[1], k[2]);
+      k[3] += a.g[0] * gmx + a.g[1] * gmy;
     }
     if (a.stage < 0) {
 #pragma unroll
@@ -392,11 +406,10 @@ __global__ void k_lgl_update(LglUpdateArgs a) {
     }
     float u[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const long g = so + c * cells + o;
-      float ac = (a.stage == 0) ? 0.0f : a.acc[g];
-      u[c] = rk_update_incr(a.stage, rk, k[c], a.Un[g], ac);
-      if (a.stage != 3) a.acc[g] = ac;
+    for (int c = 0; c < 4; ++c) u[c] = rk_update_incr(a.stage, rk, k[c], un[c], ac[c]);
+    if (a.stage != 3) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a.acc[so + c * cells + o] = ac[c];
     }
     clamp_state<2>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll

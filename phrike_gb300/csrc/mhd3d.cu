@@ -107,17 +107,28 @@ __global__ void __launch_bounds__(EW_THREADS) k_mhd3_update(Mhd3UpdateArgs a) {
     }
     const float* un = a.Un + so + i;
     float* acc = a.acc + so + i;
-    float u[8];
+    // the cell's loads before its stores (a store between them would make
+    // each component wait for the previous one's round trip to memory)
+    float vu[8], va[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const long o = (long)c * cells;
+      vu[c] = (a.stage != 3) ? un[o] : 0.0f;
+      va[c] = (a.stage != 0) ? acc[o] : 0.0f;
+    }
+    float u[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
       if (a.stage == 3) {
-        u[c] = fmaf(rk.wacc, k[c], acc[o]);
+        u[c] = fmaf(rk.wacc, k[c], va[c]);
       } else {
-        const float v = un[o];
-        acc[o] = fmaf(rk.wacc, k[c], (a.stage == 0) ? v : acc[o]);
-        u[c] = fmaf(rk.wnext, k[c], v);
+        va[c] = fmaf(rk.wacc, k[c], (a.stage == 0) ? vu[c] : va[c]);
+        u[c] = fmaf(rk.wnext, k[c], vu[c]);
       }
+    }
+    if (a.stage != 3) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[(long)c * cells] = va[c];
     }
     clamp_mhd(u, a.gamma, a.rho_min, a.p_min);
 #pragma unroll
@@ -334,13 +345,24 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_proj3_xi(Proj3Args a) {
     float* by = a.B[1] + base;
     float* bz = a.B[2] + base;
     float* e = (a.E != nullptr) ? a.E + base : nullptr;
+    if (e != nullptr) {  // every old B and E of the row loaded before the first store
+      float ox[B], oy[B], oz[B], oe[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const int i = t + A * n2;
+        ox[n2] = bx[i];
+        oy[n2] = by[i];
+        oz[n2] = bz[i];
+        oe[n2] = e[i];
+      }
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2)
+        e[t + A * n2] = oe[n2] + 0.5f * ((z[n2].x * z[n2].x + z[n2].y * z[n2].y + w[n2].x * w[n2].x) -
+                                         (ox[n2] * ox[n2] + oy[n2] * oy[n2] + oz[n2] * oz[n2]));
+    }
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) {
       const int i = t + A * n2;
-      if (e != nullptr) {
-        const float ox = bx[i], oy = by[i], oz = bz[i];
-        e[i] += 0.5f * ((z[n2].x * z[n2].x + z[n2].y * z[n2].y + w[n2].x * w[n2].x) - (ox * ox + oy * oy + oz * oz));
-      }
       bx[i] = z[n2].x;
       by[i] = z[n2].y;
       bz[i] = w[n2].x;

@@ -355,13 +355,22 @@ __global__ void __launch_bounds__(Shape<N>::A * T) k_proj_xi(ProjArgs a) {
     float* bx = a.Bx + (long)sol * a.ss + (long)j * N;
     float* by = a.By + (long)sol * a.ss + (long)j * N;
     float* e = (a.E != nullptr) ? a.E + (long)sol * a.ss + (long)j * N : nullptr;
+    if (e != nullptr) {  // every old B and E of the row loaded before the first store
+      float ox[B], oy[B], oe[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) {
+        const int i = t + A * n2;
+        ox[n2] = bx[i];
+        oy[n2] = by[i];
+        oe[n2] = e[i];
+      }
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2)
+        e[t + A * n2] = oe[n2] + 0.5f * ((z[n2].x * z[n2].x + z[n2].y * z[n2].y) - (ox[n2] * ox[n2] + oy[n2] * oy[n2]));
+    }
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) {
       const int i = t + A * n2;
-      if (e != nullptr) {
-        const float ox = bx[i], oy = by[i];
-        e[i] += 0.5f * ((z[n2].x * z[n2].x + z[n2].y * z[n2].y) - (ox * ox + oy * oy));
-      }
       bx[i] = z[n2].x;
       by[i] = z[n2].y;
     }

@@ -416,17 +416,27 @@ __global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_last(MrLastArgs
       for (int c = 0; c < NC; ++c) out_s[c * a.fs + off] = k[c];
       return;
     }
-    float u[NC];
+    // the point's loads before its stores: a store between them would make
+    // each component wait for the previous one's round trip to memory
+    float vu[NC], va[NC], u[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       const long o = c * a.fs + off;
+      vu[c] = (a.stage != 3) ? un_s[o] : 0.0f;
+      va[c] = (a.stage != 0) ? acc_s[o] : 0.0f;
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
       if (a.stage == 3) {
-        u[c] = fmaf(rk.wacc, k[c], acc_s[o]);
+        u[c] = fmaf(rk.wacc, k[c], va[c]);
       } else {
-        const float un = un_s[o];
-        acc_s[o] = fmaf(rk.wacc, k[c], (a.stage == 0) ? un : acc_s[o]);
-        u[c] = fmaf(rk.wnext, k[c], un);
+        va[c] = fmaf(rk.wacc, k[c], (a.stage == 0) ? vu[c] : va[c]);
+        u[c] = fmaf(rk.wnext, k[c], vu[c]);
       }
+    }
+    if (a.stage != 3) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc_s[c * a.fs + off] = va[c];
     }
     if (a.clamp) clamp_state<ND>(u, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
@@ -512,12 +522,17 @@ __global__ void __launch_bounds__(kMrThreads, kMrMinBlocks) k_mr_line(MrLineArgs
       for (int c = 0; c < 3; ++c) out[c * n + i] = k[c];
       return;
     }
-    float u3[3];
+    float u3[3], vu[3], va[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float ac = (a.stage == 0) ? 0.0f : acc[c * n + i];
-      u3[c] = rk_update_incr(a.stage, rk, k[c], un[c * n + i], ac);
-      if (a.stage != 3) acc[c * n + i] = ac;
+    for (int c = 0; c < 3; ++c) {  // loads before stores
+      vu[c] = un[c * n + i];
+      va[c] = (a.stage == 0) ? 0.0f : acc[c * n + i];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u3[c] = rk_update_incr(a.stage, rk, k[c], vu[c], va[c]);
+    if (a.stage != 3) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c * n + i] = va[c];
     }
     clamp_state<1>(u3, a.gamma, a.rho_min, pmin_shift);
 #pragma unroll
