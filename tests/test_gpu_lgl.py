@@ -186,7 +186,7 @@ def test_lgl_acoustic_pulse_vs_oracle(cuda_device, prec):
 @pytest.mark.parametrize("n,prec", [(257, "fp32"), (257, "bf16x3"), (513, "fp32"), (513, "bf16x3")])
 def test_lgl_workload_size_500_steps(cuda_device, n, prec):
     """The precision workload at its stated sizes: 257^2 and 513^2 nodes, 500
-    steps of dt = 1e-5 (measured momentum: FP32 2.1e-6 and 8.6e-6,
+    steps of dt = 1e-5 (measured momentum: FP32 2.1e-6 and 6.1e-6,
     split-bf16 x3 3.0e-5 and 4.6e-5; density 6.4e-7, energy 4.4e-9)."""
     U0 = _pulse(n, n)
     R = _oracle_steps(n, U0, 500, 1e-5)
