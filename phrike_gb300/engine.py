@@ -211,19 +211,22 @@ class Plan:
         """Advance a stream of independent states held in pinned host memory:
         output i = input i after ``nsteps`` RK4 steps of ``dt``.  The copy of
         state i + 1 to the device and of state i - 1 back to the host overlap
-        the steps of state i (two device buffers, one copy stream per
-        direction; the steps themselves stay on the current stream, in order,
-        since they share the plan's scratch).  Returns when every output has
-        landed.  Inputs and outputs may repeat the same host tensors."""
+        the steps of state i (three device buffers, one copy stream per
+        direction: the copy in of state i + 1 waits only for the copy out of
+        state i - 2, so the two directions run at the same time; the steps
+        themselves stay on the current stream, in order, since they share the
+        plan's scratch).  Returns when every output has landed.  Inputs and
+        outputs may repeat the same host tensors."""
         if len(inputs) != len(outputs):
             raise ValueError("inputs and outputs differ in length")
         comp = torch.cuda.current_stream(self.device)
         h2d, d2h = torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)
-        bufs, freed = [], [None, None]
+        nbuf = 3
+        bufs, freed = [], [None] * nbuf
         for i, (hi, ho) in enumerate(zip(inputs, outputs)):
             if not (hi.is_pinned() and ho.is_pinned()):
                 raise ValueError("host states must be in pinned memory")
-            b = i % 2
+            b = i % nbuf
             if len(bufs) <= b:
                 bufs.append(torch.empty(hi.shape, dtype=torch.float32, device=self.device))
             with torch.cuda.stream(h2d):
