@@ -476,28 +476,35 @@ __global__ void k_lgl_bc(float* U, int nx, int ny, long ss, const int* active) {
   if (active != nullptr && active[sol] == 0) return;
   float* u = U + (long)sol * ss;
   const long cells = (long)nx * ny;
+  // Each row's (column's) interior neighbours are loaded before its wall
+  // values are stored: the walls never overwrite what they copy, and loads
+  // issued behind possibly aliasing stores would each wait a round trip.
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
     const long l = (long)j * nx, r = l + nx - 1;
-    u[l] = u[l + 1];
+    const float l0 = u[l + 1], l2 = u[2 * cells + l + 1], l3 = u[3 * cells + l + 1];
+    const float r0 = u[r - 1], r2 = u[2 * cells + r - 1], r3 = u[3 * cells + r - 1];
+    u[l] = l0;
     u[cells + l] = 0.0f;
-    u[2 * cells + l] = u[2 * cells + l + 1];
-    u[3 * cells + l] = u[3 * cells + l + 1];
-    u[r] = u[r - 1];
+    u[2 * cells + l] = l2;
+    u[3 * cells + l] = l3;
+    u[r] = r0;
     u[cells + r] = 0.0f;
-    u[2 * cells + r] = u[2 * cells + r - 1];
-    u[3 * cells + r] = u[3 * cells + r - 1];
+    u[2 * cells + r] = r2;
+    u[3 * cells + r] = r3;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nx; i += blockDim.x) {
     const long t = (long)(ny - 1) * nx + i, b = i;
-    u[t] = u[t - nx];
-    u[cells + t] = u[cells + t - nx];
+    const float t0 = u[t - nx], t1 = u[cells + t - nx], t3 = u[3 * cells + t - nx];
+    const float b0 = u[b + nx], b1 = u[cells + b + nx], b3 = u[3 * cells + b + nx];
+    u[t] = t0;
+    u[cells + t] = t1;
     u[2 * cells + t] = 0.0f;
-    u[3 * cells + t] = u[3 * cells + t - nx];
-    u[b] = u[b + nx];
-    u[cells + b] = u[cells + b + nx];
+    u[3 * cells + t] = t3;
+    u[b] = b0;
+    u[cells + b] = b1;
     u[2 * cells + b] = 0.0f;
-    u[3 * cells + b] = u[3 * cells + b + nx];
+    u[3 * cells + b] = b3;
   }
 }
 
