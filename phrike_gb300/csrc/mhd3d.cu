@@ -26,8 +26,8 @@ __global__ void __launch_bounds__(EW_THREADS) k_mhd3_flux(Mhd3FluxArgs a) {
   const float g1 = a.gamma - 1.0f;
   float m = 0.0f;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < cells; i += (long)gridDim.x * blockDim.x) {
-    const float rho = U[i];
-    const float ux = U[cells + i] / rho, uy = U[2 * cells + i] / rho, uz = U[3 * cells + i] / rho;
+    const float rho = U[i], mx = U[cells + i], my = U[2 * cells + i], mz = U[3 * cells + i];
+    const float ux = mx / rho, uy = my / rho, uz = mz / rho;
     const float E = U[4 * cells + i];
     const float bx = U[5 * cells + i], by = U[6 * cells + i], bz = U[7 * cells + i];
     const float b2 = bx * bx + by * by + bz * bz;
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_mhd3_flux(Mhd3FluxArgs a) {
       F[7 * cells] = (d == 2) ? 0.0f : un * bz - uz * bn;
     }
     if (a.dif != nullptr) {  // (rho u, B) for the three Laplacian terms
-      const float x[6] = {U[cells + i], U[2 * cells + i], U[3 * cells + i], bx, by, bz};
+      const float x[6] = {mx, my, mz, bx, by, bz};
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         float* D = a.dif + ((long)d * a.nsolve + sol) * 6 * cells + i;
