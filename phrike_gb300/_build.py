@@ -55,7 +55,9 @@ def _compile(nvcc: str, src: str, verbose: bool) -> str:
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
     """Compile every csrc/*.cu and link libphrike_gb300.so; returns its path."""
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    # the pass-kernel instantiations (kern_*.cu) take longest: start them first
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")),
+                  key=lambda f: (not os.path.basename(f).startswith("kern_"), f))
     deps = srcs + sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + \
         sorted(glob.glob(os.path.join(os.path.dirname(HERE), "include", "*.h")))
     stamp = os.path.join(BUILD, "stamp")

@@ -2,5 +2,5 @@
 #include "launch.cuh"
 
 namespace ps {
-PS_DEFINE_LAUNCHERS(16)
+PS_DEFINE_ALL_LAUNCHERS(16)
 }  // namespace ps

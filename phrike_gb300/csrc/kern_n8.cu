@@ -2,5 +2,5 @@
 #include "launch.cuh"
 
 namespace ps {
-PS_DEFINE_LAUNCHERS(8)
+PS_DEFINE_ALL_LAUNCHERS(8)
 }  // namespace ps

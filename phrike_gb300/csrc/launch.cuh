@@ -192,6 +192,11 @@ cudaError_t dispatch_proj_cols(long units, F&& f) {
   return f(std::integral_constant<int, TMAX>{});
 }
 
+// Launchers of the 2D/3D pencil lengths, in four groups so that the largest
+// lengths compile as four translation units in parallel: the x pass and the
+// operator and y passes, the 1D whole-step kernels, the last pass (every
+// stage / clamp / MHD variant), and the 2D MHD x pass with the Helmholtz
+// projection.  PS_DEFINE_ALL_LAUNCHERS puts the four in one unit.
 #define PS_DEFINE_LAUNCHERS(NN)                                                                       \
   template <>                                                                                         \
   cudaError_t launch_xfirst<NN>(int nd, const XFirstArgs& a, cudaStream_t s) {                        \
@@ -226,7 +231,7 @@ cudaError_t dispatch_proj_cols(long units, F&& f) {
   template <>                                                                                         \
   cudaError_t launch_ymid3_t<NN>(const CUtensorMap& mG, const YMidTArgs& a, cudaStream_t s) {         \
     constexpr int T = TmaTile<NN>::T, R = TmaTile<NN>::R;                                             \
-    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                              \
+    const dim3 grid((a.g.ncol + T - 1) / T, a.g.nouter * a.nsolve);                                   \
     const size_t sm = sizeof(TmaStridedSmem<NN, T, R>);                                               \
     cudaError_t e;                                                                                    \
     if ((e = set_smem(k_ymid3_t<NN, T, R>, sm)) != cudaSuccess) return e;                             \
@@ -234,16 +239,50 @@ cudaError_t dispatch_proj_cols(long units, F&& f) {
     return cudaGetLastError();                                                                        \
   }                                                                                                   \
   template <>                                                                                         \
+  cudaError_t launch_op_t<NN>(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {             \
+    return dispatch_tcols<NN>(a.tcols, [&](auto tc) { return op_t_T<NN, decltype(tc)::value>(mIn, a, s); });\
+  }
+
+#define PS_DEFINE_STEP1D_LAUNCHERS(NN)                                                                \
+  template <>                                                                                         \
+  cudaError_t launch_step1d<NN>(const Step1DArgs& a, int nsolve, cudaStream_t s) {                    \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
+    k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_ark1d<NN>(const Ark1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
+    cudaError_t e;                                                                                    \
+    if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
+    k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
+    return cudaGetLastError();                                                                        \
+  }                                                                                                   \
+  template <>                                                                                         \
+  cudaError_t launch_mhd1d<NN>(const Mhd1DArgs& a, int nsolve, cudaStream_t s) {                      \
+    if constexpr (NN > 2048) {                                                                        \
+      return cudaErrorInvalidValue; /* 1D MHD pencils up to 2048 points */                            \
+    } else {                                                                                          \
+      const size_t sm = sizeof(Mhd1DSmem<NN>);                                                        \
+      cudaError_t e;                                                                                  \
+      if ((e = set_smem(k_mhd1d<NN>, sm)) != cudaSuccess) return e;                                   \
+      k_mhd1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                \
+      return cudaGetLastError();                                                                      \
+    }                                                                                                 \
+  }
+
+#define PS_DEFINE_LAST_LAUNCHERS(NN)                                                                  \
+  template <>                                                                                         \
   cudaError_t launch_last_t<NN>(int nd, const CUtensorMap& mAB, const CUtensorMap& mU,                \
                                 const CUtensorMap& mAcc, const LastTArgs& a, cudaStream_t s) {        \
     return dispatch_tcols<NN>(a.tcols, [&](auto tc) {                                                 \
       return last_t_T<NN, decltype(tc)::value>(nd, mAB, mU, mAcc, a, s);                              \
     });                                                                                               \
-  }                                                                                                   \
-  template <>                                                                                         \
-  cudaError_t launch_op_t<NN>(const CUtensorMap& mIn, const OpTArgs& a, cudaStream_t s) {             \
-    return dispatch_tcols<NN>(a.tcols, [&](auto tc) { return op_t_T<NN, decltype(tc)::value>(mIn, a, s); }); \
-  }                                                                                                   \
+  }
+
+#define PS_DEFINE_MHD_LAUNCHERS(NN)                                                                   \
   template <>                                                                                         \
   cudaError_t launch_xfirst_mhd<NN>(const MhdXArgs& a, cudaStream_t s) {                              \
     constexpr int T = Tile<NN>::TC;                                                                   \
@@ -276,7 +315,7 @@ cudaError_t dispatch_proj_cols(long units, F&& f) {
       const size_t sm = sizeof(ProjYSmem<NN, T>);                                                     \
       cudaError_t e;                                                                                  \
       if ((e = set_smem(k_proj_y<NN, T>, sm)) != cudaSuccess) return e;                               \
-      k_proj_y<NN, T><<<dim3((a.hx + T - 1) / T, a.nsolve), Shape<NN>::A * T, sm, s>>>(a);             \
+      k_proj_y<NN, T><<<dim3((a.hx + T - 1) / T, a.nsolve), Shape<NN>::A * T, sm, s>>>(a);            \
       return cudaGetLastError();                                                                      \
     });                                                                                               \
   }                                                                                                   \
@@ -287,38 +326,16 @@ cudaError_t dispatch_proj_cols(long units, F&& f) {
       const size_t sm = sizeof(MhdXSmem<NN, T>);                                                      \
       cudaError_t e;                                                                                  \
       if ((e = set_smem(k_proj_xi<NN, T>, sm)) != cudaSuccess) return e;                              \
-      k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                 \
+      k_proj_xi<NN, T><<<(a.ny * a.nsolve + T - 1) / T, Shape<NN>::A * T, sm, s>>>(a);                \
       return cudaGetLastError();                                                                      \
     });                                                                                               \
-  }                                                                                                   \
-  template <>                                                                                         \
-  cudaError_t launch_step1d<NN>(const Step1DArgs& a, int nsolve, cudaStream_t s) {                    \
-    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_step1d<NN>, sm)) != cudaSuccess) return e;                                    \
-    k_step1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                 \
-    return cudaGetLastError();                                                                        \
-  }                                                                                                   \
-  template <>                                                                                         \
-  cudaError_t launch_ark1d<NN>(const Ark1DArgs& a, int nsolve, cudaStream_t s) {                      \
-    const size_t sm = sizeof(Step1DSmem<NN>);                                                         \
-    cudaError_t e;                                                                                    \
-    if ((e = set_smem(k_ark1d<NN>, sm)) != cudaSuccess) return e;                                     \
-    k_ark1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                  \
-    return cudaGetLastError();                                                                        \
-  }                                                                                                   \
-  template <>                                                                                         \
-  cudaError_t launch_mhd1d<NN>(const Mhd1DArgs& a, int nsolve, cudaStream_t s) {                      \
-    if constexpr (NN > 2048) {                                                                        \
-      return cudaErrorInvalidValue; /* 1D MHD pencils up to 2048 points */                            \
-    } else {                                                                                          \
-      const size_t sm = sizeof(Mhd1DSmem<NN>);                                                        \
-      cudaError_t e;                                                                                  \
-      if ((e = set_smem(k_mhd1d<NN>, sm)) != cudaSuccess) return e;                                   \
-      k_mhd1d<NN><<<nsolve, Shape<NN>::A, sm, s>>>(a);                                                \
-      return cudaGetLastError();                                                                      \
-    }                                                                                                 \
   }
+
+#define PS_DEFINE_ALL_LAUNCHERS(NN) \
+  PS_DEFINE_LAUNCHERS(NN)             \
+  PS_DEFINE_STEP1D_LAUNCHERS(NN)      \
+  PS_DEFINE_LAST_LAUNCHERS(NN)        \
+  PS_DEFINE_MHD_LAUNCHERS(NN)
 
 // Launchers of the 1D-only pencil lengths: the whole-step kernel and the
 // contiguous operator (ps_derivative / ps_filter / 1D ps_rhs).
