@@ -109,3 +109,24 @@ def test_mixed_radix_descriptor_validation_without_device(built_lib):
     fake = C.c_void_p(256)  # never dereferenced: the call is refused first
     assert built_lib.ps_rhs_static(C.byref(desc), fake, fake, None) == 2
     assert b"powers of two" in built_lib.ps_last_error()
+
+
+def test_scratch_accounts_for_the_split_2d_right_hand_side(built_lib):
+    """From 256 rows (n[1]) the 2D Euler and MHD last pass is split and keeps
+    its right-hand side in a scratch buffer of 4 (Euler) or 8 (MHD) fields;
+    HBM admission reads these bytes.  Swapping the axes of a 256 x 128 grid
+    changes nothing else in the count."""
+    import ctypes as C
+    from phrike_gb300 import _lib
+    cells = 256 * 128
+    for eq, extra in ((_lib.PS_EQ_EULER, 4), (_lib.PS_EQ_MHD, 8)):
+        sizes = []
+        for nx, ny in ((256, 128), (128, 256)):
+            desc = _lib.PlanDesc()
+            assert built_lib.ps_plan_desc_init(C.byref(desc), 2) == 0
+            desc.equations = eq
+            desc.n[0], desc.n[1] = nx, ny
+            size = C.c_size_t()
+            assert built_lib.ps_batch_scratch_bytes(C.byref(desc), 2, C.byref(size)) == 0
+            sizes.append(size.value)
+        assert sizes[1] - sizes[0] == extra * cells * 4 * 2, (eq, sizes)
