@@ -35,6 +35,11 @@ struct ps_plan_s {
   // fields) and an elementwise kernel applies the RK stage and the clamp
   bool split2d = false;
   float* R2 = nullptr;
+  // 3D Euler with gravity: a second stage input (nc fields).  The last pass
+  // reads the stage input for the gravity source one component pair at a
+  // time while it writes the next stage input, so stages 1 and 2 must not
+  // share the buffer: stage 1 writes Us2, stage 2 reads it.
+  float* Us2 = nullptr;
   // per-solve device scalars
   float* speed = nullptr;  // CFL wave speed maxima
   float* eref = nullptr;   // E_ref of the energy-perturbation form

@@ -102,6 +102,14 @@ bool split2d_grid(const ps_plan_desc* d) {
 // Fields of the split 2D right-hand side buffer.
 int split2d_fields(const ps_plan_desc* d) { return d->equations == PS_EQ_MHD ? 8 : 4; }
 
+// 3D Fourier Euler with gravity on power-of-two axes keeps a second stage
+// input (plan.cuh Us2); the mixed-radix last pass reads every component of a
+// point before writing it and needs none.
+bool stage_buffer3d(const ps_plan_desc* d) {
+  return d->ndim == 3 && d->equations == PS_EQ_EULER && !is_lgl(d) && !is_mr(d) &&
+         (d->gravity[0] != 0.0 || d->gravity[1] != 0.0 || d->gravity[2] != 0.0);
+}
+
 int validate(const ps_plan_desc* d) {
   if (!d) return fail(PS_ERR_INVALID, "null descriptor");
   if (d->ndim < 1 || d->ndim > 3) return fail(PS_ERR_INVALID, "ndim must be 1, 2 or 3 (got %d)", d->ndim);
@@ -414,7 +422,7 @@ int ymid(ps_plan p, cudaStream_t s, const int* active) {
 }
 
 int last(ps_plan p, int stage, const float* Un, float* out, double dt, const double* d_dt, bool filter_last,
-         cudaStream_t s, const int* active) {
+         cudaStream_t s, const int* active, const float* stage_in = nullptr) {
   int rc;
   if (p->mr) {
     const int st_words = (stage < 0) ? 1 : (stage == 0) ? 3 : (stage == 3) ? 2 : 4;
@@ -529,7 +537,8 @@ int last(ps_plan p, int stage, const float* Un, float* out, double dt, const dou
   a.filter_last = filter_last ? 1 : 0;
   a.status = p->status;
   a.tcols = (p->nd == 2) ? p->tcols : 0;
-  a.Uin = (stage <= 0) ? Un : p->Us;  // the stage input: U^n at stage 0 and for a bare rhs
+  // the stage input: U^n at stage 0 and for a bare rhs
+  a.Uin = (stage_in != nullptr) ? stage_in : (stage <= 0) ? Un : p->Us;
   a.gravity = 0;
   for (int d = 0; d < p->nd && d < 3; ++d) {
     a.grav[d] = (float)p->desc.gravity[d];
@@ -674,7 +683,8 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
     const bool filt = filter_due(p, p->step_counter);
     for (int stage = 0; stage < 4; ++stage) {
       if (p->desc.scheme == PS_SCHEME_RK2 && (stage == 1 || stage == 2)) continue;  // midpoint RK2
-      const float* src = (stage == 0) ? U : p->Us;
+      // stage inputs U, Us, Us, Us (3D with gravity: U, Us, Us2, Us)
+      const float* src = (stage == 0) ? U : (stage == 2 && p->Us2 != nullptr) ? p->Us2 : p->Us;
       float* Uw = (stage == 0 && pending_px) ? U : nullptr;
       if (p->av_buf && (rc = av_prepass(p, src, s, act)) != PS_OK) return rc;
       if ((rc = xfirst(p, src, Uw, (cfl && stage == 0) ? p->speed : nullptr, s, false, act)) != PS_OK) return rc;
@@ -683,8 +693,8 @@ int steps_nd(ps_plan p, float* U, int nsteps, double dt, const double* d_dt, dou
         PS_CU(ps::launch_step_control(p->speed, p->desc.cfl, p->hmin(), d_t, d_tend, p->nsolve, p->dt, p->active, s),
               "step control");
       if (p->nd == 3 && (rc = ymid(p, s, act)) != PS_OK) return rc;
-      float* out = (stage < 3) ? p->Us : U;
-      if ((rc = last(p, stage, U, out, dt, dtp, filt && stage == 3, s, act)) != PS_OK) return rc;
+      float* out = (stage == 1 && p->Us2 != nullptr) ? p->Us2 : (stage < 3) ? p->Us : U;
+      if ((rc = last(p, stage, U, out, dt, dtp, filt && stage == 3, s, act, src)) != PS_OK) return rc;
     }
     pending_px = false;
     if (filt) {
@@ -1179,6 +1189,7 @@ int create(const ps_plan_desc* d, int nsolve, ps_plan* out) {
     if ((rc = dalloc(p, &p->Us, p->nc * c)) != PS_OK) return cleanup(rc);
     if (split2d_grid(d) && (rc = dalloc(p, &p->R2, split2d_fields(d) * c)) != PS_OK) return cleanup(rc);
     p->split2d = split2d_grid(d);
+    if (stage_buffer3d(d) && (rc = dalloc(p, &p->Us2, p->nc * c)) != PS_OK) return cleanup(rc);
   }
   p->av = av_params(d);
   if (p->nd == 2 && !lgl && !mr) {
@@ -1282,6 +1293,7 @@ int ps_batch_scratch_bytes(const ps_plan_desc* d, int nsolve, size_t* bytes) {
   size_t fields = scratch_fields(d->ndim, d->equations == PS_EQ_MHD);
   if (is_mr(d) && d->ndim == 1) fields += 6;  // stage input and increments
   if (split2d_grid(d)) fields += split2d_fields(d);  // the 2D right-hand side
+  if (stage_buffer3d(d)) fields += 5;                // the second 3D stage input
   if (d->av_mode != PS_AV_OFF && d->ndim == 2) fields += 21;
   const bool mhd = d->equations == PS_EQ_MHD;
   if (d->ndim == 1 && !mhd && d->n[0] >= 4096) fields += 6;  // global U^n and accumulator

@@ -49,6 +49,31 @@ def test_gravity_2d_3d_match_reference(cuda_device):
     assert max(_errs(T.cpu().numpy(), z["grav3d_U"])) < 2e-5
 
 
+def test_gravity_3d_strong_field_vs_oracle(cuda_device):
+    """3D gravity at g = (5, -10, 3), 20 steps of dt = 1e-2, against the
+    oracle.  The last pass reads the stage input for the gravity source one
+    component pair at a time while it writes the next stage input, so stages
+    1 and 2 take their inputs and outputs from different buffers; sharing one
+    would feed the y/z-momentum and energy sources partly updated values
+    (the energy 2.5e-4 off here, the momentum 1.1e-5, by the oracle with that
+    mistake planted)."""
+    from oracle import spectral as O
+    from phrike_gb300.engine import Plan
+    n, g, dt, steps = 16, [5.0, -10.0, 3.0], 1e-2, 20
+    U0 = problems.taylor_green_3d(n)
+    s = O.EulerSolver(O.FourierBox((n, n, n), (2 * np.pi,) * 3, dealias=True), cfl=0.25, gravity=g)
+    R = U0.astype(np.float32).astype(np.float64)
+    for _ in range(steps):
+        R = s.step(R, dt)
+    p = Plan((n, n, n), (2 * np.pi,) * 3, gravity=g)
+    U = _dev(U0)
+    p.run_(U, steps, dt)
+    e = _errs(U.cpu().numpy(), R)
+    print(f"\n3D gravity (5, -10, 3), {steps} steps of {dt}: rho {e[0]:.2e} mom {e[1]:.2e} E {e[2]:.2e}")
+    assert e[0] < 1e-6 and e[1] < 1e-6 and e[2] < 1e-6, e  # measured 1.2e-7, 2.0e-7, 3.4e-8
+    assert p.status() == 0
+
+
 def test_gravity_lgl_vs_oracle(cuda_device):
     from phrike_gb300.engine import Plan
     n = 33
