@@ -130,3 +130,22 @@ def test_scratch_accounts_for_the_split_2d_right_hand_side(built_lib):
             assert built_lib.ps_batch_scratch_bytes(C.byref(desc), 2, C.byref(size)) == 0
             sizes.append(size.value)
         assert sizes[1] - sizes[0] == extra * cells * 4 * 2, (eq, sizes)
+
+
+def test_scratch_accounts_for_the_second_3d_stage_input(built_lib):
+    """3D Euler with gravity keeps a second 5-field stage input (stages 1 and
+    2 must not read and write one buffer); mixed-radix 3D plans need none."""
+    import ctypes as C
+    from phrike_gb300 import _lib
+
+    def size(n, grav):
+        desc = _lib.PlanDesc()
+        assert built_lib.ps_plan_desc_init(C.byref(desc), 3) == 0
+        desc.n[0] = desc.n[1] = desc.n[2] = n
+        desc.gravity[2] = grav
+        out = C.c_size_t()
+        assert built_lib.ps_batch_scratch_bytes(C.byref(desc), 3, C.byref(out)) == 0
+        return out.value
+
+    assert size(32, -1.0) - size(32, 0.0) == 5 * 32 ** 3 * 4 * 3
+    assert size(48, -1.0) == size(48, 0.0)
